@@ -1,0 +1,448 @@
+#!/usr/bin/env python3
+"""Benchmark of the complex-baseband filtering path on GB300 — one JSON line on stdout.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload fir1025|fir63|pfb64]
+
+A step is one pass of the hot path over one batch of synthetic input: by default the long FIR
+(2^24 cf32 samples = 8 tones over 60 dB + AWGN at 10 dB SNR, 1025 Kaiser-windowed-sinc taps),
+the workload the headline metric (Msamples/s, FIR 1025 taps) is quoted on.
+
+Timing: W untimed steps, then exactly K steps between a barrier + device synchronize on both
+sides, measured with CUDA events on the launching stream; max over ranks. Two input/output
+buffer pairs alternate, so each step touches 536 MB (more than the 129 MB L2) and nothing is
+served from L2 across steps. `value` = all ranks' samples / time; `e2e` = the same metric
+through rfx_fir_host (pinned host buffers, upload + compute + download per step).
+
+--impl reference: the oracle's float64 restatement of the project's tools/reference.py FIR,
+threaded over every host core, on a bounded sample of the same workload (rank 0 only).
+
+Under torchrun with N > 1 every rank runs its own replica of the workload (the path needs no
+exchange between GPUs): weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "gpu-rf-pipeline_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Msamples/s (FIR 1025 taps, 64-ch PFB) tensor-core vs FP32, rel err <=2e-6"
+L2_BYTES = 129 * 1024 * 1024
+
+
+# --- distributed plumbing (one process per GPU under torchrun) ----------------------------
+
+def dist_env() -> tuple[int, int, int]:
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def init_dist(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(value: float, dist, device=None) -> float:
+    """Max of a float over all ranks (the timing reduction; no data-path collective)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist, device=None) -> None:
+    if dist is not None:
+        if device is not None and device.type == "cuda":
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+# --- clocks during the timed region ---------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi -lms 200 in the background; median SM clock while the GPU was busy."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int) -> None:
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self) -> None:
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc) -> None:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread is not None:
+                self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        rows = []
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append({"sm": float(parts[1]), "max": float(parts[2]),
+                             "util": float(parts[4]),
+                             "reasons": [name for name, v in zip(
+                                 ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                  "sw_power_cap"], parts[5:9]) if v.lower() == "active"]})
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        busy = [r for r in rows if r["util"] > 0] or rows
+        reasons = sorted({x for r in busy for x in r["reasons"]})
+        return {"sm_mhz": statistics.median(r["sm"] for r in busy),
+                "sm_max_mhz": max(r["max"] for r in rows), "reasons": reasons,
+                "samples": len(busy)}
+
+
+# --- the workloads ---------------------------------------------------------------------------
+
+def load_workload(name: str):
+    from rfx import signals
+
+    if name == "fir1025":
+        return signals.long_fir(1 << 24)
+    if name == "fir63":
+        return signals.plain_fir(1 << 24)
+    if name == "pfb64":
+        return signals.channelizer64(1 << 24)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "source": "fallback"}
+
+
+def pick_fir_impl(rfx, x, h, y) -> str:
+    """The tensor-core form when this library has it, else the plain kernel."""
+    try:
+        rfx.fir_launch("tc_split", x, h, y)
+        return "tc_split"
+    except rfx.RfxError as e:
+        if e.status == 4 and "not supported" in str(e):
+            return "plain"
+        raise
+
+
+def time_device(launch, steps: int, warmup: int, dist, device) -> float:
+    """Seconds for `steps` launches: barrier + synchronize on both sides, CUDA events on the
+    current stream, max over ranks."""
+    import torch
+
+    for i in range(warmup):
+        launch(i)
+    torch.cuda.synchronize()
+    barrier(dist, device)
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for i in range(steps):
+        launch(i)
+    stop.record()
+    torch.cuda.synchronize()
+    barrier(dist, device)
+    elapsed = start.elapsed_time(stop) / 1e3
+    return max_over_ranks(elapsed, dist, device)
+
+
+def kernel_average_s(launch, count: int) -> float:
+    """Average duration of one launch, CUDA events on the launching stream, after the timed
+    region (for the roofline)."""
+    import torch
+
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for i in range(count):
+        launch(i)
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3 / count
+
+
+def cpu_fir_baseline(x: np.ndarray, h: np.ndarray, target_s: float = 2.0) -> dict:
+    """The oracle's float64 FIR on all host cores over a growing prefix of the workload, until
+    one pass takes at least target_s."""
+    from oracle import rf_oracle as orc
+
+    threads = os.cpu_count() or 1
+    n = 1 << 14
+    while True:
+        n = min(n, x.size)
+        t0 = time.perf_counter()
+        orc.fir_fast(x[:n], h, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n == x.size:
+            break
+        n *= 2
+    return {"value": n / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} samples of the workload, {h.size} taps, float64, "
+                      f"{dt:.2f} s on {threads} threads"}
+
+
+def cpu_chan_baseline(x: np.ndarray, h: np.ndarray, m: int, target_s: float = 2.0) -> dict:
+    from oracle import rf_oracle as orc
+
+    threads = os.cpu_count() or 1
+    n = 1 << 14
+    while True:
+        n = min(n, x.size)
+        t0 = time.perf_counter()
+        orc.channelize_fast(x[:n], h, m, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n == x.size:
+            break
+        n *= 2
+    return {"value": n / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} samples of the workload, M={m}, {h.size} taps, float64, "
+                      f"{dt:.2f} s on {threads} threads"}
+
+
+# --- the reference arm -------------------------------------------------------------------------
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    w = load_workload(args.workload)
+    times = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        if w.channels:
+            b = cpu_chan_baseline(w.x, w.taps, w.channels, target_s=1.0)
+        else:
+            b = cpu_fir_baseline(w.x, w.taps, target_s=1.0)
+        if i >= args.warmup:
+            times.append(b["value"])
+            base = b
+    value = statistics.median(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "samples": int(w.x.size), "taps": int(w.taps.size),
+                   "channels": w.channels or None, "l2": "n/a (CPU)"},
+        "cpu_baseline": {**base, "value": value},
+        "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --- our arm ---------------------------------------------------------------------------------
+
+def run_ours(args) -> None:
+    import torch
+
+    import rfx
+    from oracle import rf_oracle as orc
+
+    rank, world, local = dist_env()
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    dist = init_dist(world, "nccl")
+    rfx.load()
+
+    w = load_workload(args.workload)
+    n = int(w.x.size)
+    xs = [torch.from_numpy(w.x).to(device) for _ in range(2)]
+    h = torch.from_numpy(w.taps).to(device)
+    pk = peaks()
+    launches_per_step = 1
+    extras: dict = {}
+
+    if w.channels:
+        m = w.channels
+        frames = rfx.frames(n, m)
+        outs = [torch.empty((frames, m), dtype=torch.complex64, device=device) for _ in range(2)]
+        impl = "plain"
+        plan = rfx.ChanPlan(m, n, impl)
+        launches_per_step = 2  # branch kernel + the cuFFT inverse transform
+
+        def launch(i: int) -> None:
+            plan.launch(xs[i % 2], h, outs[i % 2])
+
+        dtype = "f32"
+    else:
+        ys = [torch.empty_like(xs[0]) for _ in range(2)]
+        impl = pick_fir_impl(rfx, xs[0], h, ys[0])
+
+        def launch(i: int) -> None:
+            rfx.fir_launch(impl, xs[i % 2], h, ys[i % 2])
+
+        dtype = "f16x3->f32" if impl == "tc_split" else "f32"
+
+    with ClockSampler(device.index if device.index is not None else 0) as clocks:
+        seconds = time_device(launch, args.steps, args.warmup, dist, device)
+    kernel_s = kernel_average_s(launch, max(3, min(args.steps, 10)))
+    value = world * n / seconds / 1e6
+
+    # Accuracy of this run's output against the float64 oracle, on a prefix (rank 0).
+    err = None
+    if rank == 0:
+        check_n = min(n, 1 << 18)
+        if w.channels:
+            got = outs[0].reshape(-1)[: (check_n // w.channels) * w.channels].cpu().numpy()
+            ref = orc.channelize_fast(w.x[:check_n], w.taps, w.channels).reshape(-1)
+            err = orc.normwise_error(got, ref[: got.size])
+        else:
+            launch(0)
+            torch.cuda.synchronize()
+            got = ys[0][:check_n].cpu().numpy()
+            err = orc.normwise_error(got, orc.fir_fast(w.x[:check_n], w.taps))
+
+    # Roofline of the dominant kernel.
+    algo_bytes = 16.0 * n  # 8 B read + 8 B written per sample
+    achieved_gbs = algo_bytes / kernel_s / 1e9
+    flops = 4.0 * n * (w.taps.size if not w.channels else
+                       (-(-w.taps.size // w.channels)))  # useful FIR / branch flops
+    if impl == "tc_split":
+        roofline = {"bound": "tensor", "achieved": flops / kernel_s / 1e12,
+                    "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                    "frac": flops / kernel_s / 1e12 / pk["bf16_tflops"], "traffic": None}
+    else:
+        roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"],
+                    "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None}
+    roofline["peak_source"] = pk["source"]
+    if not w.channels:
+        sm_mhz = clocks.summary().get("sm_mhz") or 1900.0
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        extras["fp32_simt"] = {"achieved_tflops": flops / kernel_s / 1e12,
+                               "peak_tflops_at_sampled_clock": fp32_peak,
+                               "frac": flops / kernel_s / 1e12 / fp32_peak}
+
+    # End to end through the public host-buffer call, pinned host memory.
+    e2e = None
+    if rank == 0:
+        xp = torch.from_numpy(w.x).pin_memory()
+        if w.channels:
+            zp = torch.empty(rfx.frames(n, w.channels) * w.channels, dtype=torch.complex64
+                             ).pin_memory()
+            b = rfx.Bench(warmup=args.warmup, runs=args.steps)
+            lib = rfx.load()
+            rfx._check(lib.rfx_channelize_host(rfx.parse_chan_impl(impl), xp.data_ptr(), n,
+                                               w.taps.ctypes.data, w.taps.size, w.channels,
+                                               zp.data_ptr(), rfx.ctypes.byref(b)))
+            d2h = zp.numel() * 8
+        else:
+            yp = torch.empty_like(xp).pin_memory()
+            b = rfx.Bench(warmup=args.warmup, runs=args.steps)
+            lib = rfx.load()
+            rfx._check(lib.rfx_fir_host(rfx.parse_fir_impl(impl), xp.data_ptr(), n,
+                                        w.taps.ctypes.data, w.taps.size, 256, yp.data_ptr(),
+                                        rfx.ctypes.byref(b)))
+            d2h = n * 8
+        step_ms = b.h2d_ms_mean + b.kernel_ms_mean + b.d2h_ms_mean
+        e2e = {"value": n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
+               "h2d_bytes_per_step": n * 8 + w.taps.size * 4, "d2h_bytes_per_step": d2h,
+               "h2d_ms": b.h2d_ms_mean, "kernel_ms": b.kernel_ms_mean, "d2h_ms": b.d2h_ms_mean}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = (cpu_chan_baseline(w.x, w.taps, w.channels) if w.channels
+               else cpu_fir_baseline(w.x, w.taps))
+
+    fault = rfx.device_fault()
+    if fault:
+        raise SystemExit(f"a kernel recorded fault code {fault:#x}")
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": seconds / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": {"workload": w.name, "impl": impl, "samples": n,
+                       "taps": int(w.taps.size), "channels": w.channels or None,
+                       "l2": "inputs larger than L2: two 268 MB buffer sets alternate",
+                       "seed": w.meta.get("seed")},
+            "max_rel_err_vs_f64": err,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clocks.summary(),
+            "gpu_launches": args.steps * launches_per_step,
+            **extras,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="fir1025", choices=["fir1025", "fir63", "pfb64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

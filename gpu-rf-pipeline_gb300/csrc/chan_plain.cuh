@@ -1,0 +1,12 @@
+// Plain channelizer branch-sum kernel (chan_plain.cu): internal launch interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace rfx {
+
+// u (frames * channels cf32, frame-major) = the polyphase branch sums of x.
+cudaError_t chan_branch_launch(const void* x, const float* taps, void* u, long long frames,
+                               int channels, int num_taps, cudaStream_t stream);
+
+}  // namespace rfx

@@ -1,0 +1,301 @@
+// Plain FP32 FIR for sm_103a.
+//
+//   y[n] = sum_{k=0}^{K-1} h[k] x[n-k],  x[m] = 0 for m < 0,  n < N      (src/fir.cu:1-5)
+//
+// Arithmetic: every output is one chain of fused multiply-adds over k = 0, 1, ..., K-1 starting
+// from +0.0f, separately for I and Q. That is the order of the project's naive, tiled and
+// register kernels (src/fir.cu:35-40, :377-395), so the results are bit-identical to theirs.
+// Taps past the start of the input multiply zeros, which leaves the chain unchanged.
+//
+// Work decomposition: a block of 256 threads owns a tile of 2304 consecutive outputs; thread t
+// owns outputs t0 + 9t ... t0 + 9t + 8. Nine (odd) outputs per thread put the 64-bit shared
+// loads of a warp (stride 72 bytes) on distinct bank pairs.
+//
+// Staging: the tile's samples x[t0 - (K-1) .. t0 + 2303] (start rounded down to an even index so
+// the copy is 16-byte aligned) arrive in shared memory through ONE bulk copy on the TMA engine,
+// completed on an mbarrier; tiles that touch either end of the input are filled by the threads
+// with zeros outside [0, N). Results go back through shared memory and one bulk store.
+//
+// Inner loop: taps are taken nine at a time. For taps 9g .. 9g+8 a thread needs the 17 samples
+// x[n0 - 9g - 8 .. n0 - 9g + 8] (n0 = its first output), i.e. the sample blocks
+// S_g = x[n0 - 9g .. +8] and S_{g+1}. Two register blocks alternate between those roles, so
+// sliding the window costs nine 64-bit loads per nine taps and no register moves. Each
+// tap-sample product is one packed fma.rn.f32x2 on (I, Q) with the tap duplicated in both lanes.
+#include "fir_plain.cuh"
+#include "ptx.cuh"
+
+#include <cuda_runtime.h>
+
+namespace rfx {
+
+static __device__ unsigned int g_fault_fir_plain;
+
+namespace {
+
+constexpr int kThreads = kPlainThreads;
+constexpr int kR = kPlainOutputsPerThread;
+constexpr int kTile = kPlainTileOutputs;
+constexpr int kGuard = 16;  // zero samples in front of the tile: the last window block may
+                            // reach up to 10 samples before it (those values are never used)
+
+struct Layout {
+    uint32_t taps_off;   // (h, h) pairs, K entries
+    uint32_t tile_off;   // guard + tile samples
+    uint32_t bytes;
+};
+
+__host__ __device__ inline Layout plain_layout(int num_taps)
+{
+    Layout l;
+    l.taps_off = 16;
+    l.tile_off = (l.taps_off + 8u * static_cast<uint32_t>(num_taps) + 15u) & ~15u;
+    const uint32_t tile_samples = kGuard + kTile + static_cast<uint32_t>(num_taps) + 2u;
+    l.bytes = l.tile_off + 8u * tile_samples;
+    return l;
+}
+
+// Nine taps 9g + q (q < nq) against output window blocks: cur = S_g, nxt = S_{g+1}.
+__device__ __forceinline__ void tap_group(f32x2 (&acc)[kR], const f32x2 (&cur)[kR],
+                                          const f32x2 (&nxt)[kR], const f32x2* taps2, int k0,
+                                          int nq)
+{
+#pragma unroll
+    for (int q = 0; q < kR; ++q) {
+        if (q < nq) {
+            const f32x2 h = taps2[k0 + q];
+#pragma unroll
+            for (int j = 0; j < kR; ++j) {
+                acc[j] = fma2(h, j >= q ? cur[j - q] : nxt[kR + j - q], acc[j]);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void load_block(f32x2 (&blk)[kR], const f32x2* tile, int p, int m)
+{
+    // S_m[i] = x[n0 - 9m + i] = tile[p - 9m + i]
+    const f32x2* src = tile + (p - kR * m);
+#pragma unroll
+    for (int i = 0; i < kR; ++i) {
+        blk[i] = src[i];
+    }
+}
+
+// Computes this thread's nine outputs of the tile staged at `tile` (tile[i] = x[base + i]).
+__device__ __forceinline__ void compute_outputs(f32x2 (&acc)[kR], const f32x2* tile,
+                                                const f32x2* taps2, int p, int num_taps)
+{
+#pragma unroll
+    for (int j = 0; j < kR; ++j) {
+        acc[j] = 0ull;  // +0.0f, +0.0f
+    }
+    const int groups = num_taps / kR;
+    const int rem = num_taps - groups * kR;
+    f32x2 a[kR];
+    f32x2 b[kR];
+    load_block(a, tile, p, 0);
+    int g = 0;
+    for (; g + 2 <= groups; g += 2) {
+        load_block(b, tile, p, g + 1);
+        tap_group(acc, a, b, taps2, kR * g, kR);
+        load_block(a, tile, p, g + 2);
+        tap_group(acc, b, a, taps2, kR * (g + 1), kR);
+    }
+    if (g < groups) {
+        load_block(b, tile, p, g + 1);
+        tap_group(acc, a, b, taps2, kR * g, kR);
+        if (rem > 0) {
+            load_block(a, tile, p, g + 2);
+            tap_group(acc, b, a, taps2, kR * (g + 1), rem);
+        }
+    } else if (rem > 0) {
+        load_block(b, tile, p, g + 1);
+        tap_group(acc, a, b, taps2, kR * g, rem);
+    }
+}
+
+}  // namespace
+
+// One tile of one capture. Shared by the single-capture and the batched kernels.
+__device__ __forceinline__ void fir_plain_tile(const float2* __restrict__ x,
+                                               const float* __restrict__ taps,
+                                               float2* __restrict__ y, long long n,
+                                               int num_taps, long long tile_index,
+                                               unsigned char* smem)
+{
+    const Layout lay = plain_layout(num_taps);
+    const uint32_t sbase = smem_u32(smem);
+    const uint32_t bar = sbase;  // mbarrier at offset 0
+    f32x2* taps2 = reinterpret_cast<f32x2*>(smem + lay.taps_off);
+    f32x2* guard = reinterpret_cast<f32x2*>(smem + lay.tile_off);
+    f32x2* tile = guard + kGuard;
+    const int tid = threadIdx.x;
+
+    const long long t0 = tile_index * kTile;
+    const long long base = (t0 - (num_taps - 1)) & ~1ll;      // even: 16-byte aligned copy
+    const int tile_len = static_cast<int>(t0 + kTile - base); // even
+    const bool interior = base >= 0 && t0 + kTile <= n;
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (interior && tid == 0) {
+        const uint32_t bytes = 8u * static_cast<uint32_t>(tile_len);
+        mbar_arrive_expect_tx(bar, bytes);
+        bulk_g2s(smem_u32(tile), x + base, bytes, bar);
+    }
+    // Taps (duplicated into both lanes) and the guard while the copy is in flight.
+    for (int k = tid; k < num_taps; k += kThreads) {
+        const float h = __ldg(taps + k);
+        taps2[k] = pack2(h, h);
+    }
+    if (tid < kGuard) {
+        guard[tid] = 0ull;
+    }
+    if (!interior) {
+        for (int i = tid; i < tile_len; i += kThreads) {
+            const long long m = base + i;
+            f32x2 v = 0ull;
+            if (m >= 0 && m < n) {
+                const float2 s = x[m];
+                v = pack2(s.x, s.y);
+            }
+            tile[i] = v;
+        }
+    }
+    __syncthreads();
+    bool ok = true;
+    if (interior) {
+        ok = mbar_wait_bounded(bar, 0, &g_fault_fir_plain, kFaultTileLoad, nullptr);
+    }
+
+    const long long n0 = t0 + static_cast<long long>(kR) * tid;
+    f32x2 acc[kR];
+    if (ok && n0 < n) {
+        compute_outputs(acc, tile, taps2, static_cast<int>(n0 - base), num_taps);
+    }
+    __syncthreads();  // every thread is done reading the tile: reuse it for the results
+    if (ok && n0 < n) {
+#pragma unroll
+        for (int j = 0; j < kR; ++j) {
+            tile[kR * tid + j] = acc[j];
+        }
+    }
+    if (interior) {
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (!ok) {
+        return;
+    }
+    if (interior) {
+        if (tid == 0) {
+            bulk_s2g(y + t0, smem_u32(tile), 8u * kTile);
+            bulk_commit();
+            bulk_wait_read_all();
+        }
+    } else {
+        const long long valid = n - t0 < kTile ? n - t0 : kTile;
+        for (int i = tid; i < valid; i += kThreads) {
+            const float2 v = unpack2(tile[i]);
+            y[t0 + i] = v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 3)
+fir_plain_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
+                 float2* __restrict__ y, long long n, int num_taps)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    fir_plain_tile(x, taps, y, n, num_taps, blockIdx.x, smem);
+}
+
+// Several captures sharing one tap set: blockIdx.y picks the capture; blocks past a shorter
+// capture's end return at once (as the project's batched kernels, src/fused.cu:141-162).
+__global__ void __launch_bounds__(kThreads, 3)
+fir_plain_batched_kernel(PlainBatch batch, const float* __restrict__ taps, int num_taps)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int c = blockIdx.y;
+    const long long n = batch.num_samples[c];
+    if (static_cast<long long>(blockIdx.x) * kTile >= n) {
+        return;
+    }
+    fir_plain_tile(static_cast<const float2*>(batch.x[c]), taps, static_cast<float2*>(batch.y[c]),
+                   n, num_taps, blockIdx.x, smem);
+}
+
+size_t fir_plain_smem_bytes(int num_taps) { return plain_layout(num_taps).bytes; }
+
+static cudaError_t ensure_smem_attr(const void* fn, size_t bytes)
+{
+    // The opt-in limit only has to be raised once per function and size class; raising it to
+    // the device maximum once covers every tap count.
+    if (bytes <= 48 * 1024) {
+        return cudaSuccess;
+    }
+    int device = 0;
+    cudaError_t err = cudaGetDevice(&device);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    int optin = 0;
+    err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
+cudaError_t fir_plain_launch(const void* x, const float* taps, void* y, long long n,
+                             int num_taps, cudaStream_t stream)
+{
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    const size_t bytes = fir_plain_smem_bytes(num_taps);
+    cudaError_t err = ensure_smem_attr(reinterpret_cast<const void*>(fir_plain_kernel), bytes);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    const long long tiles = (n + kTile - 1) / kTile;
+    fir_plain_kernel<<<static_cast<unsigned>(tiles), kThreads, bytes, stream>>>(
+        static_cast<const float2*>(x), taps, static_cast<float2*>(y), n, num_taps);
+    return cudaGetLastError();
+}
+
+cudaError_t fir_plain_batched_launch(const PlainBatch& batch, int count, const float* taps,
+                                     int num_taps, cudaStream_t stream)
+{
+    long long longest = 0;
+    for (int c = 0; c < count; ++c) {
+        longest = batch.num_samples[c] > longest ? batch.num_samples[c] : longest;
+    }
+    if (longest == 0) {
+        return cudaSuccess;
+    }
+    const size_t bytes = fir_plain_smem_bytes(num_taps);
+    cudaError_t err =
+        ensure_smem_attr(reinterpret_cast<const void*>(fir_plain_batched_kernel), bytes);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    const dim3 grid(static_cast<unsigned>((longest + kTile - 1) / kTile), count);
+    fir_plain_batched_kernel<<<grid, kThreads, bytes, stream>>>(batch, taps, num_taps);
+    return cudaGetLastError();
+}
+
+cudaError_t fir_plain_take_fault(unsigned int* code)
+{
+    unsigned int zero = 0;
+    cudaError_t err = cudaMemcpyFromSymbol(code, g_fault_fir_plain, sizeof(unsigned int));
+    if (err != cudaSuccess) {
+        return err;
+    }
+    return cudaMemcpyToSymbol(g_fault_fir_plain, &zero, sizeof(unsigned int));
+}
+
+}  // namespace rfx

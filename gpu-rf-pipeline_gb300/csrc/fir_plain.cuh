@@ -1,0 +1,29 @@
+// Plain FP32 FIR kernels (fir_plain.cu): internal launch interface used by the C ABI.
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+
+namespace rfx {
+
+constexpr int kPlainThreads = 256;
+constexpr int kPlainOutputsPerThread = 9;
+constexpr int kPlainTileOutputs = kPlainThreads * kPlainOutputsPerThread;  // 2304
+constexpr int kMaxTaps = 8192;  // the project's constant-bank capacity (src/fir.cu:208)
+
+// Captures sharing one tap set, passed by value as one kernel argument (64 * 24 bytes).
+constexpr int kPlainBatchMax = 64;
+struct PlainBatch {
+    const void* x[kPlainBatchMax];
+    void* y[kPlainBatchMax];
+    long long num_samples[kPlainBatchMax];
+};
+
+size_t fir_plain_smem_bytes(int num_taps);
+cudaError_t fir_plain_launch(const void* x, const float* taps, void* y, long long n,
+                             int num_taps, cudaStream_t stream);
+cudaError_t fir_plain_batched_launch(const PlainBatch& batch, int count, const float* taps,
+                                     int num_taps, cudaStream_t stream);
+cudaError_t fir_plain_take_fault(unsigned int* code);
+
+}  // namespace rfx

@@ -1,0 +1,30 @@
+// Tensor-core FIR (fir_tc.cu) and the per-capture batch (fir_batch.cu): internal interface.
+#pragma once
+
+#include "rfx.h"
+
+#include <cuda_runtime.h>
+
+namespace rfx {
+
+// Tile shape of the tensor-core FIR, chosen by the tuner.
+struct TcConfig {
+    int tile_blocks;  // 128-output blocks per tile (the GEMM's N is twice this: I and Q)
+    int stages;       // operand ring depth
+};
+
+constexpr int kTcBatchMax = 4096;
+
+// Whether the tensor-core kernel takes this tap count. One tap is an exact elementwise scale,
+// which the plain kernel computes exactly; the split form would round it.
+bool fir_tc_supported(int num_taps);
+
+cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n, int num_taps,
+                          TcConfig config, cudaStream_t stream);
+cudaError_t fir_tc_take_fault(unsigned int* code);
+
+// Per-capture-taps batch in one launch.
+cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
+                             cudaStream_t stream);
+
+}  // namespace rfx

@@ -1,0 +1,636 @@
+// The C ABI of librfx.so (include/rfx.h): argument checks, implementation dispatch, channelizer
+// plans, host-buffer operations with phase timing, and the fault word readout.
+#include "rfx.h"
+
+#include "chan_plain.cuh"
+#include "fir_plain.cuh"
+#include "fir_tc.cuh"
+#include "tuning.hpp"
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+int cuda_fail(cudaError_t err, const char* what)
+{
+    return fail(RFX_ERR_CUDA, "CUDA error: %s (code %d) in %s", cudaGetErrorString(err),
+                static_cast<int>(err), what);
+}
+
+const char* cufft_text(cufftResult r)
+{
+    switch (r) {
+    case CUFFT_SUCCESS: return "CUFFT_SUCCESS";
+    case CUFFT_INVALID_PLAN: return "CUFFT_INVALID_PLAN";
+    case CUFFT_ALLOC_FAILED: return "CUFFT_ALLOC_FAILED";
+    case CUFFT_INVALID_TYPE: return "CUFFT_INVALID_TYPE";
+    case CUFFT_INVALID_VALUE: return "CUFFT_INVALID_VALUE";
+    case CUFFT_INTERNAL_ERROR: return "CUFFT_INTERNAL_ERROR";
+    case CUFFT_EXEC_FAILED: return "CUFFT_EXEC_FAILED";
+    case CUFFT_SETUP_FAILED: return "CUFFT_SETUP_FAILED";
+    case CUFFT_INVALID_SIZE: return "CUFFT_INVALID_SIZE";
+    case CUFFT_UNALIGNED_DATA: return "CUFFT_UNALIGNED_DATA";
+    default: return "cuFFT error";
+    }
+}
+
+int cufft_fail(cufftResult r, const char* what)
+{
+    return fail(RFX_ERR_CUDA, "cuFFT error: %s (code %d) in %s", cufft_text(r),
+                static_cast<int>(r), what);
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+constexpr int64_t kMaxSamples = INT32_MAX;
+
+const char* const kFirImplNames[] = {"plain", "tc_split", "auto"};
+const char* const kChanImplNames[] = {"plain", "tc_split", "auto"};
+
+int check_fir_args(int impl, const void* x, const float* taps, const void* y, int64_t n,
+                   int num_taps)
+{
+    if (impl < RFX_FIR_PLAIN || impl > RFX_FIR_AUTO) {
+        return fail(RFX_ERR_INVALID, "fir: unknown implementation %d", impl);
+    }
+    if (n < 0 || n > kMaxSamples) {
+        return fail(RFX_ERR_INVALID, "fir: %lld samples, expected 0 to %lld",
+                    static_cast<long long>(n), static_cast<long long>(kMaxSamples));
+    }
+    if (num_taps < 1) {
+        return fail(RFX_ERR_INVALID, "fir: need at least one tap");
+    }
+    if (num_taps > rfx::kMaxTaps) {
+        return fail(RFX_ERR_CAPACITY, "fir: %d taps, more than the %d supported", num_taps,
+                    rfx::kMaxTaps);
+    }
+    if (n > 0 && (x == nullptr || y == nullptr || taps == nullptr)) {
+        return fail(RFX_ERR_INVALID, "fir: null pointer");
+    }
+    if (n > 0 && (!aligned16(x) || !aligned16(y))) {
+        return fail(RFX_ERR_ALIGNMENT, "fir: sample buffers must be 16-byte aligned");
+    }
+    if (n > 0 && (reinterpret_cast<uintptr_t>(taps) & 3u) != 0) {
+        return fail(RFX_ERR_ALIGNMENT, "fir: taps must be 4-byte aligned");
+    }
+    return RFX_OK;
+}
+
+// Resolves RFX_FIR_AUTO and the cases the tensor-core kernel hands to the plain one.
+int resolve_fir_impl(int impl, int num_taps, int64_t n)
+{
+    if (impl == RFX_FIR_AUTO) {
+        impl = rfx::tuned_fir_impl(num_taps, n);
+    }
+    if (impl == RFX_FIR_TC && !rfx::fir_tc_supported(num_taps)) {
+        impl = RFX_FIR_PLAIN;  // one tap: an exact elementwise scale, see fir_tc_supported
+    }
+    return impl;
+}
+
+int launch_fir(int impl, const void* x, const float* taps, void* y, int64_t n, int num_taps,
+               cudaStream_t stream)
+{
+    cudaError_t err;
+    if (impl == RFX_FIR_TC) {
+        err = rfx::fir_tc_launch(x, taps, y, n, num_taps, rfx::tuned_fir_tc_config(num_taps, n),
+                                 stream);
+        return err == cudaSuccess ? RFX_OK : cuda_fail(err, "fir_tc_launch");
+    }
+    err = rfx::fir_plain_launch(x, taps, y, n, num_taps, stream);
+    return err == cudaSuccess ? RFX_OK : cuda_fail(err, "fir_plain_launch");
+}
+
+}  // namespace
+
+struct rfx_chan_plan {
+    int impl;
+    int channels;
+    int64_t frames;       // cuFFT batch (plain); maximum frames (tensor core)
+    cufftHandle fft;
+    bool has_fft;
+};
+
+extern "C" {
+
+const char* rfx_last_error(void) { return g_last_error.c_str(); }
+
+const char* rfx_version(void) { return "rfx 0.1.0 sm_103a"; }
+
+int rfx_device_fault(unsigned int* code)
+{
+    if (code == nullptr) {
+        return fail(RFX_ERR_INVALID, "rfx_device_fault: null pointer");
+    }
+    cudaError_t err = cudaDeviceSynchronize();
+    if (err != cudaSuccess) {
+        return cuda_fail(err, "cudaDeviceSynchronize");
+    }
+    unsigned int total = 0;
+    unsigned int part = 0;
+    if ((err = rfx::fir_plain_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "fir_plain fault word");
+    }
+    total |= part;
+    part = 0;
+    if ((err = rfx::fir_tc_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "fir_tc fault word");
+    }
+    total |= part;
+    *code = total;
+    return RFX_OK;
+}
+
+int rfx_fir_impl_name(int index, char* name, size_t size)
+{
+    if (index < 0 || index >= 3 || name == nullptr || size == 0) {
+        return RFX_ERR_INVALID;
+    }
+    std::snprintf(name, size, "%s", kFirImplNames[index]);
+    return RFX_OK;
+}
+
+int rfx_chan_impl_name(int index, char* name, size_t size)
+{
+    if (index < 0 || index >= 3 || name == nullptr || size == 0) {
+        return RFX_ERR_INVALID;
+    }
+    std::snprintf(name, size, "%s", kChanImplNames[index]);
+    return RFX_OK;
+}
+
+int rfx_parse_fir_impl(const char* name, int* impl)
+{
+    if (name == nullptr || impl == nullptr) {
+        return fail(RFX_ERR_INVALID, "rfx_parse_fir_impl: null pointer");
+    }
+    static const struct {
+        const char* name;
+        int impl;
+    } table[] = {{"plain", RFX_FIR_PLAIN}, {"tc_split", RFX_FIR_TC}, {"auto", RFX_FIR_AUTO},
+                 {"naive", RFX_FIR_PLAIN}, {"tiled", RFX_FIR_PLAIN},
+                 {"tiled_const", RFX_FIR_PLAIN}, {"register", RFX_FIR_PLAIN}};
+    for (const auto& row : table) {
+        if (std::strcmp(name, row.name) == 0) {
+            *impl = row.impl;
+            return RFX_OK;
+        }
+    }
+    return fail(RFX_ERR_INVALID, "unknown fir implementation '%s'", name);
+}
+
+int rfx_parse_chan_impl(const char* name, int* impl)
+{
+    if (name == nullptr || impl == nullptr) {
+        return fail(RFX_ERR_INVALID, "rfx_parse_chan_impl: null pointer");
+    }
+    for (int i = 0; i < 3; ++i) {
+        if (std::strcmp(name, kChanImplNames[i]) == 0) {
+            *impl = i;
+            return RFX_OK;
+        }
+    }
+    if (std::strcmp(name, "polyphase") == 0) {  // the project's report name for its one impl
+        *impl = RFX_CHAN_PLAIN;
+        return RFX_OK;
+    }
+    return fail(RFX_ERR_INVALID, "unknown channelize implementation '%s'", name);
+}
+
+// ---- FIR ---------------------------------------------------------------------------------
+
+int rfx_fir_launch(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
+                   int num_taps, cudaStream_t stream)
+{
+    const int rc = check_fir_args(impl, x, taps, y, num_samples, num_taps);
+    if (rc != RFX_OK || num_samples == 0) {
+        return rc;
+    }
+    return launch_fir(resolve_fir_impl(impl, num_taps, num_samples), x, taps, y, num_samples,
+                      num_taps, stream);
+}
+
+int rfx_fir_device(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
+                   int num_taps)
+{
+    return rfx_fir_launch(impl, x, taps, y, num_samples, num_taps, nullptr);
+}
+
+int rfx_fir_load_const_taps(const float* taps, int num_taps, cudaStream_t stream)
+{
+    (void)stream;
+    if (num_taps < 1) {
+        return fail(RFX_ERR_INVALID, "fir: need at least one tap");
+    }
+    if (num_taps > rfx::kMaxTaps) {
+        return fail(RFX_ERR_CAPACITY, "fir: %d taps, more than the %d supported", num_taps,
+                    rfx::kMaxTaps);
+    }
+    if (taps == nullptr) {
+        return fail(RFX_ERR_INVALID, "fir: null taps");
+    }
+    return RFX_OK;
+}
+
+int rfx_fir_batched_device(int impl, const void* const* x, void* const* y,
+                           const int64_t* num_samples, int count, const float* taps,
+                           int num_taps, cudaStream_t stream)
+{
+    if (count < 1 || x == nullptr || y == nullptr || num_samples == nullptr) {
+        return fail(RFX_ERR_INVALID, "batched fir: %d channels, expected at least 1", count);
+    }
+    int64_t longest = 0;
+    for (int c = 0; c < count; ++c) {
+        const int rc = check_fir_args(impl, x[c], taps, y[c], num_samples[c], num_taps);
+        if (rc != RFX_OK) {
+            return rc;
+        }
+        longest = std::max(longest, num_samples[c]);
+    }
+    const int resolved = resolve_fir_impl(impl, num_taps, longest);
+    if (resolved == RFX_FIR_TC) {
+        for (int c = 0; c < count; ++c) {
+            if (num_samples[c] == 0) {
+                continue;
+            }
+            const int rc = launch_fir(resolved, x[c], taps, y[c], num_samples[c], num_taps,
+                                      stream);
+            if (rc != RFX_OK) {
+                return rc;
+            }
+        }
+        return RFX_OK;
+    }
+    for (int first = 0; first < count; first += rfx::kPlainBatchMax) {
+        const int chunk = std::min(count - first, rfx::kPlainBatchMax);
+        rfx::PlainBatch batch{};
+        for (int c = 0; c < chunk; ++c) {
+            batch.x[c] = x[first + c];
+            batch.y[c] = y[first + c];
+            batch.num_samples[c] = num_samples[first + c];
+        }
+        const cudaError_t err =
+            rfx::fir_plain_batched_launch(batch, chunk, taps, num_taps, stream);
+        if (err != cudaSuccess) {
+            return cuda_fail(err, "fir_plain_batched_launch");
+        }
+    }
+    return RFX_OK;
+}
+
+int rfx_fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
+                         cudaStream_t stream)
+{
+    if (count < 1 || count > rfx::kTcBatchMax || captures == nullptr) {
+        return fail(RFX_ERR_INVALID, "fir batch: %d captures, expected 1 to %d", count,
+                    rfx::kTcBatchMax);
+    }
+    for (int c = 0; c < count; ++c) {
+        const rfx_fir_capture& cap = captures[c];
+        const int rc = check_fir_args(impl, cap.x, cap.taps, cap.y, cap.num_samples,
+                                      cap.num_taps);
+        if (rc != RFX_OK) {
+            return rc;
+        }
+        if (cap.reserved != 0) {
+            return fail(RFX_ERR_INVALID, "fir batch: capture %d: reserved field must be 0", c);
+        }
+    }
+    cudaError_t err = rfx::fir_batch_launch(impl, captures, count, stream);
+    return err == cudaSuccess ? RFX_OK : cuda_fail(err, "fir_batch_launch");
+}
+
+// ---- channelizer --------------------------------------------------------------------------
+
+int64_t rfx_channelize_frames(int64_t num_samples, int channels)
+{
+    if (channels < 1 || num_samples < 0) {
+        return 0;
+    }
+    return (num_samples + channels - 1) / channels;
+}
+
+int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_plan** plan)
+{
+    if (plan == nullptr) {
+        return fail(RFX_ERR_INVALID, "channelize: null plan pointer");
+    }
+    *plan = nullptr;
+    if (impl == RFX_CHAN_AUTO) {
+        impl = RFX_CHAN_PLAIN;
+    }
+    if (impl != RFX_CHAN_PLAIN && impl != RFX_CHAN_TC) {
+        return fail(RFX_ERR_INVALID, "channelize: unknown implementation %d", impl);
+    }
+    if (channels < 1) {
+        return fail(RFX_ERR_INVALID, "channelize: need at least one channel");
+    }
+    if (max_samples < 0 || max_samples > kMaxSamples) {
+        return fail(RFX_ERR_INVALID, "channelize: %lld samples, expected 0 to %lld",
+                    static_cast<long long>(max_samples), static_cast<long long>(kMaxSamples));
+    }
+    if (impl == RFX_CHAN_TC) {
+        return fail(RFX_ERR_CAPACITY, "channelize: the tensor-core form is not available for "
+                                      "%d channels",
+                    channels);
+    }
+    auto* p = new rfx_chan_plan{impl, channels, rfx_channelize_frames(max_samples, channels), 0,
+                                false};
+    if (p->frames > 0) {
+        int nfft = channels;
+        const cufftResult r = cufftPlanMany(&p->fft, 1, &nfft, nullptr, 1, nfft, nullptr, 1,
+                                            nfft, CUFFT_C2C, static_cast<int>(p->frames));
+        if (r != CUFFT_SUCCESS) {
+            delete p;
+            return cufft_fail(r, "cufftPlanMany");
+        }
+        p->has_fft = true;
+    }
+    *plan = p;
+    return RFX_OK;
+}
+
+int rfx_chan_plan_destroy(rfx_chan_plan* plan)
+{
+    if (plan == nullptr) {
+        return RFX_OK;
+    }
+    cufftResult r = CUFFT_SUCCESS;
+    if (plan->has_fft) {
+        r = cufftDestroy(plan->fft);
+    }
+    delete plan;
+    return r == CUFFT_SUCCESS ? RFX_OK : cufft_fail(r, "cufftDestroy");
+}
+
+int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
+                          int64_t num_samples, int num_taps, cudaStream_t stream)
+{
+    if (plan == nullptr) {
+        return fail(RFX_ERR_INVALID, "channelize: null plan");
+    }
+    if (num_samples < 0 || num_samples > kMaxSamples) {
+        return fail(RFX_ERR_INVALID, "channelize: bad sample count %lld",
+                    static_cast<long long>(num_samples));
+    }
+    if (num_taps < 1) {
+        return fail(RFX_ERR_INVALID, "channelize: need at least one tap");
+    }
+    const int64_t frames = rfx_channelize_frames(num_samples, plan->channels);
+    if (frames == 0) {
+        return RFX_OK;
+    }
+    if (x == nullptr || taps == nullptr || out == nullptr) {
+        return fail(RFX_ERR_INVALID, "channelize: null pointer");
+    }
+    if (!aligned16(x) || !aligned16(out)) {
+        return fail(RFX_ERR_ALIGNMENT, "channelize: sample buffers must be 16-byte aligned");
+    }
+    if (frames != plan->frames) {
+        return fail(RFX_ERR_INVALID, "channelize: plan made for %lld frames, call has %lld",
+                    static_cast<long long>(plan->frames), static_cast<long long>(frames));
+    }
+    cudaError_t err = rfx::chan_branch_launch(x, taps, out, frames, plan->channels, num_taps,
+                                              stream);
+    if (err != cudaSuccess) {
+        return cuda_fail(err, "chan_branch_launch");
+    }
+    cufftResult r = cufftSetStream(plan->fft, stream);
+    if (r != CUFFT_SUCCESS) {
+        return cufft_fail(r, "cufftSetStream");
+    }
+    r = cufftExecC2C(plan->fft, static_cast<cufftComplex*>(out), static_cast<cufftComplex*>(out),
+                     CUFFT_INVERSE);
+    return r == CUFFT_SUCCESS ? RFX_OK : cufft_fail(r, "cufftExecC2C");
+}
+
+// ---- host-buffer operations ----------------------------------------------------------------
+
+}  // extern "C"
+
+namespace {
+
+struct DeviceMem {
+    void* p = nullptr;
+    ~DeviceMem()
+    {
+        if (p != nullptr) {
+            cudaFree(p);
+        }
+    }
+};
+
+struct Event {
+    cudaEvent_t e = nullptr;
+    ~Event()
+    {
+        if (e != nullptr) {
+            cudaEventDestroy(e);
+        }
+    }
+};
+
+void summarize(const std::vector<double>& v, double* mean, double* std_dev)
+{
+    *mean = 0.0;
+    *std_dev = 0.0;
+    if (v.empty()) {
+        return;
+    }
+    double s = 0.0;
+    for (double d : v) {
+        s += d;
+    }
+    *mean = s / static_cast<double>(v.size());
+    if (v.size() > 1) {
+        double q = 0.0;
+        for (double d : v) {
+            q += (d - *mean) * (d - *mean);
+        }
+        *std_dev = std::sqrt(q / static_cast<double>(v.size() - 1));
+    }
+}
+
+// warmup untimed passes, then `runs` passes with events around upload / compute / download on
+// the legacy default stream (src/bench.cpp:65-93).
+template <class Up, class Compute, class Down>
+int timed_passes(rfx_bench* bench, Up up, Compute compute, Down down)
+{
+    const int warmup = bench != nullptr ? std::max(0, bench->warmup) : 0;
+    const int runs = bench != nullptr ? std::max(1, bench->runs) : 1;
+    for (int i = 0; i < warmup; ++i) {
+        int rc;
+        if ((rc = up()) != RFX_OK || (rc = compute()) != RFX_OK || (rc = down()) != RFX_OK) {
+            return rc;
+        }
+    }
+    Event start, uploaded, computed, downloaded;
+    cudaError_t err;
+    if ((err = cudaEventCreate(&start.e)) != cudaSuccess ||
+        (err = cudaEventCreate(&uploaded.e)) != cudaSuccess ||
+        (err = cudaEventCreate(&computed.e)) != cudaSuccess ||
+        (err = cudaEventCreate(&downloaded.e)) != cudaSuccess) {
+        return cuda_fail(err, "cudaEventCreate");
+    }
+    std::vector<double> h2d, kernel, d2h;
+    for (int i = 0; i < runs; ++i) {
+        int rc;
+        cudaEventRecord(start.e, nullptr);
+        if ((rc = up()) != RFX_OK) {
+            return rc;
+        }
+        cudaEventRecord(uploaded.e, nullptr);
+        if ((rc = compute()) != RFX_OK) {
+            return rc;
+        }
+        cudaEventRecord(computed.e, nullptr);
+        if ((rc = down()) != RFX_OK) {
+            return rc;
+        }
+        cudaEventRecord(downloaded.e, nullptr);
+        if ((err = cudaEventSynchronize(downloaded.e)) != cudaSuccess) {
+            return cuda_fail(err, "cudaEventSynchronize");
+        }
+        float a = 0, b = 0, c = 0;
+        cudaEventElapsedTime(&a, start.e, uploaded.e);
+        cudaEventElapsedTime(&b, uploaded.e, computed.e);
+        cudaEventElapsedTime(&c, computed.e, downloaded.e);
+        h2d.push_back(a);
+        kernel.push_back(b);
+        d2h.push_back(c);
+    }
+    if (bench != nullptr) {
+        summarize(h2d, &bench->h2d_ms_mean, &bench->h2d_ms_std);
+        summarize(kernel, &bench->kernel_ms_mean, &bench->kernel_ms_std);
+        summarize(d2h, &bench->d2h_ms_mean, &bench->d2h_ms_std);
+    }
+    return RFX_OK;
+}
+
+int copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind)
+{
+    if (bytes == 0) {
+        return RFX_OK;
+    }
+    const cudaError_t err = cudaMemcpy(dst, src, bytes, kind);
+    return err == cudaSuccess ? RFX_OK : cuda_fail(err, "cudaMemcpy");
+}
+
+}  // namespace
+
+extern "C" {
+
+int rfx_fir_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
+                 int num_taps, int block, void* y_iq, rfx_bench* bench)
+{
+    if (block < 32 || block > 1024 || block % 32 != 0) {
+        return fail(RFX_ERR_INVALID, "--block needs a multiple of 32 up to 1024, got %d", block);
+    }
+    if (num_samples > 0 && (x_iq == nullptr || y_iq == nullptr || taps == nullptr)) {
+        return fail(RFX_ERR_INVALID, "fir: null host pointer");
+    }
+    DeviceMem dx, dy, dh;
+    const size_t xbytes = static_cast<size_t>(num_samples) * 8;
+    cudaError_t err;
+    if (num_samples > 0) {
+        if ((err = cudaMalloc(&dx.p, xbytes)) != cudaSuccess ||
+            (err = cudaMalloc(&dy.p, xbytes)) != cudaSuccess) {
+            return cuda_fail(err, "cudaMalloc");
+        }
+    }
+    if (num_taps > 0 && (err = cudaMalloc(&dh.p, sizeof(float) * num_taps)) != cudaSuccess) {
+        return cuda_fail(err, "cudaMalloc");
+    }
+    int rc = check_fir_args(impl, dx.p, static_cast<const float*>(dh.p), dy.p, num_samples,
+                            num_taps);
+    if (rc != RFX_OK) {
+        return rc;
+    }
+    return timed_passes(
+        bench,
+        [&] {
+            int r = copy(dx.p, x_iq, xbytes, cudaMemcpyHostToDevice);
+            return r != RFX_OK ? r
+                               : copy(dh.p, taps, sizeof(float) * num_taps,
+                                      cudaMemcpyHostToDevice);
+        },
+        [&] {
+            return rfx_fir_launch(impl, dx.p, static_cast<const float*>(dh.p), dy.p, num_samples,
+                                  num_taps, nullptr);
+        },
+        [&] { return copy(y_iq, dy.p, xbytes, cudaMemcpyDeviceToHost); });
+}
+
+int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
+                        int num_taps, int channels, void* z_iq, rfx_bench* bench)
+{
+    if (channels < 1) {
+        return fail(RFX_ERR_INVALID, "channelize: need at least one channel");
+    }
+    if (num_taps < 1) {
+        return fail(RFX_ERR_INVALID, "channelize: need at least one tap");
+    }
+    const int64_t frames = rfx_channelize_frames(num_samples, channels);
+    if (frames == 0) {
+        return RFX_OK;
+    }
+    if (x_iq == nullptr || z_iq == nullptr || taps == nullptr) {
+        return fail(RFX_ERR_INVALID, "channelize: null host pointer");
+    }
+    rfx_chan_plan* plan = nullptr;
+    int rc = rfx_chan_plan_create(impl, channels, num_samples, &plan);
+    if (rc != RFX_OK) {
+        return rc;
+    }
+    struct PlanGuard {
+        rfx_chan_plan* p;
+        ~PlanGuard() { rfx_chan_plan_destroy(p); }
+    } guard{plan};
+    DeviceMem dx, dz, dh;
+    const size_t xbytes = static_cast<size_t>(num_samples) * 8;
+    const size_t zbytes = static_cast<size_t>(frames) * channels * 8;
+    cudaError_t err;
+    if ((err = cudaMalloc(&dx.p, xbytes)) != cudaSuccess ||
+        (err = cudaMalloc(&dz.p, zbytes)) != cudaSuccess ||
+        (err = cudaMalloc(&dh.p, sizeof(float) * num_taps)) != cudaSuccess) {
+        return cuda_fail(err, "cudaMalloc");
+    }
+    return timed_passes(
+        bench,
+        [&] {
+            int r = copy(dx.p, x_iq, xbytes, cudaMemcpyHostToDevice);
+            return r != RFX_OK ? r
+                               : copy(dh.p, taps, sizeof(float) * num_taps,
+                                      cudaMemcpyHostToDevice);
+        },
+        [&] {
+            return rfx_channelize_launch(plan, dx.p, static_cast<const float*>(dh.p), dz.p,
+                                         num_samples, num_taps, nullptr);
+        },
+        [&] { return copy(z_iq, dz.p, zbytes, cudaMemcpyDeviceToHost); });
+}
+
+}  // extern "C"

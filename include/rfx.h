@@ -1,0 +1,192 @@
+/*
+ * rfx.h — C ABI of the GB300-native complex-baseband filtering library (librfx.so).
+ *
+ * The library replaces the hot path of the gpu-rf-pipeline project: the complex-float32 FIR
+ * filter (src/fir.cu) and the critically sampled polyphase channelizer (src/channelize.cu),
+ * behind the project's device-pointer entry points (src/device_ops.hpp) and its host-vector
+ * operations (src/ops.hpp). Every function here names the project interface it replaces.
+ *
+ * Conventions (all functions):
+ *   - Plain C types only. A cf32 sample is two little-endian float32 values, I then Q
+ *     (src/types.hpp:7-12); `x`, `y`, `out` point to arrays of them.
+ *   - Device pointers must be 16-byte aligned (cudaMalloc and PyTorch allocations are).
+ *   - Lengths are 64-bit. The FIR and the channelizer accept up to 2^31 - 1 samples per call.
+ *   - Every function returns an rfx_status; RFX_OK is 0. On failure, rfx_last_error() returns a
+ *     message for the calling thread. The C++ layer above maps non-zero statuses to
+ *     std::runtime_error, as the project's CUDA_CHECK does (src/check.hpp:42-66).
+ *   - The launch functions only enqueue work on the given stream (0 = the legacy default
+ *     stream): no allocation, no host transfer, no synchronization (src/device_ops.hpp:3-7).
+ *   - Device-side waits inside the kernels are bounded. A kernel that gives up records a fault
+ *     code that rfx_device_fault() reports; the CUDA context stays usable.
+ */
+#ifndef RFX_H
+#define RFX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rfx_status {
+    RFX_OK = 0,
+    RFX_ERR_INVALID = 1,     /* bad argument (null pointer, negative length, no taps ...) */
+    RFX_ERR_CAPACITY = 2,    /* valid but beyond what the chosen implementation supports */
+    RFX_ERR_ALIGNMENT = 3,   /* a device pointer is not 16-byte aligned */
+    RFX_ERR_CUDA = 4,        /* a CUDA runtime or cuFFT call failed */
+    RFX_ERR_DEVICE_FAULT = 5 /* a kernel gave up on a bounded wait (see rfx_device_fault) */
+} rfx_status;
+
+/* FIR implementations (values of `impl`). */
+typedef enum rfx_fir_impl {
+    /* FP32 CUDA-core kernel: sample tile staged in shared memory by the bulk-copy (TMA) engine,
+     * nine outputs per thread from a register window, packed f32x2 fused multiply-adds.
+     * Same arithmetic as the project's naive/tiled/register kernels (one fused multiply-add
+     * per tap, taps in ascending order), so results are bit-identical to theirs. */
+    RFX_FIR_PLAIN = 0,
+    /* Tensor-core kernel (tcgen05): the FIR as a block-Toeplitz GEMM in split FP16
+     * (hi + lo operands, three products, FP32 accumulation in tensor memory) with one
+     * power-of-two scale per tile. Tolerance-tested, not bit-exact; one tap uses RFX_FIR_PLAIN. */
+    RFX_FIR_TC = 1,
+    /* Chooses per call from the tuned table (rfx_autotune) or a built-in rule. */
+    RFX_FIR_AUTO = 2
+} rfx_fir_impl;
+
+/* Channelizer implementations. */
+typedef enum rfx_chan_impl {
+    /* FP32 branch-sum kernel (bit-identical to the project's channelize_branch_kernel) followed
+     * by cuFFT's batched in-place inverse transform, as the project computes it. */
+    RFX_CHAN_PLAIN = 0,
+    /* One fused tensor-core kernel: FP32 branch sums into shared memory, then the M-point DFT as
+     * a split-FP16 GEMM on tcgen05 (M = 64 here; M = 1024 as a 32 x 32 factorization). */
+    RFX_CHAN_TC = 1,
+    RFX_CHAN_AUTO = 2
+} rfx_chan_impl;
+
+/* ---- errors and identification -------------------------------------------------------- */
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* rfx_last_error(void);
+
+/* Synchronizes the current device, returns the fault code any kernel of this library recorded
+ * since the last call (0 = none) and clears it. */
+int rfx_device_fault(unsigned int* code);
+
+/* Library version, e.g. "rfx 0.1.0 sm_103a". */
+const char* rfx_version(void);
+
+/* Implementation names for `rfgpu info` and --impl: writes at most `size` bytes of the name of
+ * implementation `index` into `name`; returns RFX_ERR_INVALID past the last one.
+ * Replaces fir_impls() (src/ops.hpp:36, table at src/fir.cu:725-734). */
+int rfx_fir_impl_name(int index, char* name, size_t size);
+int rfx_chan_impl_name(int index, char* name, size_t size);
+
+/* Parses an --impl name into an rfx_fir_impl. Accepts "plain", "tc_split", "auto" and, as
+ * aliases of "plain" (same results bit for bit), the project's "naive", "tiled",
+ * "tiled_const" and "register". Replaces parse_fir_impl (src/device_ops.hpp:75). */
+int rfx_parse_fir_impl(const char* name, int* impl);
+int rfx_parse_chan_impl(const char* name, int* impl);
+
+/* ---- FIR, device pointers ------------------------------------------------------------- */
+
+/* y[n] = sum_k taps[k] x[n - k] for 0 <= n < num_samples, x[m < 0] = 0; `taps` in GPU memory
+ * (num_taps <= 8192). Enqueued on `stream`.
+ * Replaces fir_launch (src/device_ops.hpp:88-89). */
+int rfx_fir_launch(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
+                   int num_taps, cudaStream_t stream);
+
+/* rfx_fir_launch on the legacy default stream. Replaces fir_device (src/device_ops.hpp:81-82). */
+int rfx_fir_device(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
+                   int num_taps);
+
+/* Checks that `num_taps` fits the tap capacity. The kernels here read the taps from the pointer
+ * passed to each launch, so there is no constant bank to fill: callers that load it first and
+ * then launch (src/stream.cu:158-160, :195-202) get the same results.
+ * Replaces fir_load_const_taps (src/device_ops.hpp:87). */
+int rfx_fir_load_const_taps(const float* taps, int num_taps, cudaStream_t stream);
+
+/* `count` channels sharing one set of taps, in one launch; `x`, `y` and `num_samples` are HOST
+ * arrays of `count` entries (device pointers / lengths). No limit of 8 channels.
+ * Replaces fir_batched_device (src/device_ops.hpp:99-100). */
+int rfx_fir_batched_device(int impl, const void* const* x, void* const* y,
+                           const int64_t* num_samples, int count, const float* taps,
+                           int num_taps, cudaStream_t stream);
+
+/* One capture of a per-capture-taps batch. */
+typedef struct rfx_fir_capture {
+    const void* x;          /* device, cf32 */
+    void* y;                /* device, cf32 */
+    const float* taps;      /* device, float32 */
+    int64_t num_samples;
+    int32_t num_taps;
+    int32_t reserved;       /* must be 0 */
+} rfx_fir_capture;
+
+/* Up to 4096 captures, each with its own taps, in ONE persistent launch (a work list of
+ * (capture, tile) items). `captures` is a HOST array. No counterpart in the project, which
+ * runs such a batch as one fir_launch per capture (src/stream.cu:195-202 pattern). */
+int rfx_fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
+                         cudaStream_t stream);
+
+/* ---- channelizer ---------------------------------------------------------------------- */
+
+/* ceil(num_samples / channels). Replaces channelize_frames (src/device_ops.hpp:145). */
+int64_t rfx_channelize_frames(int64_t num_samples, int channels);
+
+typedef struct rfx_chan_plan rfx_chan_plan;
+
+/* Setup for channelizing up to `max_samples` samples into `channels` channels: for
+ * RFX_CHAN_PLAIN, the batched inverse cuFFT plan of `channels` points (the project's FftPlan,
+ * src/fft_plan.hpp:15-22). Allocates; call outside timed regions. */
+int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_plan** plan);
+int rfx_chan_plan_destroy(rfx_chan_plan* plan);
+
+/* z[t][k] = sum_l taps[l] x[tM - l] e^{+2 pi i k l / M}, t < ceil(N/M), into `out`
+ * (frames * channels cf32, frame-major). `taps` in GPU memory. Enqueued on `stream`.
+ * Replaces channelize_device (src/device_ops.hpp:150-151). */
+int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
+                          int64_t num_samples, int num_taps, cudaStream_t stream);
+
+/* ---- host-buffer operations (timed like the project's Bench) --------------------------- */
+
+/* Phase timings of a host-buffer call, as the project's BenchResult (src/bench.hpp:17-32). */
+typedef struct rfx_bench {
+    int warmup;              /* in: untimed passes */
+    int runs;                /* in: timed passes (>= 1) */
+    double h2d_ms_mean, h2d_ms_std;
+    double kernel_ms_mean, kernel_ms_std;
+    double d2h_ms_mean, d2h_ms_std;
+} rfx_bench;
+
+/* The FIR on host buffers: allocates device memory (setup, untimed), then `runs` passes of
+ * upload / compute / download timed with CUDA events. `x_iq`/`y_iq` are host cf32 arrays.
+ * `block` is accepted for the project's --block (a multiple of 32, at most 1024) and does
+ * not change the result. `bench` may be NULL (one untimed pass).
+ * Replaces the FirFn table entries (src/ops.hpp:33-36). */
+int rfx_fir_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
+                 int num_taps, int block, void* y_iq, rfx_bench* bench);
+
+/* The channelizer on host buffers, as above. `z_iq` receives frames * channels cf32.
+ * Replaces channelize_cuda (src/ops.hpp:40-41). */
+int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
+                        int num_taps, int channels, void* z_iq, rfx_bench* bench);
+
+/* ---- tuning --------------------------------------------------------------------------- */
+
+/* Times every candidate tile shape of `impl` for one (num_taps, num_samples) FIR case on the
+ * current device and stores the fastest in the in-process table RFX_FIR_AUTO consults.
+ * Allocates scratch buffers; synchronizes. `best_ms` may be NULL. */
+int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, double* best_ms);
+
+/* Writes / reads the tuned table as text (one line per entry, keyed by GPU name and driver). */
+int rfx_autotune_save(const char* path);
+int rfx_autotune_load(const char* path);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RFX_H */

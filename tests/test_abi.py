@@ -1,0 +1,115 @@
+"""The C ABI on the CPU: librfx.so builds, loads, exports every function include/rfx.h declares,
+and rejects bad arguments before touching the GPU (no compute calls here)."""
+from __future__ import annotations
+
+import ctypes
+import re
+
+import pytest
+
+from conftest import ROOT
+
+import rfx
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not rfx.LIB_PATH.exists():
+        import __graft_entry__
+
+        __graft_entry__.build()
+    return rfx.load()
+
+
+def declared_functions() -> list[str]:
+    text = (ROOT / "include" / "rfx.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rfx_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_function_is_exported(lib) -> None:
+    names = declared_functions()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in rfx.SIGNATURES, f"{name} missing from the Python binding"
+
+
+def test_binding_declares_nothing_the_header_does_not() -> None:
+    assert set(rfx.SIGNATURES) <= set(declared_functions())
+
+
+def test_library_targets_sm_103a(lib) -> None:
+    assert b"sm_103a" in lib.rfx_version()
+
+
+def test_impl_names_and_aliases(lib) -> None:
+    assert rfx.fir_impl_names() == ["plain", "tc_split", "auto"]
+    assert rfx.chan_impl_names() == ["plain", "tc_split", "auto"]
+    # The project's --impl names keep working and mean the plain kernel (same results).
+    for name in ["naive", "tiled", "tiled_const", "register", "plain"]:
+        assert rfx.parse_fir_impl(name) == rfx.FIR_PLAIN
+    assert rfx.parse_fir_impl("tc_split") == rfx.FIR_TC
+    with pytest.raises(rfx.RfxError) as e:
+        rfx.parse_fir_impl("no_such_impl")
+    assert e.value.status == 1 and "no_such_impl" in str(e.value)
+
+
+def test_frames_arithmetic(lib) -> None:
+    assert lib.rfx_channelize_frames(0, 16) == 0
+    assert lib.rfx_channelize_frames(1, 16) == 1
+    assert lib.rfx_channelize_frames(65536, 16) == 4096
+    assert lib.rfx_channelize_frames(10007, 16) == 626
+    assert lib.rfx_channelize_frames(1 << 26, 1024) == 1 << 16
+    assert lib.rfx_channelize_frames(5, 0) == 0
+
+
+@pytest.mark.parametrize("n,k,status", [(-1, 63, 1), (100, 0, 1), (100, 8193, 2),
+                                         (1 << 31, 63, 1)])
+def test_fir_argument_errors(lib, n: int, k: int, status: int) -> None:
+    buf = ctypes.create_string_buffer(64)
+    p = (ctypes.addressof(buf) + 15) & ~15
+    rc = lib.rfx_fir_launch(0, p, p, p, n, k, None)
+    assert rc == status
+    assert lib.rfx_last_error()
+
+
+def test_fir_alignment_error(lib) -> None:
+    buf = ctypes.create_string_buffer(64)
+    p = (ctypes.addressof(buf) + 15) & ~15
+    assert lib.rfx_fir_launch(0, p + 8, p, p, 10, 3, None) == 3
+    assert b"aligned" in lib.rfx_last_error()
+
+
+def test_zero_samples_is_a_no_op(lib) -> None:
+    assert lib.rfx_fir_launch(0, None, None, None, 0, 5, None) == 0
+
+
+def test_load_const_taps_checks_capacity(lib) -> None:
+    buf = ctypes.create_string_buffer(64)
+    assert lib.rfx_fir_load_const_taps(ctypes.addressof(buf), 8192, None) == 0
+    assert lib.rfx_fir_load_const_taps(ctypes.addressof(buf), 8193, None) == 2
+    assert lib.rfx_fir_load_const_taps(ctypes.addressof(buf), 0, None) == 1
+
+
+def test_batch_argument_errors(lib) -> None:
+    assert lib.rfx_fir_batch_launch(0, None, 0, None) == 1
+    caps = (rfx.FirCapture * 1)()
+    caps[0] = rfx.FirCapture(None, None, None, 10, 5, 0)
+    assert lib.rfx_fir_batch_launch(0, caps, 1, None) == 1  # null pointers
+    assert lib.rfx_fir_batched_device(0, None, None, None, 0, None, 5, None) == 1
+
+
+def test_channelizer_plan_argument_errors(lib) -> None:
+    handle = ctypes.c_void_p()
+    assert lib.rfx_chan_plan_create(0, 0, 100, ctypes.byref(handle)) == 1
+    assert lib.rfx_chan_plan_create(7, 16, 100, ctypes.byref(handle)) == 1
+    assert lib.rfx_chan_plan_create(0, 16, -5, ctypes.byref(handle)) == 1
+    assert lib.rfx_channelize_launch(None, None, None, None, 10, 5, None) == 1
+    assert lib.rfx_chan_plan_destroy(None) == 0
+
+
+def test_host_block_size_is_checked(lib) -> None:
+    for block in (0, 48, 2048):
+        assert lib.rfx_fir_host(0, None, 0, None, 1, block, None, None) == 1
+        assert b"--block" in lib.rfx_last_error()

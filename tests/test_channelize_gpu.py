@@ -1,0 +1,104 @@
+"""Channelizer on the GPU through the C ABI, against the oracle.
+
+Mirrors the project's channelizer tests (tests/test_pipeline.py:360-405): its five fixture cases
+at rtol 1e-5 / atol 1e-4, the channel-3 tone, and a bad channel count; plus the channel counts
+the benchmark workloads use (64 and 1024) and ragged lengths.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import rfx
+from oracle import rf_oracle as orc
+from rfx import signals
+
+pytestmark = pytest.mark.gpu
+
+CHANNELIZE_RTOL = 1e-5
+CHANNELIZE_ATOL = 1e-4
+DEV = torch.device("cuda:0")
+
+
+def dev(a: np.ndarray) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
+
+
+def run(x: np.ndarray, h: np.ndarray, m: int, impl="plain") -> np.ndarray:
+    z = rfx.channelize(dev(x), dev(h), m, impl=impl)
+    torch.cuda.synchronize()
+    return z.cpu().numpy()
+
+
+@pytest.fixture(scope="module", autouse=True)
+def no_faults():
+    rfx.load()
+    yield
+    assert rfx.device_fault() == 0
+
+
+@pytest.mark.parametrize("name,taps,channels", [
+    ("tone", "channelizer_proto", 16),
+    ("tone_odd", "channelizer_proto", 16),   # partial last frame
+    ("tone", "lowpass_long", 64),            # taps not a multiple of M
+    ("short", "lowpass", 4),                 # input shorter than the filter
+    ("tone_odd", "identity", 1),             # one channel, one tap: the input itself
+])
+def test_channelize_matches_reference(name: str, taps: str, channels: int) -> None:
+    x, h = signals.fixture_signal(name), signals.fixture_taps(taps)
+    z = run(x, h, channels)
+    ref = orc.channelize_fast(x, h, channels)
+    assert z.shape == ref.shape
+    np.testing.assert_allclose(z, ref, rtol=CHANNELIZE_RTOL, atol=CHANNELIZE_ATOL)
+
+
+def test_channelize_puts_a_tone_in_its_channel() -> None:
+    n = np.arange(16 * 512)
+    x = signals.to_cf32(np.exp(2j * np.pi * 3 * n / 16))
+    z = run(x, signals.fixture_taps("channelizer_proto"), 16)[16:]
+    power = np.mean(np.abs(z) ** 2, axis=0)
+    assert np.argmax(power) == 3
+    assert power[3] > 1000 * np.max(np.delete(power, 3))
+    np.testing.assert_allclose(np.abs(z[:, 3]), 1.0, atol=0.02)
+
+
+@pytest.mark.parametrize("n,k,m", [(100, 37, 4), (64, 16, 16), (7, 63, 4), (33, 1, 1),
+                                   (50, 24, 8), (70001, 1024, 64), (1 << 16, 4096, 1024),
+                                   (5 * 1024 + 3, 32768, 1024), (12345, 100, 12)])
+def test_channelize_random_cases(n: int, k: int, m: int) -> None:
+    rng = np.random.default_rng(n + k + m)
+    x = signals.to_cf32(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    h = (rng.standard_normal(k) / np.sqrt(k)).astype(np.float32)
+    z = run(x, h, m)
+    ref = orc.channelize_fast(x, h, m)
+    assert orc.normwise_error(z, ref) < 1e-5
+
+
+def test_pfb64_workload_prefix() -> None:
+    w = signals.channelizer64(1 << 20)
+    z = run(w.x, w.taps, 64)
+    assert orc.normwise_error(z, orc.channelize_fast(w.x, w.taps, 64)) < 1e-5
+
+
+def test_host_buffer_path() -> None:
+    x, h = signals.fixture_signal("tone"), signals.fixture_taps("channelizer_proto")
+    z, bench = rfx.channelize_host("plain", x, h, 16, warmup=1, runs=3)
+    np.testing.assert_allclose(z, orc.channelize_fast(x, h, 16), rtol=CHANNELIZE_RTOL,
+                               atol=CHANNELIZE_ATOL)
+    assert bench.kernel_ms_mean > 0
+
+
+def test_plan_frame_count_is_checked() -> None:
+    x = dev(signals.fixture_signal("tone_odd"))
+    h = dev(signals.fixture_taps("channelizer_proto"))
+    out = torch.empty(1024 * 16, dtype=torch.complex64, device=DEV)
+    with rfx.ChanPlan(16, 4096) as plan:
+        with pytest.raises(rfx.RfxError) as e:
+            plan.launch(x, h, out)
+        assert e.value.status == 1
+
+
+def test_bad_channel_count_is_an_error() -> None:
+    with pytest.raises(rfx.RfxError):
+        rfx.ChanPlan(0, 100)
