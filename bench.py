@@ -83,65 +83,120 @@ def barrier(dist, device=None) -> None:
 # --- clocks during the timed region ---------------------------------------------------------
 
 class ClockSampler:
-    """nvidia-smi -lms 200 in the background; median SM clock while the GPU was busy."""
+    """SM clock, utilization and clock-event reasons every 10 ms during the timed region, read
+    through NVML (libnvidia-ml, read-only queries); nvidia-smi -lms 200 when NVML is absent."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, index: int) -> None:
-        self.index = index
-        self.proc = None
-        self.lines: list[str] = []
-        self.thread = None
+    def __init__(self, cuda_index: int) -> None:
+        self.cuda_index = cuda_index
+        self.rows: list[dict] = []
+        self.max_mhz = None
+        self._stop = threading.Event()
+        self._thread = None
+        self._proc = None
+        self.source = None
+
+    def _nvml_handle(self):
+        import ctypes
+
+        nvml = ctypes.CDLL("libnvidia-ml.so.1")
+        if nvml.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        handle = ctypes.c_void_p()
+        try:
+            import torch
+
+            uuid = str(torch.cuda.get_device_properties(self.cuda_index).uuid)
+            uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+            if nvml.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(handle)) != 0:
+                raise OSError
+        except Exception:
+            if nvml.nvmlDeviceGetHandleByIndex_v2(self.cuda_index, ctypes.byref(handle)) != 0:
+                raise OSError("no NVML handle")
+        return nvml, handle
+
+    def _poll_nvml(self, nvml, handle) -> None:
+        import ctypes
+
+        class Util(ctypes.Structure):
+            _fields_ = [("gpu", ctypes.c_uint), ("memory", ctypes.c_uint)]
+
+        clk = ctypes.c_uint()
+        reasons = ctypes.c_ulonglong()
+        util = Util()
+        get_reasons = getattr(nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self._stop.is_set():
+            if nvml.nvmlDeviceGetClockInfo(handle, 1, ctypes.byref(clk)) == 0:
+                get_reasons(handle, ctypes.byref(reasons))
+                nvml.nvmlDeviceGetUtilizationRates(handle, ctypes.byref(util))
+                self.rows.append({"sm": float(clk.value), "util": float(util.gpu),
+                                  "reasons": [v for k, v in self.REASONS.items()
+                                              if reasons.value & k]})
+            self._stop.wait(0.01)
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except OSError:
-            self.proc = None
+            import ctypes
+
+            nvml, handle = self._nvml_handle()
+            mx = ctypes.c_uint()
+            if nvml.nvmlDeviceGetMaxClockInfo(handle, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            self._thread = threading.Thread(target=self._poll_nvml, args=(nvml, handle),
+                                            daemon=True)
+            self.source = "nvml"
+        except Exception:
+            try:
+                self._proc = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.cuda_index),
+                     "--query-gpu=clocks.sm,clocks.max.sm,utilization.gpu,"
+                     "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                     "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                     "--format=csv,noheader,nounits", "-lms", "200"],
+                    stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                self._thread = threading.Thread(target=self._poll_smi, daemon=True)
+                self.source = "nvidia-smi"
+            except OSError:
+                self._thread = None
+        if self._thread is not None:
+            self._thread.start()
         return self
 
-    def _read(self) -> None:
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    def _poll_smi(self) -> None:
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            try:
+                self.max_mhz = float(parts[1])
+                self.rows.append({"sm": float(parts[0]), "util": float(parts[2]),
+                                  "reasons": [n for n, v in zip(names, parts[3:7])
+                                              if v.lower() == "active"]})
+            except (ValueError, IndexError):
+                continue
 
     def __exit__(self, *exc) -> None:
-        if self.proc is not None:
-            self.proc.terminate()
+        self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()
             try:
-                self.proc.wait(timeout=5)
+                self._proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
-                self.proc.kill()
-            if self.thread is not None:
-                self.thread.join(timeout=2)
+                self._proc.kill()
+        if self._thread is not None:
+            self._thread.join(timeout=2)
 
     def summary(self) -> dict:
-        rows = []
-        for line in self.lines:
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                rows.append({"sm": float(parts[1]), "max": float(parts[2]),
-                             "util": float(parts[4]),
-                             "reasons": [name for name, v in zip(
-                                 ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
-                                  "sw_power_cap"], parts[5:9]) if v.lower() == "active"]})
-            except ValueError:
-                continue
+        rows = self.rows
         if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [], "samples": 0,
+                    "source": self.source}
         busy = [r for r in rows if r["util"] > 0] or rows
-        reasons = sorted({x for r in busy for x in r["reasons"]})
-        return {"sm_mhz": statistics.median(r["sm"] for r in busy),
-                "sm_max_mhz": max(r["max"] for r in rows), "reasons": reasons,
-                "samples": len(busy)}
+        return {"sm_mhz": statistics.median(r["sm"] for r in busy), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted({x for r in busy for x in r["reasons"]}),
+                "samples": len(busy), "source": self.source}
 
 
 # --- the workloads ---------------------------------------------------------------------------
@@ -334,7 +389,7 @@ def run_ours(args) -> None:
     with ClockSampler(device.index if device.index is not None else 0) as clocks:
         seconds = time_device(launch, args.steps, args.warmup, dist, device)
     kernel_s = kernel_average_s(launch, max(3, min(args.steps, 10)))
-    value = world * n / seconds / 1e6
+    value = world * n * args.steps / seconds / 1e6
 
     # Accuracy of this run's output against the float64 oracle, on a prefix (rank 0).
     err = None
@@ -430,7 +485,7 @@ def run_ours(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="fir1025", choices=["fir1025", "fir63", "pfb64"])
