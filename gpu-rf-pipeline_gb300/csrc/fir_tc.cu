@@ -4,34 +4,44 @@
 //
 // Blocks of B = 128 outputs: with X[s][j] = x[jB + s] (s < B) the output block j is
 //   Y[:, j] = sum_{c=0}^{C} T_c X[:, j - c],   T_c(r, s) = h[cB + r - s]  (0 outside [0, K)),
-// C = floor((K + B - 2) / B). One CTA tile is NB = 128 consecutive output blocks (16384 outputs);
-// the GEMM per tile is D (128 x 256) += A (128 x 16) B (16 x 256) over K-steps (c, s0):
+// C = floor((K + B - 2) / B). One tile is NB = 128 consecutive output blocks (16384 outputs);
+// per tile the GEMM is D (128 x 256) += A (128 x 16) B (16 x 256) over K-steps (c, s0):
 //
 //  * A = T_c restricted to s in [s0, s0 + 16). Output rows are stored reversed (TMEM lane i holds
 //    output r = 127 - i); then every 8 x 8 core matrix of A depends only on (row group + K group),
 //    so ALL of T_0 .. T_C live in shared memory as one strip of 16C + 31 core matrices,
 //    G[t][q][e] = h[(C+1)B - 1 - 8t - q - e], and a K-step's A is a descriptor into that strip
 //    with leading- and stride-byte offsets both 128 (the strip is read with overlap).
-//  * B = the samples: N index 2j' + {0: I, 1: Q}. Shared memory holds, per K-step pair of
-//    8-sample "planes", one 16-byte row per (window block, component); rows are contiguous at a
-//    16-byte pitch (stride-byte offset 128 per 8 rows) so the shift by c blocks is just a start
-//    address 32c bytes further. Each sample is stored once per tile.
+//  * B = the samples: N index 2j' + {0: I, 1: Q}. Shared memory holds, per K-step, two 8-sample
+//    "planes" with one 16-byte row per (window block, component); rows are contiguous at a
+//    16-byte pitch (stride-byte offset 128 per 8 rows), so the shift by c blocks is a start
+//    address 32c bytes further. Each sample is converted once per tile.
 //
 // Split precision: x' = 2^ex x and h' = 2^eh h (powers of two chosen per tile and per filter so
 // the largest magnitude lands in [2^14, 2^15)), x' = x_hi + x_lo and h' = h_hi + h_lo in FP16,
-// and D accumulates h_hi x_hi + h_hi x_lo + h_lo x_hi in FP32 tensor memory; the epilogue scales
-// by 2^-(ex+eh) exactly. The dropped h_lo x_lo term and FP32 accumulation keep the normwise
-// error near 1e-7 (tests gate it at 2e-6 against the float64 oracle).
+// and the MMAs sum h_hi x_hi + h_hi x_lo + h_lo x_hi with FP32 accumulation; the result is
+// scaled by 2^-(ex+eh) exactly.
 //
-// Roles (416 threads): warps 0-7 produce (load fp32 samples, find the tile's scale, convert into
-// the operand ring), warps 8-11 drain accumulators (TMEM -> registers -> global, one TMEM lane
-// quarter each), warp 12 owns tensor memory and issues the MMAs (one thread). Two accumulators
-// of 256 columns let the epilogue of one tile overlap the MMAs of the next. Every wait is an
-// mbarrier wait bounded in time; a give-up sets the fault word and stops all roles.
+// Accumulation: the tensor core adds each MMA's products into its FP32 accumulator with
+// round-toward-zero, so the error of an accumulator grows with the number of MMAs it takes.
+// Each TMEM accumulator therefore takes one GROUP of at most 12 MMAs (4 block-chunks x 3
+// products); the worker warps add every group's partial sum into FP32 running sums in registers
+// (round-to-nearest). Two 256-column partial buffers alternate, so the MMAs of one group overlap
+// the drain of the previous one.
+//
+// Roles (544 threads): warps 0-15 are workers and warp 16 owns tensor memory and issues the MMAs
+// (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 64 (w / 4) .. +63, holds
+// those 64 running sums, writes those outputs, and shares the producing: the tile's scale (a max
+// over its input window, read straight from global memory), and the conversion of each K-step's
+// fp32 samples — staged by a 2-D TMA copy (zero fill outside the input) — into the FP16 planes.
+// Every wait is an mbarrier wait bounded in time; a give-up sets the fault word and every role
+// stops.
 #include "fir_tc.cuh"
 #include "fir_plain.cuh"
 #include "ptx.cuh"
+#include "tmap.hpp"
 
+#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -41,16 +51,18 @@ static __device__ unsigned int g_fault_fir_tc;
 
 namespace {
 
-constexpr int kB = 128;              // outputs per block = MMA M
-constexpr int kNB = 128;             // blocks per tile; MMA N = 2 * kNB = 256
+constexpr int kB = 128;                  // outputs per block = MMA M
+constexpr int kNB = 128;                 // blocks per tile; MMA N = 2 * kNB = 256
 constexpr int kN = 2 * kNB;
 constexpr int kStagesPerTile = kB / 16;  // K-steps of 16 samples
-constexpr int kProducerWarps = 8;
-constexpr int kEpilogueWarp0 = 8;
-constexpr int kMmaWarp = 12;
-constexpr int kThreads = 13 * 32;
-constexpr int kProducers = kProducerWarps * 32;
-constexpr uint32_t kTmemCols = 512;  // two accumulators of kN columns
+constexpr int kWorkerWarps = 16;
+constexpr int kWorkers = kWorkerWarps * 32;
+constexpr int kMmaWarp = 16;
+constexpr int kThreads = 17 * 32;
+constexpr int kCols = kN / 4;            // running sums per worker thread
+constexpr int kChunksPerGroup = 4;       // 12 MMAs per accumulator
+constexpr int kRaw = 3;                  // TMA raw-sample ring depth
+constexpr uint32_t kTmemCols = 512;      // two partial buffers of kN columns
 
 constexpr uint32_t kIdesc = (1u << 4)                       // D: F32
                             | (0u << 7) | (0u << 10)        // A, B: F16
@@ -59,26 +71,29 @@ constexpr uint32_t kIdesc = (1u << 4)                       // D: F32
 
 struct Layout {
     int C;               // previous blocks a block reaches back to
-    int W;               // window rows per plane: 2 (kNB + C)
-    uint32_t pitch;      // bytes per plane (W * 16 + 16)
+    int rows;            // window blocks per tile: kNB + C
+    uint32_t pitch;      // bytes per plane (2 rows * 16 B per block + 16)
     uint32_t split;      // bytes of one split (hi or lo) of a stage: 2 planes
-    uint32_t stage;      // bytes per stage: hi + lo
+    uint32_t stage;      // bytes per operand stage: hi + lo
+    uint32_t raw;        // bytes per raw stage: rows * 16 samples * 8 B
     int tcount;          // core matrices of the tap strip
-    uint32_t taps_hi, taps_lo, stages0, bytes;
+    uint32_t taps_hi, taps_lo, raw0, stages0, bytes;
 };
 
 __host__ __device__ inline Layout tc_layout(int num_taps, int stages)
 {
     Layout l;
     l.C = (num_taps + kB - 2) / kB;
-    l.W = 2 * (kNB + l.C);
-    l.pitch = static_cast<uint32_t>(l.W) * 16u + 16u;
+    l.rows = kNB + l.C;
+    l.pitch = static_cast<uint32_t>(2 * l.rows) * 16u + 16u;
     l.split = 2u * l.pitch;
     l.stage = 2u * l.split;
+    l.raw = static_cast<uint32_t>(l.rows) * 128u;
     l.tcount = 16 * l.C + 31;
     l.taps_hi = 1024;
     l.taps_lo = l.taps_hi + 128u * static_cast<uint32_t>(l.tcount);
-    l.stages0 = (l.taps_lo + 128u * static_cast<uint32_t>(l.tcount) + 127u) & ~127u;
+    l.raw0 = (l.taps_lo + 128u * static_cast<uint32_t>(l.tcount) + 127u) & ~127u;
+    l.stages0 = l.raw0 + kRaw * l.raw;
     l.bytes = l.stages0 + l.stage * static_cast<uint32_t>(stages);
     return l;
 }
@@ -87,15 +102,15 @@ __host__ __device__ inline Layout tc_layout(int num_taps, int stages)
 struct Ctrl {
     unsigned long long full[8];
     unsigned long long empty[8];
-    unsigned long long tmem_full[2];
-    unsigned long long tmem_empty[2];
-    unsigned long long scale_full[4];
+    unsigned long long raw_full[kRaw];
+    unsigned long long raw_empty[kRaw];
+    unsigned long long pfull[2];
+    unsigned long long pempty[2];
     unsigned long long reduce[2];
     unsigned long long teardown;
     uint32_t tmem_base;
     int abort;
-    int shift[4];             // output exponent shift per tile slot
-    uint32_t warp_max[2][kProducerWarps];
+    uint32_t warp_max[2][kWorkerWarps];
     uint32_t tap_max;
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
@@ -124,8 +139,26 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
         : "memory");
 }
 
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 2-D tiled TMA load of {32 floats, rows} at (x0, y0) into shared memory.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x0, int y0,
+                                            uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x0), "r"(y0), "r"(bar)
+        : "memory");
+}
 
 // 2^e as a float for e in [-126, 127].
 __device__ __forceinline__ float exp2i(int e)
@@ -143,7 +176,7 @@ __device__ __forceinline__ int scale_exponent(uint32_t abs_bits)
     return 141 - static_cast<int>((abs_bits >> 23) & 0xFFu);
 }
 
-// hi/lo FP16 split of one value already scaled into range.
+// hi/lo FP16 split of two values already scaled into range.
 __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo)
 {
     const __half2 h = __floats2half2_rn(a, b);
@@ -158,12 +191,29 @@ __device__ __forceinline__ void sts32(uint32_t addr, uint32_t v)
     asm volatile("st.shared.b32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ float4 lds128(uint32_t addr)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr)
+                 : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint32_t absmax4(float4 v)
+{
+    return max(max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu),
+               max(__float_as_uint(v.z) & 0x7FFFFFFFu, __float_as_uint(v.w) & 0x7FFFFFFFu));
+}
+
 }  // namespace
 
 template <int S>
-__global__ void __launch_bounds__(kThreads, 1)
-fir_tc_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
-              float2* __restrict__ y, long long n, int num_taps, int num_tiles)
+__global__ void __maxnreg__(120)
+fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict__ x,
+              const float* __restrict__ taps, float2* __restrict__ y, long long n, int num_taps,
+              int num_tiles)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
@@ -174,20 +224,28 @@ fir_tc_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
     const uint32_t sbase = smem_u32(smem);
     volatile int* abort = &ctl.abort;
     unsigned int* fault = &g_fault_fir_tc;
+    const int groups = (C + kChunksPerGroup) / kChunksPerGroup;  // per K-step: ceil((C+1)/4)
+    // This block's tiles: blockIdx.x, + gridDim.x, ...; its K-steps are numbered u = 8 k + st.
+    const int my_tiles = static_cast<int>(blockIdx.x) < num_tiles
+                             ? (num_tiles - 1 - static_cast<int>(blockIdx.x)) / gridDim.x + 1
+                             : 0;
+    const int my_steps = my_tiles * kStagesPerTile;
+    const long long full_blocks = n / kB;  // rows the tensor map covers
 
-    // ---- setup: barriers, tensor memory, tap strip ----------------------------------------
+    // ---- setup: barriers, tensor memory, first raw copies, tap strip -----------------------
     if (threadIdx.x == 0) {
         for (int i = 0; i < S; ++i) {
-            mbar_init(smem_u32(&ctl.full[i]), kProducerWarps);
+            mbar_init(smem_u32(&ctl.full[i]), kWorkerWarps);
             mbar_init(smem_u32(&ctl.empty[i]), 1);
         }
-        for (int i = 0; i < 2; ++i) {
-            mbar_init(smem_u32(&ctl.tmem_full[i]), 1);
-            mbar_init(smem_u32(&ctl.tmem_empty[i]), 4);
-            mbar_init(smem_u32(&ctl.reduce[i]), kProducerWarps);
+        for (int i = 0; i < kRaw; ++i) {
+            mbar_init(smem_u32(&ctl.raw_full[i]), 1);
+            mbar_init(smem_u32(&ctl.raw_empty[i]), kWorkerWarps);
         }
-        for (int i = 0; i < 4; ++i) {
-            mbar_init(smem_u32(&ctl.scale_full[i]), 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(smem_u32(&ctl.pfull[i]), 1);
+            mbar_init(smem_u32(&ctl.pempty[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
         }
         mbar_init(smem_u32(&ctl.teardown), 1);
         ctl.abort = 0;
@@ -201,6 +259,17 @@ fir_tc_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     __syncthreads();
+    // Raw sample stages 0 .. kRaw-1. K-step u is tile k = u / 8: window rows from block
+    // j0 - C, samples 16 (u % 8) .. +15 of each block, i.e. floats 32 (u % 8) .. +31.
+    if (threadIdx.x == 0) {
+        for (int u = 0; u < kRaw && u < my_steps; ++u) {
+            const int tile = static_cast<int>(blockIdx.x) + (u / kStagesPerTile) * gridDim.x;
+            const uint32_t bar = smem_u32(&ctl.raw_full[u]);
+            mbar_arrive_expect_tx(bar, lay.raw);
+            tma_load_2d(sbase + lay.raw0 + u * lay.raw, &xmap, 32 * (u % kStagesPerTile),
+                        tile * kNB - C, bar);
+        }
+    }
     // Largest tap magnitude (bit pattern of |h|: ordered like the value).
     {
         uint32_t m = 0;
@@ -241,198 +310,241 @@ fir_tc_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
     tc_fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    if (warp < kProducerWarps) {
-        // ---- producers ---------------------------------------------------------------------
-        const int ptid = threadIdx.x;
-        int it = 0;
-        for (int tile = blockIdx.x; tile < num_tiles && !*abort; tile += gridDim.x, ++it) {
+    if (warp < kWorkerWarps) {
+        // ---- workers ------------------------------------------------------------------------
+        const int quarter = warp & 3;
+        const int slice = warp >> 2;                       // columns kCols * slice .. +kCols-1
+        const int r = kB - 1 - (quarter * 32 + lane);      // output row of this TMEM lane
+        const uint32_t lane_addr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
+                                   static_cast<uint32_t>(slice * kCols);
+        const int wtid = threadIdx.x;                      // 0 .. kWorkers-1
+        int ex_ring[2] = {0, 0};                           // tile scale exponents, by tile parity
+
+        // Producing K-step v: the tile's scale on its first step, then raw -> FP16 planes.
+        auto produce = [&](int v) -> bool {
+            const int k = v / kStagesPerTile;
+            const int st = v % kStagesPerTile;
+            const int tile = static_cast<int>(blockIdx.x) + k * gridDim.x;
             const long long j0 = static_cast<long long>(tile) * kNB;
-            const long long win0 = (j0 - C) * kB;                       // first window sample
-            const long long lo_s = win0 > 0 ? win0 : 0;
-            const long long hi_s = (j0 + kNB) * kB < n ? (j0 + kNB) * kB : n;
-            // Phase A: the tile's largest |I| or |Q|.
-            uint32_t m = 0;
-            for (long long s = lo_s + 2 * ptid; s < hi_s; s += 2 * kProducers) {
-                if (s + 1 < hi_s) {
-                    const float4 v = __ldg(reinterpret_cast<const float4*>(x + s));
-                    m = max(m, max(max(__float_as_uint(v.x) & 0x7FFFFFFFu,
-                                       __float_as_uint(v.y) & 0x7FFFFFFFu),
-                                   max(__float_as_uint(v.z) & 0x7FFFFFFFu,
-                                       __float_as_uint(v.w) & 0x7FFFFFFFu)));
-                } else {
-                    const float2 v = __ldg(x + s);
-                    m = max(m, max(__float_as_uint(v.x) & 0x7FFFFFFFu,
-                                   __float_as_uint(v.y) & 0x7FFFFFFFu));
+            if (st == 0) {
+                const long long win0 = (j0 - C) * kB;
+                const long long lo_s = win0 > 0 ? win0 : 0;
+                const long long hi_s = (j0 + kNB) * kB < n ? (j0 + kNB) * kB : n;
+                uint32_t m = 0;
+                for (long long s = lo_s + 2 * wtid; s < hi_s; s += 2 * kWorkers) {
+                    if (s + 1 < hi_s) {
+                        m = max(m, absmax4(__ldg(reinterpret_cast<const float4*>(x + s))));
+                    } else {
+                        const float2 w2 = __ldg(x + s);
+                        m = max(m, max(__float_as_uint(w2.x) & 0x7FFFFFFFu,
+                                       __float_as_uint(w2.y) & 0x7FFFFFFFu));
+                    }
                 }
-            }
-            m = __reduce_max_sync(0xFFFFFFFFu, m);
-            const int rb = it & 1;
-            if (lane == 0) {
-                ctl.warp_max[rb][warp] = m;
-                mbar_arrive(smem_u32(&ctl.reduce[rb]));
-            }
-            if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (it >> 1) & 1, fault,
-                                   kFaultStageEmpty, abort)) {
-                break;
-            }
-            uint32_t tmax = 0;
+                m = __reduce_max_sync(0xFFFFFFFFu, m);
+                const int rb = k & 1;
+                if (lane == 0) {
+                    ctl.warp_max[rb][warp] = m;
+                    mbar_arrive(smem_u32(&ctl.reduce[rb]));
+                }
+                if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (k >> 1) & 1, fault,
+                                       kFaultStageEmpty, abort)) {
+                    return false;
+                }
+                uint32_t tmax = 0;
 #pragma unroll
-            for (int w = 0; w < kProducerWarps; ++w) {
-                tmax = max(tmax, ctl.warp_max[rb][w]);
+                for (int w = 0; w < kWorkerWarps; ++w) {
+                    tmax = max(tmax, ctl.warp_max[rb][w]);
+                }
+                ex_ring[k & 1] = scale_exponent(tmax);
             }
-            const int ex = scale_exponent(tmax);
-            if (ptid == 0) {
-                ctl.shift[it & 3] = -(ex + eh);
-                mbar_arrive(smem_u32(&ctl.scale_full[it & 3]));
-            }
+            const int ex = ex_ring[k & 1];
             const float fa = exp2i(ex / 2);
             const float fb = exp2i(ex - ex / 2);
-            // Phase B: one stage per 16-sample K-step.
-            const int rows = kNB + C;              // window blocks
-            const int items = rows * 8;            // float4 (two samples) per block row
-            for (int st = 0; st < kStagesPerTile; ++st) {
-                const int g = it * kStagesPerTile + st;
-                const int slot = g % S;
-                const int s0 = st * 16;
-                if (!mbar_wait_bounded(smem_u32(&ctl.empty[slot]), ((g / S) & 1) ^ 1, fault,
-                                       kFaultStageEmpty, abort)) {
-                    break;
-                }
-                const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
-                for (int f = ptid; f < items; f += kProducers) {
-                    const int b = f >> 3;
-                    const int q = f & 7;
-                    const long long sidx = (j0 - C + b) * kB + s0 + 2 * q;
-                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (sidx >= 0 && sidx + 1 < n) {
-                        v = __ldg(reinterpret_cast<const float4*>(x + sidx));
-                    } else if (sidx >= 0 && sidx < n) {
-                        const float2 w = __ldg(x + sidx);
-                        v.x = w.x;
-                        v.y = w.y;
-                    }
-                    uint32_t re_hi, re_lo, im_hi, im_lo;
-                    split2(v.x * fa * fb, v.z * fa * fb, re_hi, re_lo);
-                    split2(v.y * fa * fb, v.w * fa * fb, im_hi, im_lo);
-                    const uint32_t plane = static_cast<uint32_t>(q >> 2) * lay.pitch;
-                    const uint32_t elem = static_cast<uint32_t>(q & 3) * 4u;
-                    const uint32_t row_re = plane + static_cast<uint32_t>(2 * b) * 16u + elem;
-                    sts32(stage + row_re, re_hi);
-                    sts32(stage + row_re + 16u, im_hi);
-                    sts32(stage + lay.split + row_re, re_lo);
-                    sts32(stage + lay.split + row_re + 16u, im_lo);
-                }
-                fence_proxy_async_smem();
-                __syncwarp();
-                if (lane == 0) {
-                    mbar_arrive(smem_u32(&ctl.full[slot]));
-                }
+            const int slot = v % S;
+            const int rslot = v % kRaw;
+            if (!mbar_wait_bounded(smem_u32(&ctl.empty[slot]), ((v / S) & 1) ^ 1, fault,
+                                   kFaultStageEmpty, abort) ||
+                !mbar_wait_bounded(smem_u32(&ctl.raw_full[rslot]), (v / kRaw) & 1, fault,
+                                   kFaultTileLoad, abort)) {
+                return false;
             }
-        }
-    } else if (warp >= kEpilogueWarp0 && warp < kEpilogueWarp0 + 4) {
-        // ---- epilogue: TMEM lane quarter (warp % 4) ----------------------------------------
-        const int quarter = warp & 3;
-        const int lane_row = quarter * 32 + lane;          // TMEM lane = reversed output row
-        const int r = kB - 1 - lane_row;                   // output index within the block
-        int it = 0;
-        for (int tile = blockIdx.x; tile < num_tiles && !*abort; tile += gridDim.x, ++it) {
-            const int d = it & 1;
-            if (!mbar_wait_bounded(smem_u32(&ctl.scale_full[it & 3]), (it >> 2) & 1, fault,
-                                   kFaultScale, abort)) {
-                break;
-            }
-            const int shift = ctl.shift[it & 3];
-            const float fa = exp2i(shift / 2);
-            const float fb = exp2i(shift - shift / 2);
-            if (!mbar_wait_bounded(smem_u32(&ctl.tmem_full[d]), (it >> 1) & 1, fault,
-                                   kFaultAccumFull, abort)) {
-                break;
-            }
-            tc_fence_after();
-            const long long j0 = static_cast<long long>(tile) * kNB;
-            const uint32_t taddr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
-                                   static_cast<uint32_t>(d * kN);
-#pragma unroll 1
-            for (int chunk = 0; chunk < kN / 32; ++chunk) {
-                uint32_t v[32];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                      "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                      "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
-                      "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]),
-                      "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                    : "r"(taddr + static_cast<uint32_t>(chunk * 32)));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                for (int b = 0; b < 16; ++b) {
-                    const long long o = (j0 + chunk * 16 + b) * kB + r;
-                    if (o < n) {
-                        y[o] = make_float2(__uint_as_float(v[2 * b]) * fa * fb,
-                                           __uint_as_float(v[2 * b + 1]) * fa * fb);
+            const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
+            const uint32_t raw = sbase + lay.raw0 + static_cast<uint32_t>(rslot) * lay.raw;
+            const int items = lay.rows * 8;  // float4 (two samples) per window row
+            for (int f = wtid; f < items; f += kWorkers) {
+                const int b = f >> 3;
+                const int q = f & 7;
+                const long long jb = j0 - C + b;
+                float4 v4;
+                if (jb != full_blocks) {
+                    v4 = lds128(raw + static_cast<uint32_t>(f) * 16u);  // zero outside [0, n)
+                } else {
+                    // The input's last, partial block is outside the tensor map: plain loads.
+                    const long long sidx = jb * kB + 16 * st + 2 * q;
+                    v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (sidx + 1 < n) {
+                        v4 = __ldg(reinterpret_cast<const float4*>(x + sidx));
+                    } else if (sidx < n) {
+                        const float2 w2 = __ldg(x + sidx);
+                        v4.x = w2.x;
+                        v4.y = w2.y;
                     }
                 }
+                uint32_t re_hi, re_lo, im_hi, im_lo;
+                split2(v4.x * fa * fb, v4.z * fa * fb, re_hi, re_lo);
+                split2(v4.y * fa * fb, v4.w * fa * fb, im_hi, im_lo);
+                const uint32_t plane = static_cast<uint32_t>(q >> 2) * lay.pitch;
+                const uint32_t elem = static_cast<uint32_t>(q & 3) * 4u;
+                const uint32_t row_re = plane + static_cast<uint32_t>(2 * b) * 16u + elem;
+                sts32(stage + row_re, re_hi);
+                sts32(stage + row_re + 16u, im_hi);
+                sts32(stage + lay.split + row_re, re_lo);
+                sts32(stage + lay.split + row_re + 16u, im_lo);
             }
-            tc_fence_before();
+            fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {
-                mbar_arrive(smem_u32(&ctl.tmem_empty[d]));
+                mbar_arrive(smem_u32(&ctl.full[slot]));
+                mbar_arrive(smem_u32(&ctl.raw_empty[rslot]));
+            }
+            // Refill this raw slot with K-step v + kRaw once every warp has converted it.
+            if (wtid == 0 && v + kRaw < my_steps) {
+                if (!mbar_wait_bounded(smem_u32(&ctl.raw_empty[rslot]), (v / kRaw) & 1, fault,
+                                       kFaultStageEmpty, abort)) {
+                    return false;
+                }
+                const int vn = v + kRaw;
+                const int tile_n =
+                    static_cast<int>(blockIdx.x) + (vn / kStagesPerTile) * gridDim.x;
+                const uint32_t bar = smem_u32(&ctl.raw_full[rslot]);
+                mbar_arrive_expect_tx(bar, lay.raw);
+                tma_load_2d(raw, &xmap, 32 * (vn % kStagesPerTile), tile_n * kNB - C, bar);
+            }
+            return true;
+        };
+
+        bool ok = true;
+        for (int v = 0; v < S && v < my_steps && ok; ++v) {
+            ok = produce(v);
+        }
+        float acc[kCols];
+#pragma unroll
+        for (int i = 0; i < kCols; ++i) {
+            acc[i] = 0.0f;
+        }
+        for (int u = 0; u < my_steps && ok && !*abort; ++u) {
+            // Drain the partial sums of K-step u's groups into the running sums.
+            for (int gi = 0; gi < groups; ++gi) {
+                const int g = u * groups + gi;
+                const int pb = g & 1;
+                if (!mbar_wait_bounded(smem_u32(&ctl.pfull[pb]), (g >> 1) & 1, fault,
+                                       kFaultAccumFull, abort)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+#pragma unroll
+                for (int c16 = 0; c16 < kCols / 16; ++c16) {
+                    uint32_t t[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]),
+                          "=r"(t[5]), "=r"(t[6]), "=r"(t[7]), "=r"(t[8]), "=r"(t[9]),
+                          "=r"(t[10]), "=r"(t[11]), "=r"(t[12]), "=r"(t[13]), "=r"(t[14]),
+                          "=r"(t[15])
+                        : "r"(lane_addr + static_cast<uint32_t>(pb * kN + c16 * 16)));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        acc[c16 * 16 + i] += __uint_as_float(t[i]);
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(&ctl.pempty[pb]));
+                }
+            }
+            if (!ok) {
+                break;
+            }
+            const int k = u / kStagesPerTile;
+            if (u % kStagesPerTile == kStagesPerTile - 1) {
+                // Last K-step of tile k: scale and store this thread's outputs.
+                const int shift = -(ex_ring[k & 1] + eh);
+                const float fa = exp2i(shift / 2);
+                const float fb = exp2i(shift - shift / 2);
+                const long long jb0 =
+                    static_cast<long long>(static_cast<int>(blockIdx.x) + k * gridDim.x) * kNB +
+                    slice * (kCols / 2);
+#pragma unroll
+                for (int b = 0; b < kCols / 2; ++b) {
+                    const long long o = (jb0 + b) * kB + r;
+                    if (o < n) {
+                        y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
+                    }
+                    acc[2 * b] = 0.0f;
+                    acc[2 * b + 1] = 0.0f;
+                }
+            }
+            if (u + S < my_steps) {
+                ok = produce(u + S);
             }
         }
-    } else if (warp == kMmaWarp && lane == 0) {
-        // ---- MMA issuer ----------------------------------------------------------------------
+    } else if (lane == 0) {
+        // ---- MMA issuer (warp 16, one thread) ----------------------------------------------
         const uint32_t taps_hi = sbase + lay.taps_hi;
         const uint32_t taps_lo = sbase + lay.taps_lo;
-        int it = 0;
-        bool issued = false;
-        for (int tile = blockIdx.x; tile < num_tiles && !*abort; tile += gridDim.x, ++it) {
-            const int d = it & 1;
-            if (!mbar_wait_bounded(smem_u32(&ctl.tmem_empty[d]), ((it >> 1) & 1) ^ 1, fault,
-                                   kFaultAccumEmpty, abort)) {
+        bool stop = false;
+        for (int u = 0; u < my_steps && !stop && !*abort; ++u) {
+            const int slot = u % S;
+            if (!mbar_wait_bounded(smem_u32(&ctl.full[slot]), (u / S) & 1, fault,
+                                   kFaultStageFull, abort)) {
                 break;
             }
             tc_fence_after();
-            const uint32_t dt = tmem + static_cast<uint32_t>(d * kN);
-            bool stop = false;
-            for (int st = 0; st < kStagesPerTile; ++st) {
-                const int g = it * kStagesPerTile + st;
-                const int slot = g % S;
-                if (!mbar_wait_bounded(smem_u32(&ctl.full[slot]), (g / S) & 1, fault,
-                                       kFaultStageFull, abort)) {
+            const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
+            const int s0 = (u % kStagesPerTile) * 16;
+            for (int gi = 0; gi < groups; ++gi) {
+                const int g = u * groups + gi;
+                const int pb = g & 1;
+                if (!mbar_wait_bounded(smem_u32(&ctl.pempty[pb]), ((g >> 1) & 1) ^ 1, fault,
+                                       kFaultAccumEmpty, abort)) {
                     stop = true;
                     break;
                 }
                 tc_fence_after();
-                const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
-                const int s0 = st * 16;
-                for (int c = 0; c <= C; ++c) {
+                const uint32_t dt = tmem + static_cast<uint32_t>(pb * kN);
+                const int c0 = gi * kChunksPerGroup;
+                const int c1 = c0 + kChunksPerGroup <= C + 1 ? c0 + kChunksPerGroup : C + 1;
+                for (int c = c0; c < c1; ++c) {
                     const uint32_t t0 = static_cast<uint32_t>(16 * (C - c) + s0 / 8) * 128u;
                     const unsigned long long a_hi = smem_desc(taps_hi + t0, 128, 128);
                     const unsigned long long a_lo = smem_desc(taps_lo + t0, 128, 128);
                     const uint32_t row0 = static_cast<uint32_t>(2 * (C - c)) * 16u;
                     const unsigned long long b_hi = smem_desc(stage + row0, lay.pitch, 128);
-                    const unsigned long long b_lo = smem_desc(stage + lay.split + row0, lay.pitch, 128);
-                    mma_f16(dt, a_hi, b_hi, (st > 0 || c > 0) ? 1u : 0u);
+                    const unsigned long long b_lo =
+                        smem_desc(stage + lay.split + row0, lay.pitch, 128);
+                    mma_f16(dt, a_hi, b_hi, c > c0 ? 1u : 0u);
                     mma_f16(dt, a_hi, b_lo, 1u);
                     mma_f16(dt, a_lo, b_hi, 1u);
-                    issued = true;
                 }
-                mma_commit(smem_u32(&ctl.empty[slot]));
+                mma_commit(smem_u32(&ctl.pfull[pb]));
             }
-            if (stop) {
-                break;
-            }
-            mma_commit(smem_u32(&ctl.tmem_full[d]));
+            mma_commit(smem_u32(&ctl.empty[slot]));
         }
         // Every MMA this thread issued has completed before tensor memory is released.
         mma_commit(smem_u32(&ctl.teardown));
-        (void)issued;
         mbar_wait_bounded(smem_u32(&ctl.teardown), 0, fault, kFaultTeardown, nullptr);
     }
 
+    // After a give-up, raw copies may still be in flight: give them time to land (bounded).
+    if (threadIdx.x == 0 && *abort) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (globaltimer_ns() - t0 < 2000000ull) {
+        }
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -444,7 +556,8 @@ fir_tc_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
 
 bool fir_tc_supported(int num_taps)
 {
-    return num_taps > 1 && tc_layout(num_taps, 4).bytes <= 227u * 1024u;
+    const Layout l = tc_layout(num_taps, 2);
+    return num_taps > 1 && l.bytes <= 227u * 1024u && l.rows <= 256;
 }
 
 template <int S>
@@ -465,13 +578,20 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
             cudaSuccess) {
         return err;
     }
-    if (lay.bytes > static_cast<uint32_t>(optin)) {
-        return cudaErrorInvalidValue;
-    }
     // At least 120 KB per block keeps one block per SM: each block owns all 512 TMEM columns.
     const uint32_t bytes = lay.bytes > 120u * 1024u ? lay.bytes : 120u * 1024u;
+    if (bytes > static_cast<uint32_t>(optin)) {
+        return cudaErrorInvalidValue;
+    }
     err = cudaFuncSetAttribute(fir_tc_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(bytes));
+    if (err != cudaSuccess) {
+        return err;
+    }
+    // x viewed as rows of 256 floats (one 128-sample block per row), full blocks only; boxes
+    // of 32 floats (16 samples) by the tile's window rows.
+    CUtensorMap map;
+    err = encode_rows_f32(&map, x, n / kB, 2 * kB, 32, static_cast<uint32_t>(lay.rows));
     if (err != cudaSuccess) {
         return err;
     }
@@ -479,7 +599,7 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
     const int tiles = static_cast<int>((blocks + kNB - 1) / kNB);
     const int grid = tiles < sms ? tiles : sms;
     fir_tc_kernel<S><<<grid, kThreads, bytes, stream>>>(
-        static_cast<const float2*>(x), taps, static_cast<float2*>(y), n, num_taps, tiles);
+        map, static_cast<const float2*>(x), taps, static_cast<float2*>(y), n, num_taps, tiles);
     return cudaGetLastError();
 }
 
@@ -492,10 +612,17 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
     if (!fir_tc_supported(num_taps)) {
         return cudaErrorInvalidValue;
     }
+    if (n < kB) {
+        // Shorter than one block: the tensor map would be empty; the plain kernel is exact.
+        return fir_plain_launch(x, taps, y, n, num_taps, stream);
+    }
     if (config.stages >= 6 && tc_layout(num_taps, 6).bytes <= 227u * 1024u) {
         return launch_stages<6>(x, taps, y, n, num_taps, stream);
     }
-    return launch_stages<4>(x, taps, y, n, num_taps, stream);
+    if (tc_layout(num_taps, 4).bytes <= 227u * 1024u) {
+        return launch_stages<4>(x, taps, y, n, num_taps, stream);
+    }
+    return launch_stages<2>(x, taps, y, n, num_taps, stream);
 }
 
 cudaError_t fir_tc_take_fault(unsigned int* code)
