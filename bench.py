@@ -224,15 +224,68 @@ def peaks() -> dict:
             "source": "fallback"}
 
 
-def pick_fir_impl(rfx, x, h, y) -> str:
-    """The tensor-core form when this library has it, else the plain kernel."""
+class Arm:
+    """One implementation on one workload: its device buffers and one step's launch."""
+
+    def __init__(self, rfx, w, impl: str, device) -> None:
+        import torch
+
+        self.rfx, self.w, self.impl = rfx, w, impl
+        n = int(w.x.size)
+        self.n = n
+        self.xs = [torch.from_numpy(w.x).to(device) for _ in range(2)]
+        self.h = torch.from_numpy(w.taps).to(device)
+        if w.channels:
+            m = w.channels
+            f = rfx.frames(n, m)
+            self.outs = [torch.empty((f, m), dtype=torch.complex64, device=device)
+                         for _ in range(2)]
+            self.plan = rfx.ChanPlan(m, n, impl)
+            # plain: the branch kernel and cuFFT's inverse transform (counted as one of ours)
+            self.launches_per_step = 2 if impl == "plain" else 1
+        else:
+            self.outs = [torch.empty_like(self.xs[0]) for _ in range(2)]
+            self.launches_per_step = 1
+        self.dtype = "f16x3->f32" if impl == "tc_split" else "f32"
+
+    def launch(self, i: int) -> None:
+        if self.w.channels:
+            self.plan.launch(self.xs[i % 2], self.h, self.outs[i % 2])
+        else:
+            self.rfx.fir_launch(self.impl, self.xs[i % 2], self.h, self.outs[i % 2])
+
+    def error(self) -> float:
+        """Normwise error of this arm's output against the float64 oracle, first 2^18 samples."""
+        import torch
+        from oracle import rf_oracle as orc
+
+        w = self.w
+        self.launch(0)
+        torch.cuda.synchronize()
+        check_n = min(self.n, 1 << 18)
+        if w.channels:
+            frames = check_n // w.channels
+            got = self.outs[0][:frames].cpu().numpy()
+            ref = orc.channelize_fast(w.x[: frames * w.channels], w.taps, w.channels)
+            return orc.normwise_error(got, ref)
+        got = self.outs[0][:check_n].cpu().numpy()
+        return orc.normwise_error(got, orc.fir_fast(w.x[:check_n], w.taps))
+
+    def release(self) -> None:
+        self.xs = self.outs = None
+        if self.w.channels:
+            self.plan.close()
+
+
+def available(rfx, w, impl: str, device) -> bool:
+    """Whether this library can run `impl` on workload `w` (tries one launch)."""
     try:
-        rfx.fir_launch("tc_split", x, h, y)
-        return "tc_split"
-    except rfx.RfxError as e:
-        if e.status == 4 and "not supported" in str(e):
-            return "plain"
-        raise
+        arm = Arm(rfx, w, impl, device)
+        arm.launch(0)
+        arm.release()
+        return True
+    except rfx.RfxError:
+        return False
 
 
 def time_device(launch, steps: int, warmup: int, dist, device) -> float:
@@ -345,103 +398,111 @@ def run_reference(args) -> None:
 
 # --- our arm ---------------------------------------------------------------------------------
 
+def measure_arms(rfx, w, impls, args, dist, device, sample_clocks=False):
+    """Times every available implementation of workload `w`; returns {impl: result}."""
+    out = {}
+    clocks = None
+    for impl in impls:
+        if not available(rfx, w, impl, device):
+            continue
+        arm = Arm(rfx, w, impl, device)
+        if sample_clocks and clocks is None:
+            with ClockSampler(device.index if device.index is not None else 0) as cs:
+                seconds = time_device(arm.launch, args.steps, args.warmup, dist, device)
+            clocks = cs.summary()
+        else:
+            seconds = time_device(arm.launch, args.steps, args.warmup, dist, device)
+        kernel_s = kernel_average_s(arm.launch, max(3, min(args.steps, 10)))
+        world = dist.get_world_size() if dist is not None else 1
+        out[impl] = {"msamples_s": world * arm.n * args.steps / seconds / 1e6,
+                     "ms_per_step": seconds / args.steps * 1e3, "kernel_s": kernel_s,
+                     "seconds": seconds, "launches_per_step": arm.launches_per_step,
+                     "dtype": arm.dtype, "max_rel_err_vs_f64": arm.error()}
+        arm.release()
+    return out, clocks
+
+
 def run_ours(args) -> None:
     import torch
 
     import rfx
-    from oracle import rf_oracle as orc
 
     rank, world, local = dist_env()
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
     dist = init_dist(world, "nccl")
     rfx.load()
+    pk = peaks()
 
     w = load_workload(args.workload)
     n = int(w.x.size)
-    xs = [torch.from_numpy(w.x).to(device) for _ in range(2)]
-    h = torch.from_numpy(w.taps).to(device)
-    pk = peaks()
-    launches_per_step = 1
-    extras: dict = {}
-
-    if w.channels:
-        m = w.channels
-        frames = rfx.frames(n, m)
-        outs = [torch.empty((frames, m), dtype=torch.complex64, device=device) for _ in range(2)]
-        impl = "plain"
-        plan = rfx.ChanPlan(m, n, impl)
-        launches_per_step = 2  # branch kernel + the cuFFT inverse transform
-
-        def launch(i: int) -> None:
-            plan.launch(xs[i % 2], h, outs[i % 2])
-
-        dtype = "f32"
-    else:
-        ys = [torch.empty_like(xs[0]) for _ in range(2)]
-        impl = pick_fir_impl(rfx, xs[0], h, ys[0])
-
-        def launch(i: int) -> None:
-            rfx.fir_launch(impl, xs[i % 2], h, ys[i % 2])
-
-        dtype = "f16x3->f32" if impl == "tc_split" else "f32"
-
-    with ClockSampler(device.index if device.index is not None else 0) as clocks:
-        seconds = time_device(launch, args.steps, args.warmup, dist, device)
-    kernel_s = kernel_average_s(launch, max(3, min(args.steps, 10)))
-    value = world * n * args.steps / seconds / 1e6
-
-    # Accuracy of this run's output against the float64 oracle, on a prefix (rank 0).
-    err = None
-    if rank == 0:
-        check_n = min(n, 1 << 18)
-        if w.channels:
-            got = outs[0].reshape(-1)[: (check_n // w.channels) * w.channels].cpu().numpy()
-            ref = orc.channelize_fast(w.x[:check_n], w.taps, w.channels).reshape(-1)
-            err = orc.normwise_error(got, ref[: got.size])
-        else:
-            launch(0)
-            torch.cuda.synchronize()
-            got = ys[0][:check_n].cpu().numpy()
-            err = orc.normwise_error(got, orc.fir_fast(w.x[:check_n], w.taps))
+    arms, clocks = measure_arms(rfx, w, ["tc_split", "plain"], args, dist, device,
+                                sample_clocks=True)
+    impl = next(iter(arms))
+    prim = arms[impl]
+    value = prim["msamples_s"]
+    kernel_s = prim["kernel_s"]
 
     # Roofline of the dominant kernel.
+    extras: dict = {}
+    if w.channels:
+        useful = 4.0 * n * (-(-w.taps.size // w.channels))  # branch FIR flops
+    else:
+        useful = 4.0 * n * w.taps.size                       # FIR flops
     algo_bytes = 16.0 * n  # 8 B read + 8 B written per sample
     achieved_gbs = algo_bytes / kernel_s / 1e9
-    flops = 4.0 * n * (w.taps.size if not w.channels else
-                       (-(-w.taps.size // w.channels)))  # useful FIR / branch flops
-    if impl == "tc_split":
-        roofline = {"bound": "tensor", "achieved": flops / kernel_s / 1e12,
+    if impl == "tc_split" and not w.channels:
+        roofline = {"bound": "tensor", "achieved": useful / kernel_s / 1e12,
                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                    "frac": flops / kernel_s / 1e12 / pk["bf16_tflops"], "traffic": None}
+                    "frac": useful / kernel_s / 1e12 / pk["bf16_tflops"], "traffic": None,
+                    "note": "useful FIR flops 4*N*K; executed tensor flops are "
+                            "3*4*N*(128+128*C) with C = floor((K+126)/128)"}
+        c = (w.taps.size + 126) // 128
+        executed = 3.0 * 4.0 * n * 128 * (c + 1)
+        extras["tensor_executed_tflops"] = executed / kernel_s / 1e12
     else:
         roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"],
                     "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None}
     roofline["peak_source"] = pk["source"]
-    if not w.channels:
-        sm_mhz = clocks.summary().get("sm_mhz") or 1900.0
+    if "plain" in arms and not w.channels:
+        sm_mhz = (clocks or {}).get("sm_mhz") or 1900.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-        extras["fp32_simt"] = {"achieved_tflops": flops / kernel_s / 1e12,
-                               "peak_tflops_at_sampled_clock": fp32_peak,
-                               "frac": flops / kernel_s / 1e12 / fp32_peak}
+        ks = arms["plain"]["kernel_s"]
+        extras["plain_fp32_simt"] = {"achieved_tflops": useful / ks / 1e12,
+                                     "peak_tflops_at_sampled_clock": fp32_peak,
+                                     "frac": useful / ks / 1e12 / fp32_peak}
+    compare = {k: {kk: vv for kk, vv in v.items() if kk not in ("seconds",)}
+               for k, v in arms.items()}
+    if "plain" in arms and impl != "plain":
+        extras["speedup_vs_plain_fp32"] = value / arms["plain"]["msamples_s"]
+
+    # The other headline workload (64-channel PFB) in the same run.
+    if args.workload == "fir1025" and not args.no_secondary:
+        w2 = load_workload("pfb64")
+        arms2, _ = measure_arms(rfx, w2, ["tc_split", "plain"], args, dist, device)
+        extras["pfb64"] = {k: {kk: vv for kk, vv in v.items() if kk != "seconds"}
+                           for k, v in arms2.items()}
+        if "plain" in arms2 and len(arms2) > 1:
+            first = next(iter(arms2))
+            extras["pfb64"]["speedup_vs_plain_fp32"] = (
+                arms2[first]["msamples_s"] / arms2["plain"]["msamples_s"])
+        del w2
 
     # End to end through the public host-buffer call, pinned host memory.
     e2e = None
     if rank == 0:
         xp = torch.from_numpy(w.x).pin_memory()
+        b = rfx.Bench(warmup=args.warmup, runs=args.steps)
+        lib = rfx.load()
         if w.channels:
-            zp = torch.empty(rfx.frames(n, w.channels) * w.channels, dtype=torch.complex64
-                             ).pin_memory()
-            b = rfx.Bench(warmup=args.warmup, runs=args.steps)
-            lib = rfx.load()
+            zp = torch.empty(rfx.frames(n, w.channels) * w.channels,
+                             dtype=torch.complex64).pin_memory()
             rfx._check(lib.rfx_channelize_host(rfx.parse_chan_impl(impl), xp.data_ptr(), n,
                                                w.taps.ctypes.data, w.taps.size, w.channels,
                                                zp.data_ptr(), rfx.ctypes.byref(b)))
             d2h = zp.numel() * 8
         else:
             yp = torch.empty_like(xp).pin_memory()
-            b = rfx.Bench(warmup=args.warmup, runs=args.steps)
-            lib = rfx.load()
             rfx._check(lib.rfx_fir_host(rfx.parse_fir_impl(impl), xp.data_ptr(), n,
                                         w.taps.ctypes.data, w.taps.size, 256, yp.data_ptr(),
                                         rfx.ctypes.byref(b)))
@@ -463,18 +524,20 @@ def run_ours(args) -> None:
         line = {
             "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": seconds / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "ms_per_step": prim["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": prim["dtype"],
+            "data": "synthetic",
             "config": {"workload": w.name, "impl": impl, "samples": n,
                        "taps": int(w.taps.size), "channels": w.channels or None,
                        "l2": "inputs larger than L2: two 268 MB buffer sets alternate",
                        "seed": w.meta.get("seed")},
-            "max_rel_err_vs_f64": err,
+            "max_rel_err_vs_f64": prim["max_rel_err_vs_f64"],
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "clocks": clocks.summary(),
-            "gpu_launches": args.steps * launches_per_step,
+            "clocks": clocks,
+            "gpu_launches": args.steps * prim["launches_per_step"],
+            "compare": compare,
             **extras,
         }
         print(json.dumps(line), flush=True)
@@ -490,6 +553,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="fir1025", choices=["fir1025", "fir63", "pfb64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the 64-channel PFB measured beside the FIR")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

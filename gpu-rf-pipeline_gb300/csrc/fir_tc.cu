@@ -210,7 +210,7 @@ __device__ __forceinline__ uint32_t absmax4(float4 v)
 }  // namespace
 
 template <int S>
-__global__ void __maxnreg__(120)
+__global__ void __maxnreg__(112)
 fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict__ x,
               const float* __restrict__ taps, float2* __restrict__ y, long long n, int num_taps,
               int num_tiles)
@@ -582,6 +582,14 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
     const uint32_t bytes = lay.bytes > 120u * 1024u ? lay.bytes : 120u * 1024u;
     if (bytes > static_cast<uint32_t>(optin)) {
         return cudaErrorInvalidValue;
+    }
+    // The block's warps must fit the register file at this register count.
+    cudaFuncAttributes attr{};
+    if ((err = cudaFuncGetAttributes(&attr, fir_tc_kernel<S>)) != cudaSuccess) {
+        return err;
+    }
+    if (attr.maxThreadsPerBlock < kThreads) {
+        return cudaErrorLaunchOutOfResources;
     }
     err = cudaFuncSetAttribute(fir_tc_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(bytes));

@@ -3,6 +3,7 @@
 #include "rfx.h"
 
 #include "chan_plain.cuh"
+#include "chan_tc.cuh"
 #include "fir_plain.cuh"
 #include "fir_tc.cuh"
 #include "tuning.hpp"
@@ -132,6 +133,7 @@ struct rfx_chan_plan {
     int64_t frames;       // cuFFT batch (plain); maximum frames (tensor core)
     cufftHandle fft;
     bool has_fft;
+    void* twiddles;       // tensor core: the DFT operand image, built once in FP64
 };
 
 extern "C" {
@@ -158,6 +160,11 @@ int rfx_device_fault(unsigned int* code)
     part = 0;
     if ((err = rfx::fir_tc_take_fault(&part)) != cudaSuccess) {
         return cuda_fail(err, "fir_tc fault word");
+    }
+    total |= part;
+    part = 0;
+    if ((err = rfx::chan_tc_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "chan_tc fault word");
     }
     total |= part;
     *code = total;
@@ -340,7 +347,7 @@ int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_p
     }
     *plan = nullptr;
     if (impl == RFX_CHAN_AUTO) {
-        impl = RFX_CHAN_PLAIN;
+        impl = rfx::chan_tc_supported(channels, 1) ? RFX_CHAN_TC : RFX_CHAN_PLAIN;
     }
     if (impl != RFX_CHAN_PLAIN && impl != RFX_CHAN_TC) {
         return fail(RFX_ERR_INVALID, "channelize: unknown implementation %d", impl);
@@ -352,13 +359,30 @@ int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_p
         return fail(RFX_ERR_INVALID, "channelize: %lld samples, expected 0 to %lld",
                     static_cast<long long>(max_samples), static_cast<long long>(kMaxSamples));
     }
-    if (impl == RFX_CHAN_TC) {
-        return fail(RFX_ERR_CAPACITY, "channelize: the tensor-core form is not available for "
-                                      "%d channels",
-                    channels);
-    }
     auto* p = new rfx_chan_plan{impl, channels, rfx_channelize_frames(max_samples, channels), 0,
-                                false};
+                                false, nullptr};
+    if (impl == RFX_CHAN_TC) {
+        if (!rfx::chan_tc_supported(channels, 1)) {
+            delete p;
+            return fail(RFX_ERR_CAPACITY, "channelize: the tensor-core form takes 64 channels, "
+                                          "not %d",
+                        channels);
+        }
+        cudaError_t err = cudaMalloc(&p->twiddles, rfx::chan_tc_twiddle_bytes());
+        if (err == cudaSuccess) {
+            err = rfx::chan_tc_build_twiddles(p->twiddles, nullptr);
+        }
+        if (err == cudaSuccess) {
+            err = cudaDeviceSynchronize();
+        }
+        if (err != cudaSuccess) {
+            cudaFree(p->twiddles);
+            delete p;
+            return cuda_fail(err, "channelizer twiddles");
+        }
+        *plan = p;
+        return RFX_OK;
+    }
     if (p->frames > 0) {
         int nfft = channels;
         const cufftResult r = cufftPlanMany(&p->fft, 1, &nfft, nullptr, 1, nfft, nullptr, 1,
@@ -381,6 +405,9 @@ int rfx_chan_plan_destroy(rfx_chan_plan* plan)
     cufftResult r = CUFFT_SUCCESS;
     if (plan->has_fft) {
         r = cufftDestroy(plan->fft);
+    }
+    if (plan->twiddles != nullptr) {
+        cudaFree(plan->twiddles);
     }
     delete plan;
     return r == CUFFT_SUCCESS ? RFX_OK : cufft_fail(r, "cufftDestroy");
@@ -409,6 +436,21 @@ int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps,
     if (!aligned16(x) || !aligned16(out)) {
         return fail(RFX_ERR_ALIGNMENT, "channelize: sample buffers must be 16-byte aligned");
     }
+    if (plan->impl == RFX_CHAN_TC) {
+        if (frames > plan->frames) {
+            return fail(RFX_ERR_INVALID, "channelize: plan made for up to %lld frames, call has "
+                                         "%lld",
+                        static_cast<long long>(plan->frames), static_cast<long long>(frames));
+        }
+        if (!rfx::chan_tc_supported(plan->channels, num_taps)) {
+            return fail(RFX_ERR_CAPACITY, "channelize: %d taps exceed the tensor-core form's "
+                                          "shared memory",
+                        num_taps);
+        }
+        const cudaError_t err = rfx::chan_tc_launch(x, taps, plan->twiddles, out, num_samples,
+                                                    num_taps, stream);
+        return err == cudaSuccess ? RFX_OK : cuda_fail(err, "chan_tc_launch");
+    }
     if (frames != plan->frames) {
         return fail(RFX_ERR_INVALID, "channelize: plan made for %lld frames, call has %lld",
                     static_cast<long long>(plan->frames), static_cast<long long>(frames));
@@ -425,6 +467,31 @@ int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps,
     r = cufftExecC2C(plan->fft, static_cast<cufftComplex*>(out), static_cast<cufftComplex*>(out),
                      CUFFT_INVERSE);
     return r == CUFFT_SUCCESS ? RFX_OK : cufft_fail(r, "cufftExecC2C");
+}
+
+int rfx_channelize_branches(const void* x, const float* taps, void* u, int64_t num_samples,
+                            int channels, int num_taps, cudaStream_t stream)
+{
+    if (channels < 1 || num_taps < 1) {
+        return fail(RFX_ERR_INVALID, "channelize: need at least one channel and one tap");
+    }
+    if (num_samples < 0 || num_samples > kMaxSamples) {
+        return fail(RFX_ERR_INVALID, "channelize: bad sample count %lld",
+                    static_cast<long long>(num_samples));
+    }
+    const int64_t frames = rfx_channelize_frames(num_samples, channels);
+    if (frames == 0) {
+        return RFX_OK;
+    }
+    if (x == nullptr || taps == nullptr || u == nullptr) {
+        return fail(RFX_ERR_INVALID, "channelize: null pointer");
+    }
+    if (!aligned16(x) || !aligned16(u)) {
+        return fail(RFX_ERR_ALIGNMENT, "channelize: sample buffers must be 16-byte aligned");
+    }
+    const cudaError_t err = rfx::chan_branch_launch(x, taps, u, frames, channels, num_taps,
+                                                    stream);
+    return err == cudaSuccess ? RFX_OK : cuda_fail(err, "chan_branch_launch");
 }
 
 // ---- host-buffer operations ----------------------------------------------------------------

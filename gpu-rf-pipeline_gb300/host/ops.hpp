@@ -1,0 +1,34 @@
+#pragma once
+
+// The operations as the command-line tool sees them, with the project's interface
+// (src/ops.hpp:16-41): host data in, one-time setup outside the timed region, the upload /
+// compute / download phases handed to Bench::run(), host data out.
+
+#include "bench.hpp"
+#include "types.hpp"
+
+#include <vector>
+
+template <class Fn>
+struct Impl {
+    const char* name;     // value of --impl
+    const char* summary;  // one line for --help
+    Fn fn;
+};
+
+// y[n] = sum_k taps[k] * x[n - k], x[m] = 0 for m < 0, output length x.size(). `block` is the
+// project's --block (a multiple of 32 up to 1024); it does not change the result here.
+using FirFn = std::vector<cf32> (*)(const std::vector<cf32>& x, const std::vector<float>& taps,
+                                    int block, Bench& bench);
+constexpr int kDefaultFirBlock = 256;
+const std::vector<Impl<FirFn>>& fir_impls();  // first entry is the default
+
+// Polyphase channelizer: ceil(x.size() / channels) frames of `channels` values,
+// z[t][k] = sum_l taps[l] * x[t*M - l] * exp(+2j*pi*k*l / M).
+std::vector<cf32> channelize_cuda(const std::vector<cf32>& x, const std::vector<float>& taps,
+                                  int channels, Bench& bench);
+
+// The channelizer's implementations, selectable with --impl (the project has one).
+using ChanFn = std::vector<cf32> (*)(const std::vector<cf32>& x, const std::vector<float>& taps,
+                                     int channels, Bench& bench);
+const std::vector<Impl<ChanFn>>& channelize_impls();  // first entry is the default

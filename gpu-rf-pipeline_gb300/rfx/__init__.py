@@ -59,6 +59,7 @@ SIGNATURES = {
     "rfx_chan_plan_create": (_I, [_I, _I, _I64, ctypes.POINTER(_VP)]),
     "rfx_chan_plan_destroy": (_I, [_VP]),
     "rfx_channelize_launch": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _VP]),
+    "rfx_channelize_branches": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
     "rfx_fir_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_channelize_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_autotune_fir": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),
@@ -217,6 +218,17 @@ def channelize(x, taps, channels: int, impl="plain", stream=None):
         plan.launch(x, taps, out, stream)
         torch.cuda.current_stream().synchronize()
     return out
+
+
+def channelize_branches(x, taps, channels: int, stream=None):
+    """The float32 branch sums u (frames, channels) of the channelizer, complex64 CUDA tensor."""
+    import torch
+
+    f = frames(x.numel(), channels)
+    u = torch.empty((f, channels), dtype=torch.complex64, device=x.device)
+    _check(load().rfx_channelize_branches(x.data_ptr(), taps.data_ptr(), u.data_ptr(), x.numel(),
+                                          channels, taps.numel(), _stream_ptr(stream)))
+    return u
 
 
 def device_fault() -> int:

@@ -150,6 +150,13 @@ int rfx_chan_plan_destroy(rfx_chan_plan* plan);
 int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
                           int64_t num_samples, int num_taps, cudaStream_t stream);
 
+/* The branch sums alone: u[t][m] = sum_p taps[pM + m] x[tM - pM - m] into `u` (frames * channels
+ * cf32, frame-major), float32, bit-identical to the project's channelize_branch_kernel
+ * (src/channelize.cu:25-49). For callers that run their own inverse FFT on `u`, as the
+ * project's channelize_device(cufftHandle, ...) does (src/channelize.cu:56-72). */
+int rfx_channelize_branches(const void* x, const float* taps, void* u, int64_t num_samples,
+                            int channels, int num_taps, cudaStream_t stream);
+
 /* ---- host-buffer operations (timed like the project's Bench) --------------------------- */
 
 /* Phase timings of a host-buffer call, as the project's BenchResult (src/bench.hpp:17-32). */

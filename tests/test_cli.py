@@ -1,0 +1,253 @@
+"""The rfgpu command-line tool, tested the way the project tests its own (tests/test_pipeline.py):
+the binary runs as a subprocess on fixture files and its output files are compared with the
+oracle. Usage errors (exit 2) need no GPU; everything that computes is marked gpu."""
+from __future__ import annotations
+
+import json
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import PKG
+from oracle import rf_oracle as orc
+from rfx import signals
+
+RFGPU = PKG / "bin" / "rfgpu"
+FIR_RTOL = 1e-5          # tests/test_pipeline.py:116-117
+FIR_ATOL = 1e-5
+CHANNELIZE_RTOL = 1e-5   # tests/test_pipeline.py:363-364
+CHANNELIZE_ATOL = 1e-4
+
+
+@pytest.fixture(scope="session")
+def fixtures(tmp_path_factory) -> Path:
+    if not RFGPU.exists():
+        import __graft_entry__
+
+        __graft_entry__.build()
+    d = tmp_path_factory.mktemp("fixtures")
+    for name in ["tone", "tone_odd", "short", "zeros"]:
+        signals.fixture_signal(name).astype("<c8").tofile(d / f"{name}.cf32")
+    for name in ["lowpass", "lowpass_long", "channelizer_proto", "identity"]:
+        signals.fixture_taps(name).astype("<f4").tofile(d / f"{name}.f32")
+    return d
+
+
+def rfgpu(*args, check: bool = True) -> subprocess.CompletedProcess:
+    proc = subprocess.run([str(RFGPU), *map(str, args)], capture_output=True, text=True,
+                          timeout=300)
+    if check:
+        assert proc.returncode == 0, f"rfgpu {' '.join(map(str, args))}\n{proc.stderr}"
+    return proc
+
+
+def read_cf32(path: Path) -> np.ndarray:
+    return np.fromfile(path, dtype="<c8")
+
+
+# --- usage errors: no GPU needed -------------------------------------------------------------
+
+def test_help_lists_every_implementation() -> None:
+    if not RFGPU.exists():
+        import __graft_entry__
+
+        __graft_entry__.build()
+    proc = rfgpu("--help")
+    for name in ["plain", "tc_split", "auto", "naive", "register"]:
+        assert f"--impl {name}" in proc.stderr
+
+
+def test_unknown_impl_is_a_usage_error(fixtures: Path, tmp_path: Path) -> None:
+    proc = rfgpu("fir", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", "--impl", "no_such_impl", check=False)
+    assert proc.returncode == 2
+    assert "no_such_impl" in proc.stderr
+    assert not (tmp_path / "y.cf32").exists()
+
+
+@pytest.mark.parametrize("block", ["0", "48", "2048", "abc"])
+def test_bad_block_size_is_a_usage_error(fixtures: Path, tmp_path: Path, block: str) -> None:
+    proc = rfgpu("fir", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", "--block", block, check=False)
+    assert proc.returncode == 2
+    assert "--block" in proc.stderr
+
+
+@pytest.mark.parametrize("args", [["--channels", "0"], ["--channels", "x"], []])
+def test_bad_channel_count_is_a_usage_error(fixtures: Path, tmp_path: Path, args) -> None:
+    proc = rfgpu("channelize", "--in", fixtures / "tone.cf32", "--taps",
+                 fixtures / "channelizer_proto.f32", "--out", tmp_path / "z.cf32", *args,
+                 check=False)
+    assert proc.returncode == 2
+
+
+def test_unknown_option_and_subcommand_are_usage_errors(tmp_path: Path) -> None:
+    assert rfgpu("fir", "--nope", "1", check=False).returncode == 2
+    assert rfgpu("spectrum_of_everything", check=False).returncode == 2
+    assert rfgpu("fir", "--in", "a", "--in", "b", check=False).returncode == 2
+
+
+# --- numerics: GPU ------------------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def info() -> dict:
+    return json.loads(rfgpu("info").stdout)
+
+
+@pytest.mark.gpu
+def test_info_reports_the_device_and_impls(info: dict) -> None:
+    assert info["compute_capability"] == "10.3"
+    assert info["impls"]["fir"][0] == "plain"
+    assert "tc_split" in info["impls"]["fir"] and "tc_split" in info["impls"]["channelize"]
+
+
+FIR_IMPLS = ["plain", "tc_split", "auto", "naive", "tiled", "tiled_const", "register"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", FIR_IMPLS)
+@pytest.mark.parametrize("name,taps", [("tone", "lowpass"), ("tone", "lowpass_long"),
+                                       ("tone_odd", "lowpass"), ("tone_odd", "lowpass_long"),
+                                       ("short", "lowpass"), ("short", "lowpass_long")])
+def test_fir_matches_reference(fixtures: Path, tmp_path: Path, impl: str, name: str,
+                               taps: str) -> None:
+    out = tmp_path / "fir.cf32"
+    rfgpu("fir", "--in", fixtures / f"{name}.cf32", "--taps", fixtures / f"{taps}.f32",
+          "--out", out, "--impl", impl)
+    expected = orc.fir_fast(signals.fixture_signal(name), signals.fixture_taps(taps))
+    actual = read_cf32(out)
+    assert actual.shape == expected.shape
+    np.testing.assert_allclose(actual, expected, rtol=FIR_RTOL, atol=FIR_ATOL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", FIR_IMPLS)
+@pytest.mark.parametrize("block", [32, 96, 1024])
+def test_fir_block_size_does_not_change_the_result(fixtures: Path, tmp_path: Path, impl: str,
+                                                   block: int) -> None:
+    out = tmp_path / "fir.cf32"
+    rfgpu("fir", "--in", fixtures / "tone_odd.cf32", "--taps", fixtures / "lowpass_long.f32",
+          "--out", out, "--impl", impl, "--block", block)
+    expected = orc.fir_fast(signals.fixture_signal("tone_odd"),
+                            signals.fixture_taps("lowpass_long"))
+    np.testing.assert_allclose(read_cf32(out), expected, rtol=FIR_RTOL, atol=FIR_ATOL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", FIR_IMPLS)
+@pytest.mark.parametrize("name", ["tone", "tone_odd", "short"])
+def test_fir_identity_returns_the_input_exactly(fixtures: Path, tmp_path: Path, impl: str,
+                                                name: str) -> None:
+    out = tmp_path / "fir.cf32"
+    rfgpu("fir", "--in", fixtures / f"{name}.cf32", "--taps", fixtures / "identity.f32",
+          "--out", out, "--impl", impl)
+    assert out.read_bytes() == (fixtures / f"{name}.cf32").read_bytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", FIR_IMPLS)
+@pytest.mark.parametrize("taps", ["lowpass", "lowpass_long", "identity"])
+def test_fir_of_zeros_is_exactly_zero(fixtures: Path, tmp_path: Path, impl: str,
+                                      taps: str) -> None:
+    out = tmp_path / "fir.cf32"
+    rfgpu("fir", "--in", fixtures / "zeros.cf32", "--taps", fixtures / f"{taps}.f32",
+          "--out", out, "--impl", impl)
+    actual = read_cf32(out)
+    assert actual.shape == (4096,) and not np.any(actual)
+
+
+@pytest.mark.gpu
+def test_project_names_give_identical_bytes(fixtures: Path, tmp_path: Path) -> None:
+    outs = []
+    for impl in ["plain", "naive", "tiled", "tiled_const", "register"]:
+        out = tmp_path / f"{impl}.cf32"
+        rfgpu("fir", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass_long.f32",
+              "--out", out, "--impl", impl)
+        outs.append(out.read_bytes())
+    assert all(o == outs[0] for o in outs)
+    want = orc.fir_f32_seq(signals.fixture_signal("tone"), signals.fixture_taps("lowpass_long"))
+    assert outs[0] == want.astype("<c8").tobytes()
+
+
+@pytest.mark.gpu
+def test_bench_reports_each_phase(fixtures: Path, tmp_path: Path, info: dict) -> None:
+    proc = rfgpu("fir", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", "--bench", 10, "--warmup", 2)
+    report = json.loads(proc.stdout)
+    assert report["op"] == "fir" and report["runs"] == 10 and report["warmup"] == 2
+    assert report["gpu"] == info["gpu"]
+    for phase in ("h2d_ms", "kernel_ms", "d2h_ms"):
+        assert report[phase]["mean"] > 0 and report[phase]["std"] >= 0
+
+
+@pytest.mark.gpu
+def test_bench_does_not_change_the_output(fixtures: Path, tmp_path: Path) -> None:
+    args = ["--in", fixtures / "tone_odd.cf32", "--taps", fixtures / "lowpass_long.f32",
+            "--impl", "tc_split"]
+    rfgpu("fir", *args, "--out", tmp_path / "once.cf32")
+    rfgpu("fir", *args, "--out", tmp_path / "bench.cf32", "--bench", 10)
+    assert (tmp_path / "once.cf32").read_bytes() == (tmp_path / "bench.cf32").read_bytes()
+
+
+@pytest.mark.gpu
+def test_missing_input_file_is_a_runtime_error(fixtures: Path, tmp_path: Path) -> None:
+    proc = rfgpu("fir", "--in", tmp_path / "missing.cf32", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", check=False)
+    assert proc.returncode == 1
+    assert "missing.cf32" in proc.stderr
+
+
+@pytest.mark.gpu
+def test_truncated_cf32_is_rejected(fixtures: Path, tmp_path: Path) -> None:
+    np.zeros(3, dtype="<f4").tofile(tmp_path / "bad.cf32")
+    proc = rfgpu("fir", "--in", tmp_path / "bad.cf32", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", check=False)
+    assert proc.returncode == 1
+    assert "bad.cf32" in proc.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", ["plain", "auto"])
+@pytest.mark.parametrize("name,taps,channels", [
+    ("tone", "channelizer_proto", 16),
+    ("tone_odd", "channelizer_proto", 16),   # partial last frame
+    ("tone", "lowpass_long", 64),            # taps not a multiple of M
+    ("short", "lowpass", 4),                 # input shorter than the filter
+    ("tone_odd", "identity", 1),             # one channel, one tap: the input itself
+])
+def test_channelize_matches_reference(fixtures: Path, tmp_path: Path, impl: str, name: str,
+                                      taps: str, channels: int) -> None:
+    out = tmp_path / "ch.cf32"
+    rfgpu("channelize", "--in", fixtures / f"{name}.cf32", "--taps", fixtures / f"{taps}.f32",
+          "--channels", channels, "--out", out, "--impl", impl)
+    expected = orc.channelize_fast(signals.fixture_signal(name), signals.fixture_taps(taps),
+                                   channels).ravel()
+    actual = read_cf32(out)
+    assert actual.shape == expected.shape
+    np.testing.assert_allclose(actual, expected, rtol=CHANNELIZE_RTOL, atol=CHANNELIZE_ATOL)
+
+
+@pytest.mark.gpu
+def test_channelize_tc_on_sixty_four_channels(fixtures: Path, tmp_path: Path) -> None:
+    out = tmp_path / "ch.cf32"
+    rfgpu("channelize", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass_long.f32",
+          "--channels", 64, "--out", out, "--impl", "tc_split")
+    expected = orc.channelize_fast(signals.fixture_signal("tone"),
+                                   signals.fixture_taps("lowpass_long"), 64).ravel()
+    np.testing.assert_allclose(read_cf32(out), expected, rtol=CHANNELIZE_RTOL,
+                               atol=CHANNELIZE_ATOL)
+
+
+@pytest.mark.gpu
+def test_channelize_puts_a_tone_in_its_channel(fixtures: Path, tmp_path: Path) -> None:
+    n = np.arange(16 * 512)
+    signals.to_cf32(np.exp(2j * np.pi * 3 * n / 16)).astype("<c8").tofile(tmp_path / "x.cf32")
+    rfgpu("channelize", "--in", tmp_path / "x.cf32", "--taps",
+          fixtures / "channelizer_proto.f32", "--channels", 16, "--out", tmp_path / "ch.cf32")
+    z = read_cf32(tmp_path / "ch.cf32").reshape(-1, 16)[16:]
+    power = np.mean(np.abs(z) ** 2, axis=0)
+    assert np.argmax(power) == 3
+    assert power[3] > 1000 * np.max(np.delete(power, 3))
+    np.testing.assert_allclose(np.abs(z[:, 3]), 1.0, atol=0.02)
