@@ -202,7 +202,7 @@ __device__ __forceinline__ void branch_sums(f32x2 (&acc)[kR], const float2* __re
 
 }  // namespace
 
-__global__ void __maxnreg__(112)
+__global__ void __launch_bounds__(kThreads, 1)
 chan_tc_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
                const uint16_t* __restrict__ w_img, float2* __restrict__ z, long long n,
                long long frames, int num_taps, int num_tiles)

@@ -210,7 +210,7 @@ __device__ __forceinline__ uint32_t absmax4(float4 v)
 }  // namespace
 
 template <int S>
-__global__ void __maxnreg__(112)
+__global__ void __launch_bounds__(kThreads, 1)
 fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict__ x,
               const float* __restrict__ taps, float2* __restrict__ y, long long n, int num_taps,
               int num_tiles)

@@ -69,8 +69,12 @@ def test_tc_zeros_are_exact(taps: str) -> None:
     assert not np.any(y)
 
 
+# Tap counts whose tap strip, sample ring and operand stages fit the 227 KB of shared memory.
+TC_MAX_TAPS = 3713
+
+
 @pytest.mark.parametrize("k", [2, 3, 16, 31, 63, 64, 127, 128, 129, 255, 256, 257, 1025, 2049,
-                               4096])
+                               TC_MAX_TAPS])
 def test_tc_tap_counts(k: int) -> None:
     x, h = rand_case(40000, k, seed=k)
     y = run(x, h)
@@ -85,8 +89,9 @@ def test_tc_lengths(n: int) -> None:
     assert orc.normwise_error(y, orc.fir_fast(x, h)) <= TC_NORMWISE
 
 
-def test_tc_beyond_capacity_uses_the_plain_kernel() -> None:
-    x, h = rand_case(30000, 8192, seed=3)
+@pytest.mark.parametrize("k", [TC_MAX_TAPS + 1, 8192])
+def test_tc_beyond_capacity_uses_the_plain_kernel(k: int) -> None:
+    x, h = rand_case(30000, k, seed=3)
     y = run(x, h)
     assert np.array_equal(y.view(np.uint32), orc.fir_f32_seq(x, h).view(np.uint32))
 
