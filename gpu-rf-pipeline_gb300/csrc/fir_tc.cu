@@ -320,42 +320,76 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
         const int wtid = threadIdx.x;                      // 0 .. kWorkers-1
         int ex_ring[2] = {0, 0};                           // tile scale exponents, by tile parity
 
-        // Producing K-step v: the tile's scale on its first step, then raw -> FP16 planes.
+        // Scale of a tile: the largest |I| or |Q| over its input window, samples
+        // [(j0 - C) B, (j0 + NB) B) clipped to [0, n), read straight from global memory as float4
+        // (two samples). The window's float4 are split into kStagesPerTile slices; slice st of
+        // tile k + 1 is loaded during K-step st of tile k, before that step's waits, so the
+        // latency hides behind the pipeline. Tile 0 is scanned at once in the prologue.
+        auto window = [&](int k, long long& lo_s, long long& hi_s) {
+            const long long j0 = static_cast<long long>(static_cast<int>(blockIdx.x) +
+                                                        k * gridDim.x) * kNB;
+            const long long win0 = (j0 - C) * kB;
+            lo_s = win0 > 0 ? win0 : 0;
+            hi_s = (j0 + kNB) * kB < n ? (j0 + kNB) * kB : n;
+        };
+        auto load_pair = [&](long long s, long long hi_s) -> uint32_t {
+            if (s + 1 < hi_s) {
+                return absmax4(__ldg(reinterpret_cast<const float4*>(x + s)));
+            }
+            if (s < hi_s) {
+                const float2 w2 = __ldg(x + s);
+                return max(__float_as_uint(w2.x) & 0x7FFFFFFFu, __float_as_uint(w2.y) & 0x7FFFFFFFu);
+            }
+            return 0u;
+        };
+        // Combines every worker's partial max for tile k into ex_ring[k & 1].
+        auto reduce_scale = [&](int k, uint32_t m) -> bool {
+            m = __reduce_max_sync(0xFFFFFFFFu, m);
+            const int rb = k & 1;
+            if (lane == 0) {
+                ctl.warp_max[rb][warp] = m;
+                mbar_arrive(smem_u32(&ctl.reduce[rb]));
+            }
+            if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (k >> 1) & 1, fault,
+                                   kFaultStageEmpty, abort)) {
+                return false;
+            }
+            uint32_t tmax = 0;
+#pragma unroll
+            for (int w = 0; w < kWorkerWarps; ++w) {
+                tmax = max(tmax, ctl.warp_max[rb][w]);
+            }
+            ex_ring[k & 1] = scale_exponent(tmax);
+            return true;
+        };
+        uint32_t next_max = 0;  // running max of the next tile's window slices
+
+        // Producing K-step v: raw -> FP16 planes, plus one slice of the next tile's scan.
         auto produce = [&](int v) -> bool {
             const int k = v / kStagesPerTile;
             const int st = v % kStagesPerTile;
             const int tile = static_cast<int>(blockIdx.x) + k * gridDim.x;
             const long long j0 = static_cast<long long>(tile) * kNB;
-            if (st == 0) {
-                const long long win0 = (j0 - C) * kB;
-                const long long lo_s = win0 > 0 ? win0 : 0;
-                const long long hi_s = (j0 + kNB) * kB < n ? (j0 + kNB) * kB : n;
-                uint32_t m = 0;
-                for (long long s = lo_s + 2 * wtid; s < hi_s; s += 2 * kWorkers) {
-                    if (s + 1 < hi_s) {
-                        m = max(m, absmax4(__ldg(reinterpret_cast<const float4*>(x + s))));
-                    } else {
-                        const float2 w2 = __ldg(x + s);
-                        m = max(m, max(__float_as_uint(w2.x) & 0x7FFFFFFFu,
-                                       __float_as_uint(w2.y) & 0x7FFFFFFFu));
+            // Slice st of tile k + 1's window: float4 indices [st * per, (st + 1) * per).
+            uint32_t pre[3] = {0u, 0u, 0u};
+            const bool has_next = k + 1 < my_tiles;
+            if (has_next) {
+                long long lo_n, hi_n;
+                window(k + 1, lo_n, hi_n);
+                const long long pairs = (hi_n - lo_n + 1) / 2;
+                const long long per = (pairs + kStagesPerTile - 1) / kStagesPerTile;
+                const long long end = (st + 1) * per < pairs ? (st + 1) * per : pairs;
+                long long idx = st * per + wtid;
+#pragma unroll
+                for (int i = 0; i < 3; ++i, idx += kWorkers) {
+                    if (idx < end) {
+                        pre[i] = load_pair(lo_n + 2 * idx, hi_n);
                     }
                 }
-                m = __reduce_max_sync(0xFFFFFFFFu, m);
-                const int rb = k & 1;
-                if (lane == 0) {
-                    ctl.warp_max[rb][warp] = m;
-                    mbar_arrive(smem_u32(&ctl.reduce[rb]));
+                // A slice wider than 3 float4 per thread (very long filters) finishes here.
+                for (; idx < end; idx += kWorkers) {
+                    pre[0] = max(pre[0], load_pair(lo_n + 2 * idx, hi_n));
                 }
-                if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (k >> 1) & 1, fault,
-                                       kFaultStageEmpty, abort)) {
-                    return false;
-                }
-                uint32_t tmax = 0;
-#pragma unroll
-                for (int w = 0; w < kWorkerWarps; ++w) {
-                    tmax = max(tmax, ctl.warp_max[rb][w]);
-                }
-                ex_ring[k & 1] = scale_exponent(tmax);
             }
             const int ex = ex_ring[k & 1];
             const float fa = exp2i(ex / 2);
@@ -407,6 +441,15 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
                 mbar_arrive(smem_u32(&ctl.full[slot]));
                 mbar_arrive(smem_u32(&ctl.raw_empty[rslot]));
             }
+            if (has_next) {
+                next_max = max(next_max, max(pre[0], max(pre[1], pre[2])));
+                if (st == kStagesPerTile - 1) {
+                    if (!reduce_scale(k + 1, next_max)) {
+                        return false;
+                    }
+                    next_max = 0;
+                }
+            }
             // Refill this raw slot with K-step v + kRaw once every warp has converted it.
             if (wtid == 0 && v + kRaw < my_steps) {
                 if (!mbar_wait_bounded(smem_u32(&ctl.raw_empty[rslot]), (v / kRaw) & 1, fault,
@@ -424,6 +467,25 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
         };
 
         bool ok = true;
+        if (my_tiles > 0) {
+            long long lo0, hi0;
+            window(0, lo0, hi0);
+            uint32_t m = 0;
+            const long long pairs = (hi0 - lo0 + 1) / 2;
+            for (long long base = 0; base < pairs; base += 8 * kWorkers) {
+                uint32_t part[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const long long idx = base + wtid + i * kWorkers;
+                    part[i] = idx < pairs ? load_pair(lo0 + 2 * idx, hi0) : 0u;
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    m = max(m, part[i]);
+                }
+            }
+            ok = reduce_scale(0, m);
+        }
         for (int v = 0; v < S && v < my_steps && ok; ++v) {
             ok = produce(v);
         }
