@@ -24,25 +24,25 @@
 //
 // Accumulation: the tensor core adds each MMA's products into its FP32 accumulator with
 // round-toward-zero, so the error of an accumulator grows with the number of MMAs it takes.
-// Each TMEM accumulator therefore takes one GROUP of at most 12 MMAs (4 block-chunks x 3
-// products); the worker warps add every group's partial sum into FP32 running sums in registers
-// (round-to-nearest). Two 256-column partial buffers alternate, so the MMAs of one group overlap
-// the drain of the previous one.
+// Each TMEM accumulator therefore takes one GROUP of 12 MMAs (four consecutive (K-step, chunk)
+// steps x 3 products; a group may straddle two K-steps); the worker warps add every group's
+// partial sum into FP32 running sums in registers (round-to-nearest). Two 256-column partial
+// buffers alternate, so the MMAs of one group overlap the drain of the previous one.
 //
 // Roles (544 threads): warps 0-15 are workers and warp 16 owns tensor memory and issues the MMAs
 // (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 64 (w / 4) .. +63, holds
-// those 64 running sums, writes those outputs, and shares the producing: the tile's scale (a max
-// over its input window, read straight from global memory), and the conversion of each K-step's
-// fp32 samples — staged by a 2-D TMA copy (zero fill outside the input) — into the FP16 planes.
+// those 64 running sums, writes those outputs, and shares the producing: each K-step's fp32
+// samples arrive by a 2-D TMA copy (zero fill outside the input) and are converted into the
+// FP16 planes; the next tile's scale is a max over its input window, copied by TMA in eight
+// slices, one per K-step of the current tile, and read a K-step later.
 // Every wait is an mbarrier wait bounded in time; a give-up sets the fault word and every role
 // stops.
 #include "fir_tc.cuh"
 #include "fir_plain.cuh"
-#include "ptx.cuh"
+#include "tc_common.cuh"
 #include "tmap.hpp"
 
 #include <cuda.h>
-#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace rfx {
@@ -50,6 +50,8 @@ namespace rfx {
 static __device__ unsigned int g_fault_fir_tc;
 
 namespace {
+
+using namespace tc;
 
 constexpr int kB = 128;                  // outputs per block = MMA M
 constexpr int kNB = 128;                 // blocks per tile; MMA N = 2 * kNB = 256
@@ -60,24 +62,22 @@ constexpr int kWorkers = kWorkerWarps * 32;
 constexpr int kMmaWarp = 16;
 constexpr int kThreads = 17 * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
-constexpr int kChunksPerGroup = 4;       // 12 MMAs per accumulator
+constexpr int kStepsPerGroup = 4;        // (K-step, chunk) steps per accumulator: 12 MMAs
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
 constexpr uint32_t kTmemCols = 512;      // two partial buffers of kN columns
-
-constexpr uint32_t kIdesc = (1u << 4)                       // D: F32
-                            | (0u << 7) | (0u << 10)        // A, B: F16
-                            | (static_cast<uint32_t>(kN >> 3) << 17)
-                            | (static_cast<uint32_t>(kB >> 4) << 24);
+constexpr uint32_t kIdesc = idesc_f16(kB, kN);
 
 struct Layout {
     int C;               // previous blocks a block reaches back to
     int rows;            // window blocks per tile: kNB + C
+    int srows;           // window rows per scan slice: ceil(rows / 8)
     uint32_t pitch;      // bytes per plane (2 rows * 16 B per block + 16)
     uint32_t split;      // bytes of one split (hi or lo) of a stage: 2 planes
     uint32_t stage;      // bytes per operand stage: hi + lo
     uint32_t raw;        // bytes per raw stage: rows * 16 samples * 8 B
+    uint32_t scan;       // bytes per scan slice: srows * 128 samples * 8 B
     int tcount;          // core matrices of the tap strip
-    uint32_t taps_hi, taps_lo, raw0, stages0, bytes;
+    uint32_t taps_hi, taps_lo, raw0, scan0, stages0, bytes;
 };
 
 __host__ __device__ inline Layout tc_layout(int num_taps, int stages)
@@ -85,15 +85,18 @@ __host__ __device__ inline Layout tc_layout(int num_taps, int stages)
     Layout l;
     l.C = (num_taps + kB - 2) / kB;
     l.rows = kNB + l.C;
+    l.srows = (l.rows + kStagesPerTile - 1) / kStagesPerTile;
     l.pitch = static_cast<uint32_t>(2 * l.rows) * 16u + 16u;
     l.split = 2u * l.pitch;
     l.stage = 2u * l.split;
     l.raw = static_cast<uint32_t>(l.rows) * 128u;
+    l.scan = static_cast<uint32_t>(l.srows) * 1024u;
     l.tcount = 16 * l.C + 31;
     l.taps_hi = 1024;
     l.taps_lo = l.taps_hi + 128u * static_cast<uint32_t>(l.tcount);
     l.raw0 = (l.taps_lo + 128u * static_cast<uint32_t>(l.tcount) + 127u) & ~127u;
-    l.stages0 = l.raw0 + kRaw * l.raw;
+    l.scan0 = l.raw0 + kRaw * l.raw;
+    l.stages0 = l.scan0 + 2u * l.scan;
     l.bytes = l.stages0 + l.stage * static_cast<uint32_t>(stages);
     return l;
 }
@@ -104,6 +107,8 @@ struct Ctrl {
     unsigned long long empty[8];
     unsigned long long raw_full[kRaw];
     unsigned long long raw_empty[kRaw];
+    unsigned long long scan_full[2];
+    unsigned long long scan_empty[2];
     unsigned long long pfull[2];
     unsigned long long pempty[2];
     unsigned long long reduce[2];
@@ -115,122 +120,35 @@ struct Ctrl {
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
-__device__ __forceinline__ unsigned long long smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
-{
-    return static_cast<unsigned long long>((addr >> 4) & 0x3FFFu) |
-           (static_cast<unsigned long long>((lbo >> 4) & 0x3FFFu) << 16) |
-           (static_cast<unsigned long long>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-
-__device__ __forceinline__ void mma_f16(uint32_t d_tmem, unsigned long long a,
-                                        unsigned long long b, uint32_t accumulate)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(d_tmem), "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar)
-{
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before()
-{
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_fence_after()
-{
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// 2-D tiled TMA load of {32 floats, rows} at (x0, y0) into shared memory.
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x0, int y0,
-                                            uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x0), "r"(y0), "r"(bar)
-        : "memory");
-}
-
-// 2^e as a float for e in [-126, 127].
-__device__ __forceinline__ float exp2i(int e)
-{
-    e = e < -126 ? -126 : (e > 127 ? 127 : e);
-    return __int_as_float((e + 127) << 23);
-}
-
-// Exponent that brings a magnitude with these bits into [2^14, 2^15): 141 - biased exponent.
-__device__ __forceinline__ int scale_exponent(uint32_t abs_bits)
-{
-    if (abs_bits == 0) {
-        return 0;
-    }
-    return 141 - static_cast<int>((abs_bits >> 23) & 0xFFu);
-}
-
-// hi/lo FP16 split of two values already scaled into range.
-__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo)
-{
-    const __half2 h = __floats2half2_rn(a, b);
-    const float2 hf = __half22float2(h);
-    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
-    hi = *reinterpret_cast<const uint32_t*>(&h);
-    lo = *reinterpret_cast<const uint32_t*>(&l);
-}
-
-__device__ __forceinline__ void sts32(uint32_t addr, uint32_t v)
-{
-    asm volatile("st.shared.b32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ float4 lds128(uint32_t addr)
-{
-    float4 v;
-    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-                 : "r"(addr)
-                 : "memory");
-    return v;
-}
-
-__device__ __forceinline__ uint32_t absmax4(float4 v)
-{
-    return max(max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu),
-               max(__float_as_uint(v.z) & 0x7FFFFFFFu, __float_as_uint(v.w) & 0x7FFFFFFFu));
-}
-
 }  // namespace
 
+// xmap: x as rows of 256 floats (one block), boxes of 32 floats x `rows` (one K-step's samples
+// of a tile window). smap: the same rows, boxes of 256 floats x `srows` (a scan slice).
 template <int S>
 __global__ void __launch_bounds__(kThreads, 1)
-fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict__ x,
-              const float* __restrict__ taps, float2* __restrict__ y, long long n, int num_taps,
-              int num_tiles)
+fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap smap,
+              const float2* __restrict__ x, const float* __restrict__ taps,
+              float2* __restrict__ y, long long n, int num_taps, int num_tiles)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
     const Layout lay = tc_layout(num_taps, S);
     const int C = lay.C;
+    const int P = C + 1;                       // chunks per K-step
+    const int groups_per_tile = 2 * P;         // 8 P steps / 4 per group
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const uint32_t sbase = smem_u32(smem);
     volatile int* abort = &ctl.abort;
     unsigned int* fault = &g_fault_fir_tc;
-    const int groups = (C + kChunksPerGroup) / kChunksPerGroup;  // per K-step: ceil((C+1)/4)
     // This block's tiles: blockIdx.x, + gridDim.x, ...; its K-steps are numbered u = 8 k + st.
     const int my_tiles = static_cast<int>(blockIdx.x) < num_tiles
                              ? (num_tiles - 1 - static_cast<int>(blockIdx.x)) / gridDim.x + 1
                              : 0;
     const int my_steps = my_tiles * kStagesPerTile;
-    const long long full_blocks = n / kB;  // rows the tensor map covers
+    const int scan_slices = my_tiles > 1 ? (my_tiles - 1) * kStagesPerTile : 0;
+    const long long full_blocks = n / kB;      // rows the tensor maps cover
+    auto tile_of = [&](int k) { return static_cast<int>(blockIdx.x) + k * gridDim.x; };
 
     // ---- setup: barriers, tensor memory, first raw copies, tap strip -----------------------
     if (threadIdx.x == 0) {
@@ -243,6 +161,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
             mbar_init(smem_u32(&ctl.raw_empty[i]), kWorkerWarps);
         }
         for (int i = 0; i < 2; ++i) {
+            mbar_init(smem_u32(&ctl.scan_full[i]), 1);
+            mbar_init(smem_u32(&ctl.scan_empty[i]), kWorkerWarps);
             mbar_init(smem_u32(&ctl.pfull[i]), 1);
             mbar_init(smem_u32(&ctl.pempty[i]), kWorkerWarps);
             mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
@@ -253,28 +173,23 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
         fence_mbar_init();
     }
     if (warp == kMmaWarp) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                         smem_u32(&ctl.tmem_base)),
-                     "r"(kTmemCols));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        tmem_alloc(smem_u32(&ctl.tmem_base), kTmemCols);
     }
     __syncthreads();
-    // Raw sample stages 0 .. kRaw-1. K-step u is tile k = u / 8: window rows from block
-    // j0 - C, samples 16 (u % 8) .. +15 of each block, i.e. floats 32 (u % 8) .. +31.
+    // Raw sample stages 0 .. kRaw-1 (K-step u: rows from block 128 k - C, floats 32 (u % 8)..).
     if (threadIdx.x == 0) {
         for (int u = 0; u < kRaw && u < my_steps; ++u) {
-            const int tile = static_cast<int>(blockIdx.x) + (u / kStagesPerTile) * gridDim.x;
             const uint32_t bar = smem_u32(&ctl.raw_full[u]);
             mbar_arrive_expect_tx(bar, lay.raw);
             tma_load_2d(sbase + lay.raw0 + u * lay.raw, &xmap, 32 * (u % kStagesPerTile),
-                        tile * kNB - C, bar);
+                        tile_of(u / kStagesPerTile) * kNB - C, bar);
         }
     }
     // Largest tap magnitude (bit pattern of |h|: ordered like the value).
     {
         uint32_t m = 0;
         for (int k = threadIdx.x; k < num_taps; k += kThreads) {
-            m = max(m, __float_as_uint(__ldg(taps + k)) & 0x7FFFFFFFu);
+            m = max(m, absbits(__ldg(taps + k)));
         }
         m = __reduce_max_sync(0xFFFFFFFFu, m);
         if (lane == 0) {
@@ -305,9 +220,9 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
         }
     }
     fence_proxy_async_smem();
-    tc_fence_before();
+    fence_before();
     __syncthreads();
-    tc_fence_after();
+    fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
     if (warp < kWorkerWarps) {
@@ -319,26 +234,16 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
                                    static_cast<uint32_t>(slice * kCols);
         const int wtid = threadIdx.x;                      // 0 .. kWorkers-1
         int ex_ring[2] = {0, 0};                           // tile scale exponents, by tile parity
+        uint32_t next_max = 0;                             // running max of the next tile's scan
 
-        // Scale of a tile: the largest |I| or |Q| over its input window, samples
-        // [(j0 - C) B, (j0 + NB) B) clipped to [0, n), read straight from global memory as float4
-        // (two samples). The window's float4 are split into kStagesPerTile slices; slice st of
-        // tile k + 1 is loaded during K-step st of tile k, before that step's waits, so the
-        // latency hides behind the pipeline. Tile 0 is scanned at once in the prologue.
-        auto window = [&](int k, long long& lo_s, long long& hi_s) {
-            const long long j0 = static_cast<long long>(static_cast<int>(blockIdx.x) +
-                                                        k * gridDim.x) * kNB;
-            const long long win0 = (j0 - C) * kB;
-            lo_s = win0 > 0 ? win0 : 0;
-            hi_s = (j0 + kNB) * kB < n ? (j0 + kNB) * kB : n;
-        };
+        // Max of |samples| in [s, s + 2) clipped to hi_s (plain loads, for the partial block).
         auto load_pair = [&](long long s, long long hi_s) -> uint32_t {
             if (s + 1 < hi_s) {
                 return absmax4(__ldg(reinterpret_cast<const float4*>(x + s)));
             }
             if (s < hi_s) {
                 const float2 w2 = __ldg(x + s);
-                return max(__float_as_uint(w2.x) & 0x7FFFFFFFu, __float_as_uint(w2.y) & 0x7FFFFFFFu);
+                return max(absbits(w2.x), absbits(w2.y));
             }
             return 0u;
         };
@@ -362,35 +267,56 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
             ex_ring[k & 1] = scale_exponent(tmax);
             return true;
         };
-        uint32_t next_max = 0;  // running max of the next tile's window slices
-
-        // Producing K-step v: raw -> FP16 planes, plus one slice of the next tile's scan.
-        auto produce = [&](int v) -> bool {
-            const int k = v / kStagesPerTile;
-            const int st = v % kStagesPerTile;
-            const int tile = static_cast<int>(blockIdx.x) + k * gridDim.x;
-            const long long j0 = static_cast<long long>(tile) * kNB;
-            // Slice st of tile k + 1's window: float4 indices [st * per, (st + 1) * per).
-            uint32_t pre[3] = {0u, 0u, 0u};
-            const bool has_next = k + 1 < my_tiles;
-            if (has_next) {
-                long long lo_n, hi_n;
-                window(k + 1, lo_n, hi_n);
-                const long long pairs = (hi_n - lo_n + 1) / 2;
-                const long long per = (pairs + kStagesPerTile - 1) / kStagesPerTile;
-                const long long end = (st + 1) * per < pairs ? (st + 1) * per : pairs;
-                long long idx = st * per + wtid;
-#pragma unroll
-                for (int i = 0; i < 3; ++i, idx += kWorkers) {
-                    if (idx < end) {
-                        pre[i] = load_pair(lo_n + 2 * idx, hi_n);
-                    }
+        // Scan slice q (tile q / 8 + 1, window rows (q % 8) srows .. +srows): copied by TMA one
+        // K-step earlier; rows past the window are ignored, the partial last block is read
+        // from global memory.
+        auto consume_slice = [&](int q) -> bool {
+            const int qb = q & 1;
+            if (!mbar_wait_bounded(smem_u32(&ctl.scan_full[qb]), (q >> 1) & 1, fault,
+                                   kFaultTileLoad, abort)) {
+                return false;
+            }
+            const int k = q / kStagesPerTile + 1;
+            const long long j0 = static_cast<long long>(tile_of(k)) * kNB;
+            const int r0 = (q % kStagesPerTile) * lay.srows;
+            const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
+            const int quads = lay.srows * 64;   // float4 per slice
+            uint32_t m = next_max;
+            for (int f = wtid; f < quads; f += kWorkers) {
+                const int row = r0 + (f >> 6);
+                if (row >= lay.rows) {
+                    continue;
                 }
-                // A slice wider than 3 float4 per thread (very long filters) finishes here.
-                for (; idx < end; idx += kWorkers) {
-                    pre[0] = max(pre[0], load_pair(lo_n + 2 * idx, hi_n));
+                const long long jb = j0 - C + row;
+                if (jb != full_blocks) {
+                    m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
+                } else {
+                    m = max(m, load_pair(jb * kB + 2 * (f & 63), n));
                 }
             }
+            next_max = m;
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&ctl.scan_empty[qb]));
+            }
+            if (q % kStagesPerTile == kStagesPerTile - 1) {
+                if (!reduce_scale(k, next_max)) {
+                    return false;
+                }
+                next_max = 0;
+            }
+            return true;
+        };
+
+        // Producing K-step v: finish the scan slice copied during step v - 1, convert the raw
+        // samples into the FP16 planes, then queue step v + kRaw's raw copy and scan slice v.
+        auto produce = [&](int v) -> bool {
+            if (v >= 1 && v - 1 < scan_slices && !consume_slice(v - 1)) {
+                return false;
+            }
+            const int k = v / kStagesPerTile;
+            const int st = v % kStagesPerTile;
+            const long long j0 = static_cast<long long>(tile_of(k)) * kNB;
             const int ex = ex_ring[k & 1];
             const float fa = exp2i(ex / 2);
             const float fb = exp2i(ex - ex / 2);
@@ -413,7 +339,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
                 if (jb != full_blocks) {
                     v4 = lds128(raw + static_cast<uint32_t>(f) * 16u);  // zero outside [0, n)
                 } else {
-                    // The input's last, partial block is outside the tensor map: plain loads.
+                    // The input's last, partial block is outside the tensor maps: plain loads.
                     const long long sidx = jb * kB + 16 * st + 2 * q;
                     v4 = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (sidx + 1 < n) {
@@ -441,37 +367,46 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
                 mbar_arrive(smem_u32(&ctl.full[slot]));
                 mbar_arrive(smem_u32(&ctl.raw_empty[rslot]));
             }
-            if (has_next) {
-                next_max = max(next_max, max(pre[0], max(pre[1], pre[2])));
-                if (st == kStagesPerTile - 1) {
-                    if (!reduce_scale(k + 1, next_max)) {
+            if (wtid == 0) {
+                // Refill this raw slot with K-step v + kRaw once every warp has converted it.
+                if (v + kRaw < my_steps) {
+                    if (!mbar_wait_bounded(smem_u32(&ctl.raw_empty[rslot]), (v / kRaw) & 1,
+                                           fault, kFaultStageEmpty, abort)) {
                         return false;
                     }
-                    next_max = 0;
+                    const int vn = v + kRaw;
+                    const uint32_t bar = smem_u32(&ctl.raw_full[rslot]);
+                    mbar_arrive_expect_tx(bar, lay.raw);
+                    tma_load_2d(raw, &xmap, 32 * (vn % kStagesPerTile),
+                                tile_of(vn / kStagesPerTile) * kNB - C, bar);
                 }
-            }
-            // Refill this raw slot with K-step v + kRaw once every warp has converted it.
-            if (wtid == 0 && v + kRaw < my_steps) {
-                if (!mbar_wait_bounded(smem_u32(&ctl.raw_empty[rslot]), (v / kRaw) & 1, fault,
-                                       kFaultStageEmpty, abort)) {
-                    return false;
+                // Scan slice v (for tile v / 8 + 1) into buffer v & 1 once slice v - 2 is read.
+                if (v < scan_slices) {
+                    const int qb = v & 1;
+                    if (!mbar_wait_bounded(smem_u32(&ctl.scan_empty[qb]), ((v >> 1) & 1) ^ 1,
+                                           fault, kFaultStageEmpty, abort)) {
+                        return false;
+                    }
+                    const int kn = v / kStagesPerTile + 1;
+                    const uint32_t bar = smem_u32(&ctl.scan_full[qb]);
+                    mbar_arrive_expect_tx(bar, lay.scan);
+                    tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan, &smap,
+                                0, tile_of(kn) * kNB - C + (v % kStagesPerTile) * lay.srows,
+                                bar);
                 }
-                const int vn = v + kRaw;
-                const int tile_n =
-                    static_cast<int>(blockIdx.x) + (vn / kStagesPerTile) * gridDim.x;
-                const uint32_t bar = smem_u32(&ctl.raw_full[rslot]);
-                mbar_arrive_expect_tx(bar, lay.raw);
-                tma_load_2d(raw, &xmap, 32 * (vn % kStagesPerTile), tile_n * kNB - C, bar);
             }
             return true;
         };
 
         bool ok = true;
         if (my_tiles > 0) {
-            long long lo0, hi0;
-            window(0, lo0, hi0);
-            uint32_t m = 0;
+            // Tile 0's scale: its whole window at once, eight loads in flight per thread.
+            const long long j0 = static_cast<long long>(tile_of(0)) * kNB;
+            const long long win0 = (j0 - C) * kB;
+            const long long lo0 = win0 > 0 ? win0 : 0;
+            const long long hi0 = (j0 + kNB) * kB < n ? (j0 + kNB) * kB : n;
             const long long pairs = (hi0 - lo0 + 1) / 2;
+            uint32_t m = 0;
             for (long long base = 0; base < pairs; base += 8 * kWorkers) {
                 uint32_t part[8];
 #pragma unroll
@@ -494,52 +429,46 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
         for (int i = 0; i < kCols; ++i) {
             acc[i] = 0.0f;
         }
+        int gi = 0;  // next tile-local group to drain
         for (int u = 0; u < my_steps && ok && !*abort; ++u) {
-            // Drain the partial sums of K-step u's groups into the running sums.
-            for (int gi = 0; gi < groups; ++gi) {
-                const int g = u * groups + gi;
+            const int k = u / kStagesPerTile;
+            const int st = u % kStagesPerTile;
+            // Drain the groups whose last (K-step, chunk) step lies in K-step u.
+            while (kStepsPerGroup * gi + kStepsPerGroup - 1 < (st + 1) * P) {
+                const int g = k * groups_per_tile + gi;
                 const int pb = g & 1;
                 if (!mbar_wait_bounded(smem_u32(&ctl.pfull[pb]), (g >> 1) & 1, fault,
                                        kFaultAccumFull, abort)) {
                     ok = false;
                     break;
                 }
-                tc_fence_after();
+                fence_after();
 #pragma unroll
                 for (int c16 = 0; c16 < kCols / 16; ++c16) {
                     uint32_t t[16];
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]),
-                          "=r"(t[5]), "=r"(t[6]), "=r"(t[7]), "=r"(t[8]), "=r"(t[9]),
-                          "=r"(t[10]), "=r"(t[11]), "=r"(t[12]), "=r"(t[13]), "=r"(t[14]),
-                          "=r"(t[15])
-                        : "r"(lane_addr + static_cast<uint32_t>(pb * kN + c16 * 16)));
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    tmem_ld16(lane_addr + static_cast<uint32_t>(pb * kN + c16 * 16), t);
+                    tmem_wait_ld();
 #pragma unroll
                     for (int i = 0; i < 16; ++i) {
                         acc[c16 * 16 + i] += __uint_as_float(t[i]);
                     }
                 }
-                tc_fence_before();
+                fence_before();
                 __syncwarp();
                 if (lane == 0) {
                     mbar_arrive(smem_u32(&ctl.pempty[pb]));
                 }
+                ++gi;
             }
             if (!ok) {
                 break;
             }
-            const int k = u / kStagesPerTile;
-            if (u % kStagesPerTile == kStagesPerTile - 1) {
+            if (st == kStagesPerTile - 1) {
                 // Last K-step of tile k: scale and store this thread's outputs.
                 const int shift = -(ex_ring[k & 1] + eh);
                 const float fa = exp2i(shift / 2);
                 const float fb = exp2i(shift - shift / 2);
-                const long long jb0 =
-                    static_cast<long long>(static_cast<int>(blockIdx.x) + k * gridDim.x) * kNB +
-                    slice * (kCols / 2);
+                const long long jb0 = static_cast<long long>(tile_of(k)) * kNB + slice * (kCols / 2);
 #pragma unroll
                 for (int b = 0; b < kCols / 2; ++b) {
                     const long long o = (jb0 + b) * kB + r;
@@ -549,6 +478,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
                     acc[2 * b] = 0.0f;
                     acc[2 * b + 1] = 0.0f;
                 }
+                gi = 0;
             }
             if (u + S < my_steps) {
                 ok = produce(u + S);
@@ -560,39 +490,41 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
         const uint32_t taps_lo = sbase + lay.taps_lo;
         bool stop = false;
         for (int u = 0; u < my_steps && !stop && !*abort; ++u) {
+            const int k = u / kStagesPerTile;
+            const int st = u % kStagesPerTile;
             const int slot = u % S;
             if (!mbar_wait_bounded(smem_u32(&ctl.full[slot]), (u / S) & 1, fault,
                                    kFaultStageFull, abort)) {
                 break;
             }
-            tc_fence_after();
+            fence_after();
             const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
-            const int s0 = (u % kStagesPerTile) * 16;
-            for (int gi = 0; gi < groups; ++gi) {
-                const int g = u * groups + gi;
+            const int s0 = st * 16;
+            for (int c = 0; c < P; ++c) {
+                const int cs = st * P + c;                 // tile-local step
+                const int g = k * groups_per_tile + cs / kStepsPerGroup;
                 const int pb = g & 1;
-                if (!mbar_wait_bounded(smem_u32(&ctl.pempty[pb]), ((g >> 1) & 1) ^ 1, fault,
-                                       kFaultAccumEmpty, abort)) {
-                    stop = true;
-                    break;
+                if (cs % kStepsPerGroup == 0) {
+                    if (!mbar_wait_bounded(smem_u32(&ctl.pempty[pb]), ((g >> 1) & 1) ^ 1, fault,
+                                           kFaultAccumEmpty, abort)) {
+                        stop = true;
+                        break;
+                    }
+                    fence_after();
                 }
-                tc_fence_after();
                 const uint32_t dt = tmem + static_cast<uint32_t>(pb * kN);
-                const int c0 = gi * kChunksPerGroup;
-                const int c1 = c0 + kChunksPerGroup <= C + 1 ? c0 + kChunksPerGroup : C + 1;
-                for (int c = c0; c < c1; ++c) {
-                    const uint32_t t0 = static_cast<uint32_t>(16 * (C - c) + s0 / 8) * 128u;
-                    const unsigned long long a_hi = smem_desc(taps_hi + t0, 128, 128);
-                    const unsigned long long a_lo = smem_desc(taps_lo + t0, 128, 128);
-                    const uint32_t row0 = static_cast<uint32_t>(2 * (C - c)) * 16u;
-                    const unsigned long long b_hi = smem_desc(stage + row0, lay.pitch, 128);
-                    const unsigned long long b_lo =
-                        smem_desc(stage + lay.split + row0, lay.pitch, 128);
-                    mma_f16(dt, a_hi, b_hi, c > c0 ? 1u : 0u);
-                    mma_f16(dt, a_hi, b_lo, 1u);
-                    mma_f16(dt, a_lo, b_hi, 1u);
+                const uint32_t t0 = static_cast<uint32_t>(16 * (C - c) + s0 / 8) * 128u;
+                const unsigned long long a_hi = smem_desc(taps_hi + t0, 128, 128);
+                const unsigned long long a_lo = smem_desc(taps_lo + t0, 128, 128);
+                const uint32_t row0 = static_cast<uint32_t>(2 * (C - c)) * 16u;
+                const unsigned long long b_hi = smem_desc(stage + row0, lay.pitch, 128);
+                const unsigned long long b_lo = smem_desc(stage + lay.split + row0, lay.pitch, 128);
+                mma_f16<kIdesc>(dt, a_hi, b_hi, cs % kStepsPerGroup != 0 ? 1u : 0u);
+                mma_f16<kIdesc>(dt, a_hi, b_lo, 1u);
+                mma_f16<kIdesc>(dt, a_lo, b_hi, 1u);
+                if (cs % kStepsPerGroup == kStepsPerGroup - 1) {
+                    mma_commit(smem_u32(&ctl.pfull[pb]));
                 }
-                mma_commit(smem_u32(&ctl.pfull[pb]));
             }
             mma_commit(smem_u32(&ctl.empty[slot]));
         }
@@ -601,18 +533,17 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict
         mbar_wait_bounded(smem_u32(&ctl.teardown), 0, fault, kFaultTeardown, nullptr);
     }
 
-    // After a give-up, raw copies may still be in flight: give them time to land (bounded).
+    // After a give-up, TMA copies may still be in flight: give them time to land (bounded).
     if (threadIdx.x == 0 && *abort) {
         const unsigned long long t0 = globaltimer_ns();
         while (globaltimer_ns() - t0 < 2000000ull) {
         }
     }
-    tc_fence_before();
+    fence_before();
     __syncthreads();
-    tc_fence_after();
+    fence_after();
     if (warp == kMmaWarp) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"(kTmemCols));
+        tmem_dealloc(tmem, kTmemCols);
     }
 }
 
@@ -661,7 +592,11 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
     // x viewed as rows of 256 floats (one 128-sample block per row), full blocks only; boxes
     // of 32 floats (16 samples) by the tile's window rows.
     CUtensorMap map;
+    CUtensorMap smap;
     err = encode_rows_f32(&map, x, n / kB, 2 * kB, 32, static_cast<uint32_t>(lay.rows));
+    if (err == cudaSuccess) {
+        err = encode_rows_f32(&smap, x, n / kB, 2 * kB, 2 * kB, static_cast<uint32_t>(lay.srows));
+    }
     if (err != cudaSuccess) {
         return err;
     }
@@ -669,7 +604,8 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
     const int tiles = static_cast<int>((blocks + kNB - 1) / kNB);
     const int grid = tiles < sms ? tiles : sms;
     fir_tc_kernel<S><<<grid, kThreads, bytes, stream>>>(
-        map, static_cast<const float2*>(x), taps, static_cast<float2*>(y), n, num_taps, tiles);
+        map, smap, static_cast<const float2*>(x), taps, static_cast<float2*>(y), n, num_taps,
+        tiles);
     return cudaGetLastError();
 }
 
@@ -708,17 +644,17 @@ cudaError_t fir_tc_take_fault(unsigned int* code)
 cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
                              cudaStream_t stream)
 {
+    if (impl == RFX_FIR_TC || impl == RFX_FIR_AUTO) {
+        return fir_batch_tc_launch(captures, count, stream);
+    }
+    // The plain kernel: one launch per capture, as the project runs a batch.
     for (int c = 0; c < count; ++c) {
         if (captures[c].num_samples == 0) {
             continue;
         }
-        const bool tc = impl == RFX_FIR_TC && fir_tc_supported(captures[c].num_taps);
-        cudaError_t err = tc ? fir_tc_launch(captures[c].x, captures[c].taps, captures[c].y,
-                                             captures[c].num_samples, captures[c].num_taps,
-                                             TcConfig{kNB, 4}, stream)
-                             : fir_plain_launch(captures[c].x, captures[c].taps, captures[c].y,
-                                                captures[c].num_samples, captures[c].num_taps,
-                                                stream);
+        const cudaError_t err = fir_plain_launch(captures[c].x, captures[c].taps, captures[c].y,
+                                                 captures[c].num_samples, captures[c].num_taps,
+                                                 stream);
         if (err != cudaSuccess) {
             return err;
         }

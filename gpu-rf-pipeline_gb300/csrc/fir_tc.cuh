@@ -23,8 +23,12 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
                           TcConfig config, cudaStream_t stream);
 cudaError_t fir_tc_take_fault(unsigned int* code);
 
-// Per-capture-taps batch in one launch.
+// Per-capture-taps batch: tensor core (or auto) = one persistent launch of fir_batch.cu per
+// 192 captures; plain = one launch per capture.
 cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
                              cudaStream_t stream);
+cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cudaStream_t stream);
+bool fir_batch_supported(int num_taps);
+cudaError_t fir_batch_take_fault(unsigned int* code);
 
 }  // namespace rfx

@@ -163,6 +163,11 @@ int rfx_device_fault(unsigned int* code)
     }
     total |= part;
     part = 0;
+    if ((err = rfx::fir_batch_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "fir_batch fault word");
+    }
+    total |= part;
+    part = 0;
     if ((err = rfx::chan_tc_take_fault(&part)) != cudaSuccess) {
         return cuda_fail(err, "chan_tc fault word");
     }

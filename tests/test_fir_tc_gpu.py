@@ -70,7 +70,7 @@ def test_tc_zeros_are_exact(taps: str) -> None:
 
 
 # Tap counts whose tap strip, sample ring and operand stages fit the 227 KB of shared memory.
-TC_MAX_TAPS = 3713
+TC_MAX_TAPS = 2689
 
 
 @pytest.mark.parametrize("k", [2, 3, 16, 31, 63, 64, 127, 128, 129, 255, 256, 257, 1025, 2049,
