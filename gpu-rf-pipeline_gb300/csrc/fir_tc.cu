@@ -4,8 +4,8 @@
 //
 // Blocks of B = 128 outputs: with X[s][j] = x[jB + s] (s < B) the output block j is
 //   Y[:, j] = sum_{c=0}^{C} T_c X[:, j - c],   T_c(r, s) = h[cB + r - s]  (0 outside [0, K)),
-// C = floor((K + B - 2) / B). One tile is NB = 128 consecutive output blocks (16384 outputs);
-// per tile the GEMM is D (128 x 256) += A (128 x 16) B (16 x 256) over K-steps (c, s0):
+// C = floor((K + B - 2) / B). One tile is NB = 96 consecutive output blocks (12288 outputs);
+// per tile the GEMM is D (128 x 192) += A (128 x 16) B (16 x 192) over K-steps (c, s0):
 //
 //  * A = T_c restricted to s in [s0, s0 + 16). Output rows are stored reversed (TMEM lane i holds
 //    output r = 127 - i); then every 8 x 8 core matrix of A depends only on (row group + K group),
@@ -30,8 +30,8 @@
 // buffers alternate, so the MMAs of one group overlap the drain of the previous one.
 //
 // Roles (544 threads): warps 0-15 are workers and warp 16 owns tensor memory and issues the MMAs
-// (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 64 (w / 4) .. +63, holds
-// those 64 running sums, writes those outputs, and shares the producing: each K-step's fp32
+// (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 48 (w / 4) .. +47, holds
+// those 48 running sums (96 registers per thread: one SM sub-partition hosts five of the 17 warps), writes those outputs, and shares the producing: each K-step's fp32
 // samples arrive by a 2-D TMA copy (zero fill outside the input) and are converted into the
 // FP16 planes; the next tile's scale is a max over its input window, copied by TMA in eight
 // slices, one per K-step of the current tile, and read a K-step later.
@@ -54,7 +54,7 @@ namespace {
 using namespace tc;
 
 constexpr int kB = 128;                  // outputs per block = MMA M
-constexpr int kNB = 128;                 // blocks per tile; MMA N = 2 * kNB = 256
+constexpr int kNB = 96;                  // blocks per tile; MMA N = 2 * kNB = 192
 constexpr int kN = 2 * kNB;
 constexpr int kStagesPerTile = kB / 16;  // K-steps of 16 samples
 constexpr int kWorkerWarps = 16;
@@ -64,7 +64,7 @@ constexpr int kThreads = 17 * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
 constexpr int kStepsPerGroup = 4;        // (K-step, chunk) steps per accumulator: 12 MMAs
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
-constexpr uint32_t kTmemCols = 512;      // two partial buffers of kN columns
+constexpr uint32_t kTmemCols = 512;      // two partial buffers of kN columns (384 used)
 constexpr uint32_t kIdesc = idesc_f16(kB, kN);
 
 struct Layout {
@@ -625,7 +625,7 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
     if (config.stages >= 6 && tc_layout(num_taps, 6).bytes <= 227u * 1024u) {
         return launch_stages<6>(x, taps, y, n, num_taps, stream);
     }
-    if (tc_layout(num_taps, 4).bytes <= 227u * 1024u) {
+    if (config.stages >= 4 && tc_layout(num_taps, 4).bytes <= 227u * 1024u) {
         return launch_stages<4>(x, taps, y, n, num_taps, stream);
     }
     return launch_stages<2>(x, taps, y, n, num_taps, stream);

@@ -10,7 +10,7 @@ namespace rfx {
 // Tile shape of the tensor-core FIR, chosen by the tuner.
 struct TcConfig {
     int tile_blocks;  // 128-output blocks per tile (the GEMM's N is twice this: I and Q)
-    int stages;       // operand ring depth
+    int stages;       // operand ring depth (2, 4 or 6; the largest that fits is used)
 };
 
 constexpr int kTcBatchMax = 4096;

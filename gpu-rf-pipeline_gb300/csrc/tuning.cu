@@ -71,7 +71,7 @@ TcConfig tuned_fir_tc_config(int num_taps, long long n)
     if (lookup(num_taps, n, &e) && e.impl == RFX_FIR_TC) {
         return e.config;
     }
-    return TcConfig{128, 4};
+    return TcConfig{96, 6};
 }
 
 }  // namespace rfx
@@ -104,8 +104,8 @@ extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, dou
         candidates.push_back({RFX_FIR_PLAIN, TcConfig{0, 0}});
     }
     if ((impl == RFX_FIR_TC || impl == RFX_FIR_AUTO) && fir_tc_supported(num_taps)) {
-        for (int tb : {64, 128}) {
-            for (int st : {4, 6}) {
+        for (int tb : {96}) {
+            for (int st : {2, 4, 6}) {
                 candidates.push_back({RFX_FIR_TC, TcConfig{tb, st}});
             }
         }
@@ -113,7 +113,7 @@ extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, dou
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    Entry best{RFX_FIR_PLAIN, TcConfig{128, 4}, 1e30};
+    Entry best{RFX_FIR_PLAIN, TcConfig{96, 6}, 1e30};
     for (const Candidate& c : candidates) {
         auto run = [&]() {
             return c.impl == RFX_FIR_TC

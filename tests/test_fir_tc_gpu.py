@@ -70,7 +70,7 @@ def test_tc_zeros_are_exact(taps: str) -> None:
 
 
 # Tap counts whose tap strip, sample ring and operand stages fit the 227 KB of shared memory.
-TC_MAX_TAPS = 2689
+TC_MAX_TAPS = 3457
 
 
 @pytest.mark.parametrize("k", [2, 3, 16, 31, 63, 64, 127, 128, 129, 255, 256, 257, 1025, 2049,
@@ -81,7 +81,10 @@ def test_tc_tap_counts(k: int) -> None:
     assert orc.normwise_error(y, orc.fir_fast(x, h)) <= TC_NORMWISE
 
 
-@pytest.mark.parametrize("n", [1, 5, 127, 128, 129, 16383, 16384, 16385, 3 * 16384 + 77,
+TILE = 96 * 128  # outputs per tensor-core tile
+
+
+@pytest.mark.parametrize("n", [1, 5, 127, 128, 129, TILE - 1, TILE, TILE + 1, 3 * TILE + 77,
                                200001])
 def test_tc_lengths(n: int) -> None:
     x, h = rand_case(n, 1025, seed=n)
@@ -97,20 +100,20 @@ def test_tc_beyond_capacity_uses_the_plain_kernel(k: int) -> None:
 
 
 def test_tc_per_tile_scale_spans_extreme_levels() -> None:
-    # Tiles (16384 outputs) at 1, 1e-30, 1e30, 3, 1e-12 and 1 times the unit level. Each tile
+    # Tiles (TILE outputs) at 1, 1e-30, 1e30, 3, 1e-12 and 1 times the unit level. Each tile
     # is scaled by the largest sample of its input window, which reaches C = 2 blocks into the
     # previous tile: a tile is held to 2e-6 of its own level when the previous tile is not
     # louder, and the whole capture to 2e-6 normwise.
-    x, h = rand_case(6 * 16384, 255, seed=11)
+    x, h = rand_case(6 * TILE, 255, seed=11)
     levels = np.array([1.0, 1e-30, 1e30, 3.0, 1e-12, 1.0])
-    x = (x * np.repeat(levels, 16384).astype(np.float32)).astype(np.complex64)
+    x = (x * np.repeat(levels, TILE).astype(np.float32)).astype(np.complex64)
     y = run(x, h)
     ref = orc.fir_fast(x, h)
     assert orc.normwise_error(y, ref) <= TC_NORMWISE
     for t in range(6):
         if t > 0 and levels[t - 1] > levels[t]:
             continue
-        seg = slice(t * 16384 + 512, (t + 1) * 16384)   # past the previous tile's filter tail
+        seg = slice(t * TILE + 512, (t + 1) * TILE)   # past the previous tile's filter tail
         assert orc.normwise_error(y[seg], ref[seg]) <= TC_NORMWISE, t
 
 
