@@ -23,14 +23,17 @@
 // scaled by 2^-(ex+eh) exactly.
 //
 // Accumulation: the tensor core adds each MMA's products into its FP32 accumulator with
-// round-toward-zero, so the error of an accumulator grows with the number of MMAs it takes.
-// Each TMEM accumulator therefore takes one GROUP of 12 MMAs (four consecutive (K-step, chunk)
-// steps x 3 products; a group may straddle two K-steps); the worker warps add every group's
-// partial sum into FP32 running sums in registers (round-to-nearest). Two 256-column partial
-// buffers alternate, so the MMAs of one group overlap the drain of the previous one.
+// round-toward-zero, so the error of an accumulator grows with the number of MMAs it takes, in
+// units of its own magnitude. The large product h_hi x_hi therefore goes to accumulator H in
+// GROUPS of 12 consecutive (K-step, chunk) steps (a group may straddle K-steps); the worker
+// warps add each group's sum into FP32 running sums in registers (round-to-nearest). The two
+// cross products, 2^-11 smaller, go to accumulator X for the whole tile and are drained once.
+// Per group the MMA thread issues the 12 H MMAs, commits, then the group's 24 X MMAs, during
+// which the workers drain H.
 //
 // Roles (544 threads): warps 0-15 are workers and warp 16 owns tensor memory and issues the MMAs
-// (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 48 (w / 4) .. +47, holds
+// (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 48 (w / 4) .. +47 of H
+// and of X, holds
 // those 48 running sums (96 registers per thread: one SM sub-partition hosts five of the 17 warps), writes those outputs, and shares the producing: each K-step's fp32
 // samples arrive by a 2-D TMA copy (zero fill outside the input) and are converted into the
 // FP16 planes; the next tile's scale is a max over its input window, copied by TMA in eight
@@ -62,9 +65,10 @@ constexpr int kWorkers = kWorkerWarps * 32;
 constexpr int kMmaWarp = 16;
 constexpr int kThreads = 17 * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
-constexpr int kStepsPerGroup = 4;        // (K-step, chunk) steps per accumulator: 12 MMAs
+constexpr int kHGroup = 12;              // MMAs per H accumulation, at most
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
-constexpr uint32_t kTmemCols = 512;      // two partial buffers of kN columns (384 used)
+constexpr uint32_t kTmemCols = 512;      // H (kN columns) and X (kN columns), 384 used
+constexpr uint32_t kXCol = kN;           // first column of X
 constexpr uint32_t kIdesc = idesc_f16(kB, kN);
 
 struct Layout {
@@ -109,8 +113,10 @@ struct Ctrl {
     unsigned long long raw_empty[kRaw];
     unsigned long long scan_full[2];
     unsigned long long scan_empty[2];
-    unsigned long long pfull[2];
-    unsigned long long pempty[2];
+    unsigned long long pfull;     // H group summed (tcgen05.commit)
+    unsigned long long pempty;    // H drained (every worker warp)
+    unsigned long long xfull;     // X of a tile summed
+    unsigned long long xempty;    // X drained
     unsigned long long reduce[2];
     unsigned long long teardown;
     uint32_t tmem_base;
@@ -119,6 +125,51 @@ struct Ctrl {
     uint32_t tap_max;
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
+
+// H groups of a tile. For P <= 12 chunks a group is `ksg` whole K-steps (at most 12 MMAs, and
+// fewer K-steps than operand stages, since a group holds its stages until its X MMAs); for
+// P > 12 each K-step splits into `gpk` groups of at most `cpg` chunks.
+struct HGroups {
+    int ksg;        // K-steps per group (P <= 12)
+    int gpk;        // groups per K-step (P > 12), else 1
+    int cpg;        // chunks per group (P > 12), else P
+    int per_tile;
+};
+
+__host__ __device__ inline HGroups h_groups(int P, int S)
+{
+    HGroups g;
+    if (P <= kHGroup) {
+        g.ksg = max(1, min(kHGroup / P, S - 1));
+        g.gpk = 1;
+        g.cpg = P;
+        g.per_tile = (kStagesPerTile + g.ksg - 1) / g.ksg;
+    } else {
+        g.ksg = 1;
+        g.gpk = (P + kHGroup - 1) / kHGroup;
+        g.cpg = (P + g.gpk - 1) / g.gpk;
+        g.gpk = (P + g.cpg - 1) / g.cpg;
+        g.per_tile = kStagesPerTile * g.gpk;
+    }
+    return g;
+}
+
+// K-steps [st0, st1) and chunks [c0, c1) of group gi of a tile.
+__device__ __forceinline__ void h_group_range(const HGroups& g, int P, int gi, int& st0, int& st1,
+                                              int& c0, int& c1)
+{
+    if (g.gpk == 1) {
+        st0 = gi * g.ksg;
+        st1 = min(kStagesPerTile, st0 + g.ksg);
+        c0 = 0;
+        c1 = P;
+    } else {
+        st0 = gi / g.gpk;
+        st1 = st0 + 1;
+        c0 = (gi - st0 * g.gpk) * g.cpg;
+        c1 = min(P, c0 + g.cpg);
+    }
+}
 
 }  // namespace
 
@@ -135,7 +186,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
     const Layout lay = tc_layout(num_taps, S);
     const int C = lay.C;
     const int P = C + 1;                       // chunks per K-step
-    const int groups_per_tile = 2 * P;         // 8 P steps / 4 per group
+    const HGroups grp = h_groups(P, S);
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const uint32_t sbase = smem_u32(smem);
@@ -163,10 +214,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
         for (int i = 0; i < 2; ++i) {
             mbar_init(smem_u32(&ctl.scan_full[i]), 1);
             mbar_init(smem_u32(&ctl.scan_empty[i]), kWorkerWarps);
-            mbar_init(smem_u32(&ctl.pfull[i]), 1);
-            mbar_init(smem_u32(&ctl.pempty[i]), kWorkerWarps);
             mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
         }
+        mbar_init(smem_u32(&ctl.pfull), 1);
+        mbar_init(smem_u32(&ctl.pempty), kWorkerWarps);
+        mbar_init(smem_u32(&ctl.xfull), 1);
+        mbar_init(smem_u32(&ctl.xempty), kWorkerWarps);
         mbar_init(smem_u32(&ctl.teardown), 1);
         ctl.abort = 0;
         ctl.tap_max = 0;
@@ -233,7 +286,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
         const uint32_t lane_addr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
                                    static_cast<uint32_t>(slice * kCols);
         const int wtid = threadIdx.x;                      // 0 .. kWorkers-1
-        int ex_ring[2] = {0, 0};                           // tile scale exponents, by tile parity
+        int ex_even = 0;                                   // scale exponents of even, odd tiles
+        int ex_odd = 0;
         uint32_t next_max = 0;                             // running max of the next tile's scan
 
         // Max of |samples| in [s, s + 2) clipped to hi_s (plain loads, for the partial block).
@@ -247,7 +301,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             }
             return 0u;
         };
-        // Combines every worker's partial max for tile k into ex_ring[k & 1].
+        // Combines every worker's partial max for tile k into its scale exponent.
         auto reduce_scale = [&](int k, uint32_t m) -> bool {
             m = __reduce_max_sync(0xFFFFFFFFu, m);
             const int rb = k & 1;
@@ -264,7 +318,11 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             for (int w = 0; w < kWorkerWarps; ++w) {
                 tmax = max(tmax, ctl.warp_max[rb][w]);
             }
-            ex_ring[k & 1] = scale_exponent(tmax);
+            if (k & 1) {
+                ex_odd = scale_exponent(tmax);
+            } else {
+                ex_even = scale_exponent(tmax);
+            }
             return true;
         };
         // Scan slice q (tile q / 8 + 1, window rows (q % 8) srows .. +srows): copied by TMA one
@@ -317,7 +375,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             const int k = v / kStagesPerTile;
             const int st = v % kStagesPerTile;
             const long long j0 = static_cast<long long>(tile_of(k)) * kNB;
-            const int ex = ex_ring[k & 1];
+            const int ex = (k & 1) ? ex_odd : ex_even;
             const float fa = exp2i(ex / 2);
             const float fb = exp2i(ex - ex / 2);
             const int slot = v % S;
@@ -433,20 +491,13 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
         for (int u = 0; u < my_steps && ok && !*abort; ++u) {
             const int k = u / kStagesPerTile;
             const int st = u % kStagesPerTile;
-            // Drain the groups whose last (K-step, chunk) step lies in K-step u.
-            while (kStepsPerGroup * gi + kStepsPerGroup - 1 < (st + 1) * P) {
-                const int g = k * groups_per_tile + gi;
-                const int pb = g & 1;
-                if (!mbar_wait_bounded(smem_u32(&ctl.pfull[pb]), (g >> 1) & 1, fault,
-                                       kFaultAccumFull, abort)) {
-                    ok = false;
-                    break;
-                }
+            // Adds accumulator columns col .. col + kCols - 1 of this lane into acc.
+            auto drain = [&](uint32_t col) {
                 fence_after();
 #pragma unroll
                 for (int c16 = 0; c16 < kCols / 16; ++c16) {
                     uint32_t t[16];
-                    tmem_ld16(lane_addr + static_cast<uint32_t>(pb * kN + c16 * 16), t);
+                    tmem_ld16(lane_addr + col + static_cast<uint32_t>(c16 * 16), t);
                     tmem_wait_ld();
 #pragma unroll
                     for (int i = 0; i < 16; ++i) {
@@ -455,8 +506,20 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                 }
                 fence_before();
                 __syncwarp();
+            };
+            // Drain the H groups whose last (K-step, chunk) step lies in K-step u.
+            while (gi < grp.per_tile &&
+                   (grp.gpk == 1 ? min(kStagesPerTile, (gi + 1) * grp.ksg) - 1 : gi / grp.gpk) <=
+                       st) {
+                const int g = k * grp.per_tile + gi;
+                if (!mbar_wait_bounded(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
+                                       abort)) {
+                    ok = false;
+                    break;
+                }
+                drain(0);
                 if (lane == 0) {
-                    mbar_arrive(smem_u32(&ctl.pempty[pb]));
+                    mbar_arrive(smem_u32(&ctl.pempty));
                 }
                 ++gi;
             }
@@ -464,8 +527,17 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                 break;
             }
             if (st == kStagesPerTile - 1) {
+                // The tile's cross products.
+                if (!mbar_wait_bounded(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull,
+                                       abort)) {
+                    break;
+                }
+                drain(kXCol);
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(&ctl.xempty));
+                }
                 // Last K-step of tile k: scale and store this thread's outputs.
-                const int shift = -(ex_ring[k & 1] + eh);
+                const int shift = -(((k & 1) ? ex_odd : ex_even) + eh);
                 const float fa = exp2i(shift / 2);
                 const float fb = exp2i(shift - shift / 2);
                 const long long jb0 = static_cast<long long>(tile_of(k)) * kNB + slice * (kCols / 2);
@@ -488,45 +560,96 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
         // ---- MMA issuer (warp 16, one thread) ----------------------------------------------
         const uint32_t taps_hi = sbase + lay.taps_hi;
         const uint32_t taps_lo = sbase + lay.taps_lo;
+        // The issue loop is latency-bound in this one thread, so it is kept lean: per MMA one
+        // descriptor step and the MMA. Descriptors differ only in their start-address field
+        // (address / 16): the tap strip descriptor of (K-step st, chunk c) starts
+        // 16 (C - c) + 2 st core matrices in, the sample descriptor 2 (C - c) rows into the
+        // stage's planes; each next chunk is 128 (strip) and 2 (planes) units lower.
         bool stop = false;
-        for (int u = 0; u < my_steps && !stop && !*abort; ++u) {
-            const int k = u / kStagesPerTile;
-            const int st = u % kStagesPerTile;
-            const int slot = u % S;
-            if (!mbar_wait_bounded(smem_u32(&ctl.full[slot]), (u / S) & 1, fault,
-                                   kFaultStageFull, abort)) {
-                break;
-            }
-            fence_after();
-            const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
-            const int s0 = st * 16;
-            for (int c = 0; c < P; ++c) {
-                const int cs = st * P + c;                 // tile-local step
-                const int g = k * groups_per_tile + cs / kStepsPerGroup;
-                const int pb = g & 1;
-                if (cs % kStepsPerGroup == 0) {
-                    if (!mbar_wait_bounded(smem_u32(&ctl.pempty[pb]), ((g >> 1) & 1) ^ 1, fault,
+        const unsigned long long a_desc = smem_desc(0, 128, 128);
+        const unsigned long long b_desc = smem_desc(0, lay.pitch, 128);
+        const uint32_t a_hi0 = (taps_hi >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+        const uint32_t a_lo0 = (taps_lo >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+        const uint32_t stage_units = lay.stage >> 4;
+        const uint32_t split_units = lay.split >> 4;
+        const uint32_t b_base = ((sbase + lay.stages0) >> 4) + static_cast<uint32_t>(2 * C);
+        const uint32_t h_acc = tmem;
+        const uint32_t x_acc = tmem + kXCol;
+        int ready = 0;        // K-steps (block-wide numbering) whose stage has been waited for
+        for (int k = 0; k < my_tiles && !stop && !*abort; ++k) {
+            for (int gi = 0; gi < grp.per_tile && !stop; ++gi) {
+                const int g = k * grp.per_tile + gi;
+                int st0, st1, c0, c1;
+                h_group_range(grp, P, gi, st0, st1, c0, c1);
+                // H is free once the workers drained the previous group.
+                if (!mbar_wait_bounded(smem_u32(&ctl.pempty), (g & 1) ^ 1, fault,
+                                       kFaultAccumEmpty, abort)) {
+                    stop = true;
+                    break;
+                }
+                fence_after();
+                // Pass 0: h_hi x_hi into H.
+                uint32_t acc = 0;
+                for (int st = st0; st < st1; ++st) {
+                    const int u = k * kStagesPerTile + st;
+                    const int slot = u % S;
+                    if (u >= ready) {
+                        if (!mbar_wait_bounded(smem_u32(&ctl.full[slot]), (u / S) & 1, fault,
+                                               kFaultStageFull, abort)) {
+                            stop = true;
+                            break;
+                        }
+                        fence_after();
+                        ready = u + 1;
+                    }
+                    uint32_t a = a_hi0 + static_cast<uint32_t>(2 * st - 16 * c0) * 8u;
+                    uint32_t b = b_base + static_cast<uint32_t>(slot) * stage_units -
+                                 static_cast<uint32_t>(2 * c0);
+                    for (int c = c0; c < c1; ++c) {
+                        mma_f16<kIdesc>(h_acc, a_desc | a, b_desc | b, acc);
+                        acc = 1;
+                        a -= 128;
+                        b -= 2;
+                    }
+                }
+                if (stop) {
+                    break;
+                }
+                mma_commit(smem_u32(&ctl.pfull));
+                // Pass 1: h_hi x_lo + h_lo x_hi into X, zeroed at the tile's first MMA.
+                if (gi == 0) {
+                    if (!mbar_wait_bounded(smem_u32(&ctl.xempty), (k & 1) ^ 1, fault,
                                            kFaultAccumEmpty, abort)) {
                         stop = true;
                         break;
                     }
                     fence_after();
                 }
-                const uint32_t dt = tmem + static_cast<uint32_t>(pb * kN);
-                const uint32_t t0 = static_cast<uint32_t>(16 * (C - c) + s0 / 8) * 128u;
-                const unsigned long long a_hi = smem_desc(taps_hi + t0, 128, 128);
-                const unsigned long long a_lo = smem_desc(taps_lo + t0, 128, 128);
-                const uint32_t row0 = static_cast<uint32_t>(2 * (C - c)) * 16u;
-                const unsigned long long b_hi = smem_desc(stage + row0, lay.pitch, 128);
-                const unsigned long long b_lo = smem_desc(stage + lay.split + row0, lay.pitch, 128);
-                mma_f16<kIdesc>(dt, a_hi, b_hi, cs % kStepsPerGroup != 0 ? 1u : 0u);
-                mma_f16<kIdesc>(dt, a_hi, b_lo, 1u);
-                mma_f16<kIdesc>(dt, a_lo, b_hi, 1u);
-                if (cs % kStepsPerGroup == kStepsPerGroup - 1) {
-                    mma_commit(smem_u32(&ctl.pfull[pb]));
+                acc = gi == 0 ? 0u : 1u;
+                for (int st = st0; st < st1; ++st) {
+                    const int slot = (k * kStagesPerTile + st) % S;
+                    const uint32_t off = static_cast<uint32_t>(2 * st - 16 * c0) * 8u;
+                    uint32_t ah = a_hi0 + off;
+                    uint32_t al = a_lo0 + off;
+                    uint32_t b = b_base + static_cast<uint32_t>(slot) * stage_units -
+                                 static_cast<uint32_t>(2 * c0);
+                    for (int c = c0; c < c1; ++c) {
+                        mma_f16<kIdesc>(x_acc, a_desc | ah, b_desc | (b + split_units), acc);
+                        mma_f16<kIdesc>(x_acc, a_desc | al, b_desc | b, 1u);
+                        acc = 1;
+                        ah -= 128;
+                        al -= 128;
+                        b -= 2;
+                    }
+                    if (c1 == P) {
+                        // Every MMA reading this K-step's operand stage has been issued.
+                        mma_commit(smem_u32(&ctl.empty[slot]));
+                    }
                 }
             }
-            mma_commit(smem_u32(&ctl.empty[slot]));
+            if (!stop) {
+                mma_commit(smem_u32(&ctl.xfull));
+            }
         }
         // Every MMA this thread issued has completed before tensor memory is released.
         mma_commit(smem_u32(&ctl.teardown));
