@@ -67,6 +67,8 @@ constexpr int kThreads = 17 * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
 constexpr int kHGroup = 12;              // MMAs per H accumulation, at most
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
+constexpr int kScanBufsMax = 4;          // scan slice ring depth: 4 (2 for the longest filters);
+                                         // slices are copied depth - 1 K-steps ahead
 constexpr uint32_t kTmemCols = 512;      // H (kN columns) and X (kN columns), 384 used
 constexpr uint32_t kXCol = kN;           // first column of X
 constexpr uint32_t kIdesc = idesc_f16(kB, kN);
@@ -81,12 +83,14 @@ struct Layout {
     uint32_t raw;        // bytes per raw stage: rows * 16 samples * 8 B
     uint32_t scan;       // bytes per scan slice: srows * 128 samples * 8 B
     int tcount;          // core matrices of the tap strip
+    int sbufs;           // scan slice buffers
     uint32_t taps_hi, taps_lo, raw0, scan0, stages0, bytes;
 };
 
-__host__ __device__ inline Layout tc_layout(int num_taps, int stages)
+__host__ __device__ inline Layout tc_layout(int num_taps, int stages, int sbufs)
 {
     Layout l;
+    l.sbufs = sbufs;
     l.C = (num_taps + kB - 2) / kB;
     l.rows = kNB + l.C;
     l.srows = (l.rows + kStagesPerTile - 1) / kStagesPerTile;
@@ -100,7 +104,7 @@ __host__ __device__ inline Layout tc_layout(int num_taps, int stages)
     l.taps_lo = l.taps_hi + 128u * static_cast<uint32_t>(l.tcount);
     l.raw0 = (l.taps_lo + 128u * static_cast<uint32_t>(l.tcount) + 127u) & ~127u;
     l.scan0 = l.raw0 + kRaw * l.raw;
-    l.stages0 = l.scan0 + 2u * l.scan;
+    l.stages0 = l.scan0 + static_cast<uint32_t>(sbufs) * l.scan;
     l.bytes = l.stages0 + l.stage * static_cast<uint32_t>(stages);
     return l;
 }
@@ -111,8 +115,8 @@ struct Ctrl {
     unsigned long long empty[8];
     unsigned long long raw_full[kRaw];
     unsigned long long raw_empty[kRaw];
-    unsigned long long scan_full[2];
-    unsigned long long scan_empty[2];
+    unsigned long long scan_full[kScanBufsMax];
+    unsigned long long scan_empty[kScanBufsMax];
     unsigned long long pfull;     // H group summed (tcgen05.commit)
     unsigned long long pempty;    // H drained (every worker warp)
     unsigned long long xfull;     // X of a tile summed
@@ -179,11 +183,11 @@ template <int S>
 __global__ void __launch_bounds__(kThreads, 1)
 fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap smap,
               const float2* __restrict__ x, const float* __restrict__ taps,
-              float2* __restrict__ y, long long n, int num_taps, int num_tiles)
+              float2* __restrict__ y, long long n, int num_taps, int num_tiles, int sbufs)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
-    const Layout lay = tc_layout(num_taps, S);
+    const Layout lay = tc_layout(num_taps, S, sbufs);
     const int C = lay.C;
     const int P = C + 1;                       // chunks per K-step
     const HGroups grp = h_groups(P, S);
@@ -212,9 +216,11 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             mbar_init(smem_u32(&ctl.raw_empty[i]), kWorkerWarps);
         }
         for (int i = 0; i < 2; ++i) {
+            mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
+        }
+        for (int i = 0; i < sbufs; ++i) {
             mbar_init(smem_u32(&ctl.scan_full[i]), 1);
             mbar_init(smem_u32(&ctl.scan_empty[i]), kWorkerWarps);
-            mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
         }
         mbar_init(smem_u32(&ctl.pfull), 1);
         mbar_init(smem_u32(&ctl.pempty), kWorkerWarps);
@@ -229,13 +235,25 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
         tmem_alloc(smem_u32(&ctl.tmem_base), kTmemCols);
     }
     __syncthreads();
-    // Raw sample stages 0 .. kRaw-1 (K-step u: rows from block 128 k - C, floats 32 (u % 8)..).
+    // Scan slice q: the next tile's (q / 8 + 1) window rows (q % 8) srows .. + srows.
+    auto issue_scan = [&](int q) {
+        const int kn = q / kStagesPerTile + 1;
+        const uint32_t bar = smem_u32(&ctl.scan_full[q % sbufs]);
+        mbar_arrive_expect_tx(bar, lay.scan);
+        tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(q % sbufs) * lay.scan, &smap,
+                    0, tile_of(kn) * kNB - C + (q % kStagesPerTile) * lay.srows, bar);
+    };
+    // Raw sample stages 0 .. kRaw-1 (K-step u: rows from block 128 k - C, floats 32 (u % 8)..)
+    // and the first scan slices.
     if (threadIdx.x == 0) {
         for (int u = 0; u < kRaw && u < my_steps; ++u) {
             const uint32_t bar = smem_u32(&ctl.raw_full[u]);
             mbar_arrive_expect_tx(bar, lay.raw);
             tma_load_2d(sbase + lay.raw0 + u * lay.raw, &xmap, 32 * (u % kStagesPerTile),
                         tile_of(u / kStagesPerTile) * kNB - C, bar);
+        }
+        for (int q = 0; q < sbufs - 2 && q < scan_slices; ++q) {
+            issue_scan(q);
         }
     }
     // Largest tap magnitude (bit pattern of |h|: ordered like the value).
@@ -325,12 +343,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             }
             return true;
         };
-        // Scan slice q (tile q / 8 + 1, window rows (q % 8) srows .. +srows): copied by TMA one
-        // K-step earlier; rows past the window are ignored, the partial last block is read
-        // from global memory.
+        // Scan slice q, copied by TMA sbufs - 1 K-steps earlier: rows past the window are
+        // ignored; the partial last block lies outside the tensor map (the copy reads zeros
+        // there) and is read from global memory.
         auto consume_slice = [&](int q) -> bool {
-            const int qb = q & 1;
-            if (!mbar_wait_bounded(smem_u32(&ctl.scan_full[qb]), (q >> 1) & 1, fault,
+            const int qb = q % sbufs;
+            if (!mbar_wait_bounded(smem_u32(&ctl.scan_full[qb]), (q / sbufs) & 1, fault,
                                    kFaultTileLoad, abort)) {
                 return false;
             }
@@ -338,19 +356,14 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             const long long j0 = static_cast<long long>(tile_of(k)) * kNB;
             const int r0 = (q % kStagesPerTile) * lay.srows;
             const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
-            const int quads = lay.srows * 64;   // float4 per slice
+            const int quads = min(lay.srows, lay.rows - r0) * 64;   // float4 in the window
             uint32_t m = next_max;
             for (int f = wtid; f < quads; f += kWorkers) {
-                const int row = r0 + (f >> 6);
-                if (row >= lay.rows) {
-                    continue;
-                }
-                const long long jb = j0 - C + row;
-                if (jb != full_blocks) {
-                    m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
-                } else {
-                    m = max(m, load_pair(jb * kB + 2 * (f & 63), n));
-                }
+                m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
+            }
+            const long long tail_row = full_blocks - (j0 - C) - r0;
+            if (tail_row >= 0 && tail_row * 64 < quads && wtid < 64) {
+                m = max(m, load_pair(full_blocks * kB + 2 * wtid, n));
             }
             next_max = m;
             __syncwarp();
@@ -366,8 +379,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             return true;
         };
 
-        // Producing K-step v: finish the scan slice copied during step v - 1, convert the raw
-        // samples into the FP16 planes, then queue step v + kRaw's raw copy and scan slice v.
+        // Producing K-step v: finish scan slice v - 1, convert the raw samples into the FP16
+        // planes, then queue step v + kRaw's raw copy and scan slice v + sbufs - 2.
         auto produce = [&](int v) -> bool {
             if (v >= 1 && v - 1 < scan_slices && !consume_slice(v - 1)) {
                 return false;
@@ -389,16 +402,18 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
             const uint32_t raw = sbase + lay.raw0 + static_cast<uint32_t>(rslot) * lay.raw;
             const int items = lay.rows * 8;  // float4 (two samples) per window row
+            // Window row of the input's last, partial block (outside the tensor maps), if any.
+            const long long tail_rel = full_blocks - (j0 - C);
+            const int b_tail = tail_rel >= 0 && tail_rel < lay.rows ? static_cast<int>(tail_rel) : -1;
             for (int f = wtid; f < items; f += kWorkers) {
                 const int b = f >> 3;
                 const int q = f & 7;
-                const long long jb = j0 - C + b;
                 float4 v4;
-                if (jb != full_blocks) {
+                if (b != b_tail) {
                     v4 = lds128(raw + static_cast<uint32_t>(f) * 16u);  // zero outside [0, n)
                 } else {
-                    // The input's last, partial block is outside the tensor maps: plain loads.
-                    const long long sidx = jb * kB + 16 * st + 2 * q;
+                    // The partial block: plain loads.
+                    const long long sidx = full_blocks * kB + 16 * st + 2 * q;
                     v4 = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (sidx + 1 < n) {
                         v4 = __ldg(reinterpret_cast<const float4*>(x + sidx));
@@ -438,19 +453,15 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                     tma_load_2d(raw, &xmap, 32 * (vn % kStagesPerTile),
                                 tile_of(vn / kStagesPerTile) * kNB - C, bar);
                 }
-                // Scan slice v (for tile v / 8 + 1) into buffer v & 1 once slice v - 2 is read.
-                if (v < scan_slices) {
-                    const int qb = v & 1;
-                    if (!mbar_wait_bounded(smem_u32(&ctl.scan_empty[qb]), ((v >> 1) & 1) ^ 1,
-                                           fault, kFaultStageEmpty, abort)) {
+                // Scan slice q into its buffer once slice q - sbufs is read.
+                const int q = v + sbufs - 2;
+                if (q < scan_slices) {
+                    if (!mbar_wait_bounded(smem_u32(&ctl.scan_empty[q % sbufs]),
+                                           ((q / sbufs) & 1) ^ 1, fault, kFaultStageEmpty,
+                                           abort)) {
                         return false;
                     }
-                    const int kn = v / kStagesPerTile + 1;
-                    const uint32_t bar = smem_u32(&ctl.scan_full[qb]);
-                    mbar_arrive_expect_tx(bar, lay.scan);
-                    tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan, &smap,
-                                0, tile_of(kn) * kNB - C + (v % kStagesPerTile) * lay.srows,
-                                bar);
+                    issue_scan(q);
                 }
             }
             return true;
@@ -672,15 +683,15 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
 
 bool fir_tc_supported(int num_taps)
 {
-    const Layout l = tc_layout(num_taps, 2);
+    const Layout l = tc_layout(num_taps, 2, 2);
     return num_taps > 1 && l.bytes <= 227u * 1024u && l.rows <= 256;
 }
 
 template <int S>
 static cudaError_t launch_stages(const void* x, const float* taps, void* y, long long n,
-                                 int num_taps, cudaStream_t stream)
+                                 int num_taps, int sbufs, cudaStream_t stream)
 {
-    const Layout lay = tc_layout(num_taps, S);
+    const Layout lay = tc_layout(num_taps, S, sbufs);
     int device = 0;
     cudaError_t err = cudaGetDevice(&device);
     if (err != cudaSuccess) {
@@ -728,7 +739,7 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
     const int grid = tiles < sms ? tiles : sms;
     fir_tc_kernel<S><<<grid, kThreads, bytes, stream>>>(
         map, smap, static_cast<const float2*>(x), taps, static_cast<float2*>(y), n, num_taps,
-        tiles);
+        tiles, sbufs);
     return cudaGetLastError();
 }
 
@@ -745,13 +756,19 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
         // Shorter than one block: the tensor map would be empty; the plain kernel is exact.
         return fir_plain_launch(x, taps, y, n, num_taps, stream);
     }
-    if (config.stages >= 6 && tc_layout(num_taps, 6).bytes <= 227u * 1024u) {
-        return launch_stages<6>(x, taps, y, n, num_taps, stream);
+    // The deep scan ring first (it hides the scan copies' latency), then the most stages.
+    for (int sbufs = kScanBufsMax; sbufs >= 2; sbufs -= 2) {
+        if (config.stages >= 6 && tc_layout(num_taps, 6, sbufs).bytes <= 227u * 1024u) {
+            return launch_stages<6>(x, taps, y, n, num_taps, sbufs, stream);
+        }
+        if (config.stages >= 4 && tc_layout(num_taps, 4, sbufs).bytes <= 227u * 1024u) {
+            return launch_stages<4>(x, taps, y, n, num_taps, sbufs, stream);
+        }
+        if (tc_layout(num_taps, 2, sbufs).bytes <= 227u * 1024u) {
+            return launch_stages<2>(x, taps, y, n, num_taps, sbufs, stream);
+        }
     }
-    if (config.stages >= 4 && tc_layout(num_taps, 4).bytes <= 227u * 1024u) {
-        return launch_stages<4>(x, taps, y, n, num_taps, stream);
-    }
-    return launch_stages<2>(x, taps, y, n, num_taps, stream);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t fir_tc_take_fault(unsigned int* code)
