@@ -42,6 +42,7 @@
 // stops.
 #include "fir_tc.cuh"
 #include "fir_plain.cuh"
+#include "fir_tc2.cuh"
 #include "tc_common.cuh"
 #include "tmap.hpp"
 
@@ -751,6 +752,9 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
     }
     if (!fir_tc_supported(num_taps)) {
         return cudaErrorInvalidValue;
+    }
+    if (config.tile_blocks == kTcPairTile && n >= 2 * kB && fir_tc2_supported(num_taps)) {
+        return fir_tc2_launch(x, taps, y, n, num_taps, config.stages, stream);
     }
     if (n < kB) {
         // Shorter than one block: the tensor map would be empty; the plain kernel is exact.

@@ -7,11 +7,13 @@
 
 namespace rfx {
 
-// Tile shape of the tensor-core FIR, chosen by the tuner.
+// Form and tile shape of the tensor-core FIR, chosen by the tuner.
 struct TcConfig {
-    int tile_blocks;  // 128-output blocks per tile (the GEMM's N is twice this: I and Q)
-    int stages;       // operand ring depth (2, 4 or 6; the largest that fits is used)
+    int tile_blocks;  // 128-output blocks per tile: 96 = one CTA per tile (fir_tc.cu),
+                      // 192 = a CTA pair per tile of 96 256-output blocks (fir_tc2.cu)
+    int stages;       // operand ring depth cap (the largest that fits is used)
 };
+constexpr int kTcPairTile = 192;
 
 constexpr int kTcBatchMax = 4096;
 

@@ -6,6 +6,7 @@
 #include "chan_tc.cuh"
 #include "fir_plain.cuh"
 #include "fir_tc.cuh"
+#include "fir_tc2.cuh"
 #include "tuning.hpp"
 
 #include <cuda_runtime.h>
@@ -160,6 +161,11 @@ int rfx_device_fault(unsigned int* code)
     part = 0;
     if ((err = rfx::fir_tc_take_fault(&part)) != cudaSuccess) {
         return cuda_fail(err, "fir_tc fault word");
+    }
+    total |= part;
+    part = 0;
+    if ((err = rfx::fir_tc2_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "fir_tc2 fault word");
     }
     total |= part;
     part = 0;

@@ -104,10 +104,11 @@ extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, dou
         candidates.push_back({RFX_FIR_PLAIN, TcConfig{0, 0}});
     }
     if ((impl == RFX_FIR_TC || impl == RFX_FIR_AUTO) && fir_tc_supported(num_taps)) {
-        for (int tb : {96}) {
-            for (int st : {2, 4, 6}) {
-                candidates.push_back({RFX_FIR_TC, TcConfig{tb, st}});
-            }
+        for (int st : {2, 4, 6}) {
+            candidates.push_back({RFX_FIR_TC, TcConfig{96, st}});
+        }
+        for (int st : {2, 4, 6}) {
+            candidates.push_back({RFX_FIR_TC, TcConfig{kTcPairTile, st}});
         }
     }
     cudaEvent_t a, b;
