@@ -2,11 +2,14 @@
 """Benchmark of the complex-baseband filtering path on GB300 — one JSON line on stdout.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload fir1025|fir63|pfb64]
+                    [--workload fir1025|fir63|pfb64|pfb1024|batch256]
 
 A step is one pass of the hot path over one batch of synthetic input: by default the long FIR
 (2^24 cf32 samples = 8 tones over 60 dB + AWGN at 10 dB SNR, 1025 Kaiser-windowed-sinc taps),
-the workload the headline metric (Msamples/s, FIR 1025 taps) is quoted on.
+the workload the headline metric (Msamples/s, FIR 1025 taps) is quoted on. The other
+workloads: fir63 (2^24 samples, 63 taps), pfb64 (64-channel channelizer, 2^24 samples, 1024
+taps), pfb1024 (1024-channel channelizer, 2^26 samples, 32768 taps), batch256 (256 captures of
+2^12 .. 2^22 samples, each with its own 31 .. 1025 taps).
 
 Timing: W untimed steps, then exactly K steps between a barrier + device synchronize on both
 sides, measured with CUDA events on the launching stream; max over ranks. Two input/output
@@ -210,6 +213,10 @@ def load_workload(name: str):
         return signals.plain_fir(1 << 24)
     if name == "pfb64":
         return signals.channelizer64(1 << 24)
+    if name == "pfb1024":
+        return signals.channelizer1024(1 << 26)
+    if name == "batch256":
+        return signals.batched_fir()
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -277,10 +284,71 @@ class Arm:
             self.plan.close()
 
 
+class BatchArm:
+    """The batched workload: every capture with its own taps, device-resident; one step is
+    one rfx_fir_batch_launch over all captures (tensor core: one persistent launch per 192
+    captures; plain: one launch per capture, as the project runs a batch)."""
+
+    def __init__(self, rfx, w, impl: str, device) -> None:
+        import torch
+
+        self.rfx, self.w, self.impl = rfx, w, impl
+        # All captures packed in one buffer (each starting on a 16-byte boundary).
+        self.offsets, total = [], 0
+        for x, _ in w.captures:
+            self.offsets.append(total)
+            total += x.size + (x.size & 1)
+        self.host = np.zeros(total, np.complex64)
+        for (x, _), o in zip(w.captures, self.offsets):
+            self.host[o:o + x.size] = x
+        self.X = torch.from_numpy(self.host).to(device)
+        self.Y = torch.zeros_like(self.X)
+        self.caps = []
+        for (x, h), o in zip(w.captures, self.offsets):
+            self.caps.append((self.X[o:o + x.size], self.Y[o:o + x.size],
+                              torch.from_numpy(h).to(device)))
+        self.n = int(sum(x.size for x, _ in w.captures))
+        self.arr = (rfx.FirCapture * len(self.caps))()
+        for i, (xd, yd, hd) in enumerate(self.caps):
+            self.arr[i] = rfx.FirCapture(xd.data_ptr(), yd.data_ptr(), hd.data_ptr(), xd.numel(),
+                                         hd.numel(), 0)
+        self.impl_v = rfx.parse_fir_impl(impl)
+        count = len(self.caps)
+        self.launches_per_step = (-(-count // 192) if impl == "tc_split"
+                                  else sum(1 for x, _ in w.captures if x.size))
+        self.dtype = "f16x3->f32" if impl == "tc_split" else "f32"
+
+    def launch(self, i: int) -> None:
+        self.rfx._check(self.rfx.load().rfx_fir_batch_launch(self.impl_v, self.arr, len(self.caps),
+                                                              None))
+
+    def error(self) -> float:
+        """Largest normwise error against the float64 oracle over every 8th capture (first 2^16
+        samples of each)."""
+        import torch
+        from oracle import rf_oracle as orc
+
+        self.launch(0)
+        torch.cuda.synchronize()
+        worst = 0.0
+        for (x, h), (_, yd, _) in list(zip(self.w.captures, self.caps))[::8]:
+            m = min(x.size, 1 << 16)
+            got = yd[:m].cpu().numpy()
+            worst = max(worst, orc.normwise_error(got, orc.fir_fast(x[:m], h)))
+        return worst
+
+    def release(self) -> None:
+        self.caps = self.arr = self.X = self.Y = None
+
+
+def make_arm(rfx, w, impl: str, device):
+    return BatchArm(rfx, w, impl, device) if w.captures else Arm(rfx, w, impl, device)
+
+
 def available(rfx, w, impl: str, device) -> bool:
     """Whether this library can run `impl` on workload `w` (tries one launch)."""
     try:
-        arm = Arm(rfx, w, impl, device)
+        arm = make_arm(rfx, w, impl, device)
         arm.launch(0)
         arm.release()
         return True
@@ -364,6 +432,73 @@ def cpu_chan_baseline(x: np.ndarray, h: np.ndarray, m: int, target_s: float = 2.
                       f"{dt:.2f} s on {threads} threads"}
 
 
+def cpu_batch_baseline(captures, target_s: float = 2.0) -> dict:
+    """The oracle's float64 FIR on all host cores over the batch's captures in order, until
+    the captures run so far took at least target_s."""
+    from oracle import rf_oracle as orc
+
+    threads = os.cpu_count() or 1
+    done = 0
+    count = 0
+    t0 = time.perf_counter()
+    for x, h in captures:
+        orc.fir_fast(x, h, threads=threads)
+        done += x.size
+        count += 1
+        if time.perf_counter() - t0 >= target_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"first {count} captures of the batch ({done} samples, own taps each), "
+                      f"float64, {dt:.2f} s on {threads} threads"}
+
+
+def config_of(w, impl: str, n: int) -> dict:
+    if w.captures:
+        ks = sorted({int(h.size) for _, h in w.captures})
+        return {"workload": w.name, "impl": impl, "captures": len(w.captures), "samples": n,
+                "taps": ks, "channels": None,
+                "l2": f"inputs larger than L2: {16 * n / 1e9:.2f} GB moved per step",
+                "seed": w.meta.get("seed")}
+    return {"workload": w.name, "impl": impl, "samples": n, "taps": int(w.taps.size),
+            "channels": w.channels or None,
+            "l2": "inputs larger than L2: two input/output buffer sets alternate",
+            "seed": w.meta.get("seed")}
+
+
+def batch_e2e(rfx, w, impl: str, args, device) -> dict:
+    """The batch end to end: every step copies the packed captures from pinned host memory,
+    runs rfx_fir_batch_launch and copies every output back, timed with CUDA events."""
+    import torch
+
+    arm = BatchArm(rfx, w, impl, device)
+    xp = torch.from_numpy(arm.host).pin_memory()
+    yp = torch.empty_like(xp).pin_memory()
+
+    def step(i: int) -> None:
+        arm.X.copy_(xp, non_blocking=True)
+        arm.launch(i)
+        yp.copy_(arm.Y, non_blocking=True)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for i in range(args.steps):
+        step(i)
+    b.record()
+    torch.cuda.synchronize()
+    step_ms = a.elapsed_time(b) / args.steps
+    bytes_ = int(xp.numel()) * 8
+    arm.release()
+    return {"value": arm.n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
+            "h2d_bytes_per_step": bytes_, "d2h_bytes_per_step": bytes_, "step_ms": step_ms,
+            "note": "captures packed in one pinned buffer; one copy each way per step; the "
+                    "taps stay resident"}
+
+
 # --- the reference arm -------------------------------------------------------------------------
 
 def run_reference(args) -> None:
@@ -374,7 +509,9 @@ def run_reference(args) -> None:
     times = []
     base = None
     for i in range(args.warmup + args.steps):
-        if w.channels:
+        if w.captures:
+            b = cpu_batch_baseline(w.captures, target_s=1.0)
+        elif w.channels:
             b = cpu_chan_baseline(w.x, w.taps, w.channels, target_s=1.0)
         else:
             b = cpu_fir_baseline(w.x, w.taps, target_s=1.0)
@@ -387,8 +524,8 @@ def run_reference(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w.name, "samples": int(w.x.size), "taps": int(w.taps.size),
-                   "channels": w.channels or None, "l2": "n/a (CPU)"},
+        "config": {**config_of(w, "reference", sum(int(x.size) for x, _ in w.captures)
+                              if w.captures else int(w.x.size)), "l2": "n/a (CPU)"},
         "cpu_baseline": {**base, "value": value},
         "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -405,7 +542,7 @@ def measure_arms(rfx, w, impls, args, dist, device, sample_clocks=False):
     for impl in impls:
         if not available(rfx, w, impl, device):
             continue
-        arm = Arm(rfx, w, impl, device)
+        arm = make_arm(rfx, w, impl, device)
         if sample_clocks and clocks is None:
             with ClockSampler(device.index if device.index is not None else 0) as cs:
                 seconds = time_device(arm.launch, args.steps, args.warmup, dist, device)
@@ -435,7 +572,16 @@ def run_ours(args) -> None:
     pk = peaks()
 
     w = load_workload(args.workload)
-    n = int(w.x.size)
+    if w.captures:
+        ns = [int(x.size) for x, _ in w.captures]
+        n = sum(ns)
+        useful = sum(4.0 * h.size * m for (_, h), m in zip(w.captures, ns))
+    else:
+        n = int(w.x.size)
+        if w.channels:
+            useful = 4.0 * n * (-(-w.taps.size // w.channels))  # branch FIR flops
+        else:
+            useful = 4.0 * n * w.taps.size                       # FIR flops
     arms, clocks = measure_arms(rfx, w, ["tc_split", "plain"], args, dist, device,
                                 sample_clocks=True)
     impl = next(iter(arms))
@@ -445,13 +591,17 @@ def run_ours(args) -> None:
 
     # Roofline of the dominant kernel.
     extras: dict = {}
-    if w.channels:
-        useful = 4.0 * n * (-(-w.taps.size // w.channels))  # branch FIR flops
-    else:
-        useful = 4.0 * n * w.taps.size                       # FIR flops
     algo_bytes = 16.0 * n  # 8 B read + 8 B written per sample
     achieved_gbs = algo_bytes / kernel_s / 1e9
-    if impl == "tc_split" and not w.channels:
+    if impl == "tc_split" and w.captures:
+        roofline = {"bound": "tensor", "achieved": useful / kernel_s / 1e12,
+                    "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                    "frac": useful / kernel_s / 1e12 / pk["bf16_tflops"], "traffic": None,
+                    "note": "useful FIR flops sum 4*N_i*K_i over the captures; the short-tap "
+                            "captures are bound by HBM instead (hbm_achieved_gbs)"}
+        extras["hbm_achieved_gbs"] = achieved_gbs
+        extras["hbm_frac"] = achieved_gbs / pk["hbm_gbs"]
+    elif impl == "tc_split" and not w.channels:
         roofline = {"bound": "tensor", "achieved": useful / kernel_s / 1e12,
                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                     "frac": useful / kernel_s / 1e12 / pk["bf16_tflops"], "traffic": None,
@@ -464,7 +614,7 @@ def run_ours(args) -> None:
         roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"],
                     "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None}
     roofline["peak_source"] = pk["source"]
-    if "plain" in arms and not w.channels:
+    if "plain" in arms and not w.channels and not w.captures:
         sm_mhz = (clocks or {}).get("sm_mhz") or 1900.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         ks = arms["plain"]["kernel_s"]
@@ -491,10 +641,12 @@ def run_ours(args) -> None:
     # End to end through the public host-buffer call, pinned host memory.
     e2e = None
     if rank == 0:
-        xp = torch.from_numpy(w.x).pin_memory()
+        xp = torch.from_numpy(w.x).pin_memory() if not w.captures else None
         b = rfx.Bench(warmup=args.warmup, runs=args.steps)
         lib = rfx.load()
-        if w.channels:
+        if w.captures:
+            e2e = batch_e2e(rfx, w, impl, args, device)
+        elif w.channels:
             zp = torch.empty(rfx.frames(n, w.channels) * w.channels,
                              dtype=torch.complex64).pin_memory()
             rfx._check(lib.rfx_channelize_host(rfx.parse_chan_impl(impl), xp.data_ptr(), n,
@@ -507,15 +659,21 @@ def run_ours(args) -> None:
                                         w.taps.ctypes.data, w.taps.size, 256, yp.data_ptr(),
                                         rfx.ctypes.byref(b)))
             d2h = n * 8
-        step_ms = b.h2d_ms_mean + b.kernel_ms_mean + b.d2h_ms_mean
-        e2e = {"value": n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
-               "h2d_bytes_per_step": n * 8 + w.taps.size * 4, "d2h_bytes_per_step": d2h,
-               "h2d_ms": b.h2d_ms_mean, "kernel_ms": b.kernel_ms_mean, "d2h_ms": b.d2h_ms_mean}
+        if not w.captures:
+            step_ms = b.h2d_ms_mean + b.kernel_ms_mean + b.d2h_ms_mean
+            e2e = {"value": n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
+                   "h2d_bytes_per_step": n * 8 + w.taps.size * 4, "d2h_bytes_per_step": d2h,
+                   "h2d_ms": b.h2d_ms_mean, "kernel_ms": b.kernel_ms_mean,
+                   "d2h_ms": b.d2h_ms_mean}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = (cpu_chan_baseline(w.x, w.taps, w.channels) if w.channels
-               else cpu_fir_baseline(w.x, w.taps))
+        if w.captures:
+            cpu = cpu_batch_baseline(w.captures)
+        elif w.channels:
+            cpu = cpu_chan_baseline(w.x, w.taps, w.channels)
+        else:
+            cpu = cpu_fir_baseline(w.x, w.taps)
 
     fault = rfx.device_fault()
     if fault:
@@ -527,10 +685,7 @@ def run_ours(args) -> None:
             "ms_per_step": prim["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": prim["dtype"],
             "data": "synthetic",
-            "config": {"workload": w.name, "impl": impl, "samples": n,
-                       "taps": int(w.taps.size), "channels": w.channels or None,
-                       "l2": "inputs larger than L2: two 268 MB buffer sets alternate",
-                       "seed": w.meta.get("seed")},
+            "config": config_of(w, impl, n),
             "max_rel_err_vs_f64": prim["max_rel_err_vs_f64"],
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -551,7 +706,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="fir1025", choices=["fir1025", "fir63", "pfb64"])
+    ap.add_argument("--workload", default="fir1025",
+                    choices=["fir1025", "fir63", "pfb64", "pfb1024", "batch256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the 64-channel PFB measured beside the FIR")
