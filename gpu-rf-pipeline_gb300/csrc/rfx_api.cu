@@ -2,6 +2,8 @@
 // plans, host-buffer operations with phase timing, and the fault word readout.
 #include "rfx.h"
 
+#include "api_error.hpp"
+
 #include "chan_plain.cuh"
 #include "chan_tc.cuh"
 #include "fir_plain.cuh"
@@ -127,6 +129,12 @@ int launch_fir(int impl, const void* x, const float* taps, void* y, int64_t n, i
 }
 
 }  // namespace
+
+namespace rfx {
+
+int set_last_error(int status, const char* message) { return fail(status, "%s", message); }
+
+}  // namespace rfx
 
 struct rfx_chan_plan {
     int impl;

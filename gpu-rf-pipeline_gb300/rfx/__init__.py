@@ -60,6 +60,7 @@ SIGNATURES = {
     "rfx_chan_plan_destroy": (_I, [_VP]),
     "rfx_channelize_launch": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _VP]),
     "rfx_channelize_branches": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
+    "rfx_channelize_tc_static": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
     "rfx_fir_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_channelize_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_autotune_fir": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),

@@ -157,6 +157,23 @@ int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps,
 int rfx_channelize_branches(const void* x, const float* taps, void* u, int64_t num_samples,
                             int channels, int num_taps, cudaStream_t stream);
 
+/* The 64-channel tensor-core channelizer (what rfx_channelize_launch computes with an
+ * RFX_CHAN_TC plan, same kernel and results) without a plan and without allocating anything:
+ * its twiddle operand (66,048 bytes) lives in a fixed array of the library's device memory,
+ * shared by every call on the device. For callers that may not allocate device memory after
+ * start-up: a memory budget fixed at initialization, a device allocator owned by another
+ * framework, or no room for the implicit synchronization of cudaMalloc and cudaFree.
+ * The FIRST call on each device builds that operand on `stream` and waits for it
+ * (cudaStreamSynchronize); make it during initialization, before any stream capture. Later
+ * calls only enqueue the kernel. The array is read-only after the first call, so calls may
+ * overlap; concurrent first calls on one device are serialized by a lock.
+ * channels must be 64 (RFX_ERR_CAPACITY otherwise: the array holds that operand only);
+ * num_samples 0 or at least 64 (one frame); taps as for the RFX_CHAN_TC plan.
+ * No counterpart in the project: its channelize_device (src/device_ops.hpp:150-151) takes a
+ * cuFFT plan, which allocates. */
+int rfx_channelize_tc_static(const void* x, const float* taps, void* out, int64_t num_samples,
+                             int num_taps, int channels, cudaStream_t stream);
+
 /* ---- host-buffer operations (timed like the project's Bench) --------------------------- */
 
 /* Phase timings of a host-buffer call, as the project's BenchResult (src/bench.hpp:17-32). */
