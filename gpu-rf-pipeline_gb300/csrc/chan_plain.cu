@@ -5,10 +5,16 @@
 //   z[t][k] = sum_m u[t][m] e^{+2 pi i k m / M}        (cuFFT inverse, unnormalized)
 //
 // The branch sums use the project's arithmetic (src/channelize.cu:35-46): one fused
-// multiply-add per tap, l = m, m + M, ... ascending, stopping at the start of the input, so u is
-// bit-identical to its kernel's. One thread per (frame, branch): consecutive threads read
-// consecutive (descending) samples and consecutive taps, so every load is coalesced; the I/Q
-// pair is one packed f32x2 fused multiply-add.
+// multiply-add per tap, l = m, m + M, ... ascending from +0, skipping the terms before the start
+// of the input, so u is bit-identical to its kernel's. The project runs one thread per (frame,
+// branch), which reads every sample once per tap of its branch (32 times at 32 taps per branch)
+// through the caches. Here a thread owns one branch m and R = 8 consecutive frames: the frames
+// of one branch form a FIR over the decimated sequence s_d = x[dM - m] with taps g_p =
+// h[pM + m], computed with two alternating 8-sample register blocks, so each sample is loaded
+// (R + P - 1) / R times instead of P times. Consecutive threads take consecutive branches, so
+// every sample and tap load of a warp is one coalesced 256-byte row; the I/Q pair is one packed
+// f32x2 fused multiply-add. The first frame groups (where terms fall before the input) and the
+// last (past its end) take a path that tests every term.
 #include "chan_plain.cuh"
 #include "ptx.cuh"
 
@@ -19,43 +25,144 @@ namespace rfx {
 
 namespace {
 constexpr int kBranchThreads = 256;
+constexpr int kR = 8;   // frames per thread
+
+// Taps p0 + q (q < nq) of one branch: acc[i] += g_p s_{t0 + i - p}, with cur[i] = s_{t0 - 8g + i}
+// and nxt[i] = s_{t0 - 8(g+1) + i} for p0 = 8 g. Guarded: only terms whose sample index is >= 0.
+template <bool kGuard>
+__device__ __forceinline__ void taps_block(f32x2 (&acc)[kR], const f32x2 (&cur)[kR],
+                                           const f32x2 (&nxt)[kR], const float* __restrict__ taps,
+                                           int channels, int m, int p0, int nq, long long t0,
+                                           int first_valid_d)
+{
+#pragma unroll
+    for (int q = 0; q < kR; ++q) {
+        if (q < nq) {
+            const float hv = __ldg(taps + static_cast<long long>(p0 + q) * channels + m);
+            const f32x2 h2 = pack2(hv, hv);
+#pragma unroll
+            for (int i = 0; i < kR; ++i) {
+                const f32x2 v = i >= q ? cur[i - q] : nxt[kR + i - q];
+                if (!kGuard || t0 + i - (p0 + q) >= first_valid_d) {
+                    acc[i] = fma2(h2, v, acc[i]);
+                }
+            }
+        }
+    }
 }
 
+template <bool kGuard>
+__device__ __forceinline__ void load_block(f32x2 (&blk)[kR], const float2* __restrict__ x,
+                                           long long n, int channels, int m, long long d0)
+{
+#pragma unroll
+    for (int i = 0; i < kR; ++i) {
+        const long long s = (d0 + i) * channels - m;
+        f32x2 v = 0ull;
+        if (!kGuard || (s >= 0 && s < n)) {
+            const float2 w = __ldg(x + s);
+            v = pack2(w.x, w.y);
+        }
+        blk[i] = v;
+    }
+}
+
+template <bool kGuard>
+__device__ __forceinline__ void branch_frames(f32x2 (&acc)[kR], const float2* __restrict__ x,
+                                              const float* __restrict__ taps, long long n,
+                                              int channels, int m, int P, long long t0)
+{
+    const int first_valid_d = m > 0 ? 1 : 0;   // x[dM - m] >= 0 from this d on
+    const int groups = P / kR;
+    const int rem = P - groups * kR;
+    f32x2 a[kR];
+    f32x2 b[kR];
+    load_block<kGuard>(a, x, n, channels, m, t0);
+    int g = 0;
+    for (; g + 2 <= groups; g += 2) {
+        load_block<kGuard>(b, x, n, channels, m, t0 - kR * (g + 1));
+        taps_block<kGuard>(acc, a, b, taps, channels, m, kR * g, kR, t0, first_valid_d);
+        load_block<kGuard>(a, x, n, channels, m, t0 - kR * (g + 2));
+        taps_block<kGuard>(acc, b, a, taps, channels, m, kR * (g + 1), kR, t0, first_valid_d);
+    }
+    if (g < groups) {
+        load_block<kGuard>(b, x, n, channels, m, t0 - kR * (g + 1));
+        taps_block<kGuard>(acc, a, b, taps, channels, m, kR * g, kR, t0, first_valid_d);
+        if (rem > 0) {
+            load_block<kGuard>(a, x, n, channels, m, t0 - kR * (g + 2));
+            taps_block<kGuard>(acc, b, a, taps, channels, m, kR * (g + 1), rem, t0,
+                               first_valid_d);
+        }
+    } else if (rem > 0) {
+        load_block<kGuard>(b, x, n, channels, m, t0 - kR * (g + 1));
+        taps_block<kGuard>(acc, a, b, taps, channels, m, kR * g, rem, t0, first_valid_d);
+    }
+}
+}  // namespace
+
+// Block: `width` consecutive branches x (256 / width) frame groups of kR frames. Groups with
+// t0 < guard_frames or reaching past the last frame test every load and term.
 __global__ void __launch_bounds__(kBranchThreads)
 chan_branch_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
-                   float2* __restrict__ u, long long frames, int channels, int num_taps)
+                   float2* __restrict__ u, long long n, long long frames, int channels,
+                   int num_taps, int width, int guard_frames)
 {
-    const long long idx = static_cast<long long>(blockIdx.x) * kBranchThreads + threadIdx.x;
-    if (idx >= frames * channels) {
+    const int m = static_cast<int>(blockIdx.y) * width + static_cast<int>(threadIdx.x) % width;
+    const long long group = static_cast<long long>(blockIdx.x) * (kBranchThreads / width) +
+                            threadIdx.x / width;
+    const long long t0 = group * kR;
+    if (m >= channels || t0 >= frames) {
         return;
     }
-    const long long t = idx / channels;
-    const int m = static_cast<int>(idx - t * channels);
-    const long long newest = t * channels;  // index of x[tM]
-    f32x2 acc = 0ull;
-    for (int l = m; l < num_taps; l += channels) {
-        const long long s = newest - l;
-        if (s < 0) {
-            break;
-        }
-        const float h = __ldg(taps + l);
-        const float2 v = __ldg(x + s);
-        acc = fma2(pack2(h, h), pack2(v.x, v.y), acc);
+    // Taps of branch m: l = pM + m < num_taps.
+    const int P = m < num_taps ? (num_taps - m + channels - 1) / channels : 0;
+    f32x2 acc[kR];
+#pragma unroll
+    for (int i = 0; i < kR; ++i) {
+        acc[i] = 0ull;
     }
-    u[idx] = unpack2(acc);
+    if (t0 < guard_frames || t0 + kR > frames) {
+        branch_frames<true>(acc, x, taps, n, channels, m, P, t0);
+    } else {
+        branch_frames<false>(acc, x, taps, n, channels, m, P, t0);
+    }
+#pragma unroll
+    for (int i = 0; i < kR; ++i) {
+        if (t0 + i < frames) {
+            u[(t0 + i) * channels + m] = unpack2(acc[i]);
+        }
+    }
 }
 
 cudaError_t chan_branch_launch(const void* x, const float* taps, void* u, long long frames,
                                int channels, int num_taps, cudaStream_t stream)
 {
-    const long long total = frames * channels;
-    if (total == 0) {
+    if (frames == 0 || channels < 1) {
         return cudaSuccess;
     }
-    const long long grid = (total + kBranchThreads - 1) / kBranchThreads;
-    chan_branch_kernel<<<static_cast<unsigned>(grid), kBranchThreads, 0, stream>>>(
-        static_cast<const float2*>(x), taps, static_cast<float2*>(u), frames, channels,
-        num_taps);
+    // The newest sample any frame reads is the last frame's x[(frames - 1) M], which lies in the
+    // input: loads are bounded by that index.
+    const long long n = (frames - 1) * static_cast<long long>(channels) + 1;
+    // Branches per block: the power of two >= channels, between one warp and the whole block.
+    int w = 32;
+    while (w < channels && w < kBranchThreads) {
+        w *= 2;
+    }
+    const long long groups = (frames + kR - 1) / kR;
+    const int per_block = kBranchThreads / w;
+    const long long gx = (groups + per_block - 1) / per_block;
+    const long long gy = (channels + w - 1) / w;
+    if (gx > 0x7FFFFFFFLL || gy > 65535) {
+        return cudaErrorInvalidConfiguration;
+    }
+    // Frame groups before this one load samples before the input (the lowest sample block a
+    // group loads starts kR * ceil(P / kR) frames back): they take the tested path.
+    const int max_p = (num_taps + channels - 1) / channels;
+    const int guard_frames = kR * ((max_p + kR - 1) / kR + 1);
+    chan_branch_kernel<<<dim3(static_cast<unsigned>(gx), static_cast<unsigned>(gy)),
+                         kBranchThreads, 0, stream>>>(
+        static_cast<const float2*>(x), taps, static_cast<float2*>(u), n, frames, channels,
+        num_taps, w, guard_frames);
     return cudaGetLastError();
 }
 

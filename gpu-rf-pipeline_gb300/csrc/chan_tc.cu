@@ -8,13 +8,15 @@
 //     input) in two half-windows: frames [t0 + 64 h, +64) need rows t0 + 64 h - P .. +63
 //     (P = taps per branch), i.e. 64 + P rows per half, double-buffered so the next tile's
 //     samples stream in while this tile is finished.
-//  2. Branch sums on CUDA cores, FP32, from shared memory: a thread owns branches 2j, 2j+1 for
-//     4 consecutive frames of each half. For one branch the frames form a FIR over the
-//     decimated sequence s_d = x[(t0 + d) M - m] with taps g_p = h[pM + m]; two alternating
-//     4-sample register blocks, taps in ascending p, one packed f32x2 fused multiply-add per
-//     tap — the arithmetic order of the project's branch kernel.
+//  2. Branch sums on CUDA cores, FP32, from shared memory: lane l owns branches (64 - l) % 64
+//     and 32 - l (window columns l and 32 + l, so a warp's loads are conflict-free) for 4
+//     consecutive frames of each half. For one branch the frames form a FIR over the
+//     decimated sequence s_d = x[(t0 + d) M - m] with taps g_p = h[pM + m] (from shared memory
+//     up to 26 taps per branch, else the L1 cache); two alternating 4-sample register blocks,
+//     taps in ascending p, one packed f32x2 fused multiply-add per tap.
 //  3. The tile's largest |u| sets a power-of-two scale; u' = u_hi + u_lo in FP16 is written as
-//     the GEMM's A operand (rows = frames, K = [Re u[0..63], Im u[0..63]]).
+//     the GEMM's A operand (rows = frames, K = [Re u, Im u] in the lanes' branch order:
+//     K index 2l -> branch (64 - l) % 64, 2l + 1 -> 32 - l; W's rows follow the same order).
 //  4. The DFT as a real GEMM: [Re z, Im z] (128 x 128) = A (128 x 128) W, with
 //     W = [[cos, sin], [-sin, cos]](2 pi k m / M) built in FP64 on the GPU (rfx_chan_plan_create)
 //     and split hi/lo once; three split products per K-step on tcgen05 (M=128, N=128, K=16).
@@ -23,9 +25,10 @@
 //     (2 tiles x 2 x 128 columns) so the MMAs of tile k + 1 run while tile k is drained.
 //  5. Scale back by 2^-(eu + ew) and store each frame's 64 channels.
 //
-// Roles (544 threads): warps 0-15 compute branch sums, write operands and drain the
+// Roles (576 threads): warps 0-15 compute branch sums, write operands and drain the
 // accumulators (warp w: TMEM lane quarter w % 4 = frames 32 (w % 4) .. +31, channels
-// 16 (w / 4) .. +15); warp 16 owns tensor memory and issues the MMAs. The loop runs the branch
+// 16 (w / 4) .. +15); warp 16 owns tensor memory and issues the MMAs; warp 17 refills the
+// half-windows as the workers release them. The loop runs the branch
 // sums of tile k + 1 and stages its operand before draining tile k, so the MMAs of tile k hide
 // behind the branch sums and those of tile k + 1 behind the drain. Every wait is a bounded
 // mbarrier wait.
@@ -51,7 +54,8 @@ constexpr int kHalf = kFrames / 2;     // frames per half-window
 constexpr int kR = 4;                  // frames per thread per half
 constexpr int kWorkerWarps = 16;
 constexpr int kMmaWarp = 16;
-constexpr int kThreads = 17 * 32;
+constexpr int kTmaWarp = 17;
+constexpr int kThreads = 18 * 32;
 constexpr int kParts = 2;              // TMEM accumulators per tile, 4 K-steps each
 constexpr uint32_t kTmemCols = 512;    // 2 tiles x kParts x kK
 constexpr uint32_t kPlane = kFrames * 16 + 16;  // bytes per 8-element K plane (+16: banks)
@@ -59,12 +63,22 @@ constexpr uint32_t kSplit = (kK / 8) * kPlane;  // one split of one operand
 constexpr uint32_t kIdesc = idesc_f16(kFrames, kK);
 constexpr int kWExp = 14;              // W' = 2^14 W, |W| <= 1
 constexpr int kMaxPerBranch = 32;      // taps per branch the kernel takes
+constexpr int kSmemTapsMax = 26;       // taps per branch up to which the taps sit in smem too
+
+// The GEMM's K index of Re u (k < 64; Im u at 64 + k) -> branch. Lane l owns K indices 2l and
+// 2l + 1, i.e. branches (64 - l) % 64 and 32 - l, whose window columns (64 - m) % 64 are l and
+// 32 + l: a warp's window loads read 32 consecutive 8-byte columns (no bank conflicts).
+__host__ __device__ inline int k_to_branch(int k)
+{
+    const int l = k >> 1;
+    return (k & 1) ? 32 - l : (64 - l) & 63;
+}
 
 struct Layout {
     int P;                 // taps per branch
     int wrows;             // rows per half-window: kHalf + P
     uint32_t win;          // bytes per half-window
-    uint32_t w_hi, w_lo, a_hi, a_lo, win0, bytes;
+    uint32_t w_hi, w_lo, a_hi, a_lo, win0, taps, bytes;
 };
 
 __host__ __device__ inline Layout chan_layout(int num_taps)
@@ -78,7 +92,8 @@ __host__ __device__ inline Layout chan_layout(int num_taps)
     l.a_hi = l.w_lo + kSplit;
     l.a_lo = l.a_hi + kSplit;
     l.win0 = l.a_lo + kSplit;                     // two half-window buffers
-    l.bytes = l.win0 + 2u * l.win;
+    l.taps = l.win0 + 2u * l.win;                 // taps[p][slot], slot = the lane's column
+    l.bytes = l.taps + (l.P <= kSmemTapsMax ? static_cast<uint32_t>(l.P) * kM * 4u : 0u);
     return l;
 }
 
@@ -97,16 +112,25 @@ struct Ctrl {
 };
 
 // Taps p0 + q (q < nq) of one branch: acc[i] += g_p s_{i - p} with cur = S_g, nxt = S_{g+1},
-// S_g[i] = s_{-4g + i}. The taps come through the L1 cache: a warp reads 64 consecutive taps.
+// S_g[i] = s_{-4g + i}. The taps come from shared memory (tap_s: the branch's column of the
+// taps[p][slot] table, 256 bytes per p) or, for the longest filters, through the L1 cache.
+template <bool kTapsSmem>
 __device__ __forceinline__ void branch_group(f32x2 (&acc)[kR], const f32x2 (&cur)[kR],
                                              const f32x2 (&nxt)[kR], const float* __restrict__ taps,
-                                             int m, int p0, int nq, int num_taps)
+                                             uint32_t tap_s, int m, int p0, int nq, int num_taps)
 {
 #pragma unroll
     for (int q = 0; q < kR; ++q) {
         if (q < nq) {
-            const int l = (p0 + q) * kM + m;
-            const float hv = l < num_taps ? __ldg(taps + l) : 0.0f;
+            float hv;
+            if (kTapsSmem) {
+                asm volatile("ld.shared.f32 %0, [%1];"
+                             : "=f"(hv)
+                             : "r"(tap_s + static_cast<uint32_t>(p0 + q) * (kM * 4u)));
+            } else {
+                const int l = (p0 + q) * kM + m;
+                hv = l < num_taps ? __ldg(taps + l) : 0.0f;
+            }
             const f32x2 h2 = pack2(hv, hv);
 #pragma unroll
             for (int i = 0; i < kR; ++i) {
@@ -118,6 +142,7 @@ __device__ __forceinline__ void branch_group(f32x2 (&acc)[kR], const f32x2 (&cur
 
 }  // namespace
 
+template <bool kTapsSmem>
 __global__ void __launch_bounds__(kThreads, 1)
 chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict__ x,
                const float* __restrict__ taps, const uint16_t* __restrict__ w_img,
@@ -178,6 +203,17 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
         for (uint32_t i = threadIdx.x; i < 2 * kSplit / 16; i += kThreads) {
             dst[i] = __ldg(src + i);
         }
+        if (kTapsSmem) {
+            // taps[p][slot]: slot l < 32 holds branch (64 - l) % 64, slot 32 + l branch 32 - l.
+            float* tp = reinterpret_cast<float*>(smem + lay.taps);
+            for (int i = threadIdx.x; i < P * kM; i += kThreads) {
+                const int pp = i / kM;
+                const int slot = i - pp * kM;
+                const int m = slot < 32 ? (kM - slot) & (kM - 1) : 32 - (slot - 32);
+                const int l = pp * kM + m;
+                tp[i] = l < num_taps ? __ldg(taps + l) : 0.0f;
+            }
+        }
     }
     fence_proxy_async_smem();
     fence_before();
@@ -187,7 +223,9 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
 
     if (warp < kWorkerWarps) {
         const int wtid = threadIdx.x;
-        const int pair = wtid & 31;                      // branches 2 pair, 2 pair + 1
+        const int pair = wtid & 31;                      // K indices 2 pair, 2 pair + 1
+        const int m_a = k_to_branch(2 * pair);           // their branches
+        const int m_b = k_to_branch(2 * pair + 1);
         const int fgroup = wtid >> 5;                    // frames 4 fgroup .. +3 of each half
         const int quarter = warp & 3;
         const int slice = warp >> 2;                     // channels 16 slice .. +15
@@ -207,7 +245,7 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             }
         };
         // u[t + i][m] for i < 4 from one half-window.
-        auto branch_sums = [&](f32x2 (&acc)[kR], uint32_t buf, int m) {
+        auto branch_sums = [&](f32x2 (&acc)[kR], uint32_t buf, int m, uint32_t tap_s) {
 #pragma unroll
             for (int i = 0; i < kR; ++i) {
                 acc[i] = 0ull;
@@ -224,20 +262,20 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             int g = 0;
             for (; g + 2 <= groups; g += 2) {
                 load_block(b, base, -kR * (g + 1));
-                branch_group(acc, a, b, taps, m, kR * g, kR, num_taps);
+                branch_group<kTapsSmem>(acc, a, b, taps, tap_s, m, kR * g, kR, num_taps);
                 load_block(a, base, -kR * (g + 2));
-                branch_group(acc, b, a, taps, m, kR * (g + 1), kR, num_taps);
+                branch_group<kTapsSmem>(acc, b, a, taps, tap_s, m, kR * (g + 1), kR, num_taps);
             }
             if (g < groups) {
                 load_block(b, base, -kR * (g + 1));
-                branch_group(acc, a, b, taps, m, kR * g, kR, num_taps);
+                branch_group<kTapsSmem>(acc, a, b, taps, tap_s, m, kR * g, kR, num_taps);
                 if (rem > 0) {
                     load_block(a, base, -kR * (g + 2));
-                    branch_group(acc, b, a, taps, m, kR * (g + 1), rem, num_taps);
+                    branch_group<kTapsSmem>(acc, b, a, taps, tap_s, m, kR * (g + 1), rem, num_taps);
                 }
             } else if (rem > 0) {
                 load_block(b, base, -kR * (g + 1));
-                branch_group(acc, a, b, taps, m, kR * g, rem, num_taps);
+                branch_group<kTapsSmem>(acc, a, b, taps, tap_s, m, kR * g, rem, num_taps);
             }
         };
         // The input's last, partial frame lies outside the tensor map (its copy reads zeros):
@@ -255,7 +293,9 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             fence_proxy_async_smem();
             asm volatile("bar.sync 1, %0;" ::"n"(kWorkerWarps * 32) : "memory");
         };
-        // Branch sums of tile k for this thread: u0 (branch 2 pair), u1 (+1), by half.
+        const uint32_t tap_a = sbase + lay.taps + static_cast<uint32_t>(pair) * 4u;
+        const uint32_t tap_b = tap_a + 32u * 4u;
+        // Branch sums of tile k for this thread: u0 (branch m_a), u1 (m_b), by half.
         f32x2 u0[2][kR];
         f32x2 u1[2][kR];
         auto compute = [&](int k) -> bool {
@@ -268,21 +308,11 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
                 }
                 const uint32_t buf = sbase + lay.win0 + static_cast<uint32_t>(h) * lay.win;
                 patch_partial_row(buf, row0(k, h));
-                branch_sums(u0[h], buf, 2 * pair);
-                branch_sums(u1[h], buf, 2 * pair + 1);
+                branch_sums(u0[h], buf, m_a, tap_a);
+                branch_sums(u1[h], buf, m_b, tap_b);
                 __syncwarp();
                 if (lane == 0) {
                     mbar_arrive(smem_u32(&ctl.win_empty[h]));
-                }
-                // Refill buffer h with tile k + 1 once every warp has read it.
-                if (wtid == 0 && k + 1 < my_tiles) {
-                    if (!mbar_wait_bounded(smem_u32(&ctl.win_empty[h]), k & 1, fault,
-                                           kFaultStageEmpty, abort)) {
-                        return false;
-                    }
-                    const uint32_t bar = smem_u32(&ctl.win_full[h]);
-                    mbar_arrive_expect_tx(bar, lay.win);
-                    tma_load_2d(buf, &xmap, 0, static_cast<int>(row0(k + 1, h)), bar);
                 }
             }
             return true;
@@ -405,6 +435,23 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
                 }
             }
         }
+    } else if (warp == kTmaWarp) {
+        // Refills half-window h with tile k once every worker warp has read tile k - 1's.
+        if (lane == 0) {
+            for (int k = 1; k < my_tiles && !*abort; ++k) {
+                for (int h = 0; h < 2; ++h) {
+                    if (!mbar_wait_bounded(smem_u32(&ctl.win_empty[h]), (k - 1) & 1, fault,
+                                           kFaultStageEmpty, abort)) {
+                        k = my_tiles;
+                        break;
+                    }
+                    const uint32_t bar = smem_u32(&ctl.win_full[h]);
+                    mbar_arrive_expect_tx(bar, lay.win);
+                    tma_load_2d(sbase + lay.win0 + static_cast<uint32_t>(h) * lay.win, &xmap, 0,
+                                static_cast<int>(row0(k, h)), bar);
+                }
+            }
+        }
     } else if (lane == 0) {
         const uint32_t w_hi = sbase + lay.w_hi;
         const uint32_t w_lo = sbase + lay.w_lo;
@@ -462,7 +509,7 @@ __global__ void chan_twiddle_kernel(uint16_t* img)
     const int nrow = idx / kK;
     const int kcol = idx % kK;
     const int ch = nrow % kM;
-    const int br = kcol % kM;
+    const int br = k_to_branch(kcol % kM);
     double s, c;
     sincospi(2.0 * static_cast<double>((ch * br) % kM) / kM, &s, &c);
     double v;
@@ -498,16 +545,10 @@ cudaError_t chan_tc_build_twiddles(void* img, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddles, void* z,
-                           long long n, int num_taps, cudaStream_t stream)
+template <bool kTapsSmem>
+static cudaError_t launch_chan(const void* x, const float* taps, const void* twiddles, void* z,
+                               long long n, long long frames, int num_taps, cudaStream_t stream)
 {
-    const long long frames = (n + kM - 1) / kM;
-    if (frames == 0) {
-        return cudaSuccess;
-    }
-    if (n < kM) {
-        return cudaErrorInvalidValue;  // the caller routes inputs shorter than a frame elsewhere
-    }
     const Layout lay = chan_layout(num_taps);
     int device = 0;
     int sms = 0;
@@ -519,13 +560,14 @@ cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddle
     }
     const uint32_t bytes = lay.bytes > 120u * 1024u ? lay.bytes : 120u * 1024u;
     cudaFuncAttributes attr{};
-    if ((err = cudaFuncGetAttributes(&attr, chan_tc_kernel)) != cudaSuccess) {
+    if ((err = cudaFuncGetAttributes(&attr, chan_tc_kernel<kTapsSmem>)) != cudaSuccess) {
         return err;
     }
     if (attr.maxThreadsPerBlock < kThreads) {
         return cudaErrorLaunchOutOfResources;
     }
-    err = cudaFuncSetAttribute(chan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    err = cudaFuncSetAttribute(chan_tc_kernel<kTapsSmem>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(bytes));
     if (err != cudaSuccess) {
         return err;
@@ -539,10 +581,26 @@ cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddle
     }
     const int tiles = static_cast<int>((frames + kFrames - 1) / kFrames);
     const int grid = tiles < sms ? tiles : sms;
-    chan_tc_kernel<<<grid, kThreads, bytes, stream>>>(
+    chan_tc_kernel<kTapsSmem><<<grid, kThreads, bytes, stream>>>(
         map, static_cast<const float2*>(x), taps, static_cast<const uint16_t*>(twiddles),
         static_cast<float2*>(z), n, frames, num_taps, tiles);
     return cudaGetLastError();
+}
+
+cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddles, void* z,
+                           long long n, int num_taps, cudaStream_t stream)
+{
+    const long long frames = (n + kM - 1) / kM;
+    if (frames == 0) {
+        return cudaSuccess;
+    }
+    if (n < kM) {
+        return cudaErrorInvalidValue;  // the caller routes inputs shorter than a frame elsewhere
+    }
+    if (chan_layout(num_taps).P <= kSmemTapsMax) {
+        return launch_chan<true>(x, taps, twiddles, z, n, frames, num_taps, stream);
+    }
+    return launch_chan<false>(x, taps, twiddles, z, n, frames, num_taps, stream);
 }
 
 cudaError_t chan_tc_take_fault(unsigned int* code)

@@ -102,3 +102,18 @@ def test_plan_frame_count_is_checked() -> None:
 def test_bad_channel_count_is_an_error() -> None:
     with pytest.raises(rfx.RfxError):
         rfx.ChanPlan(0, 100)
+
+
+@pytest.mark.parametrize("n,k,m", [(100, 37, 4), (64, 16, 16), (7, 63, 4), (33, 1, 1),
+                                   (50, 24, 8), (70001, 1024, 64), (1 << 16, 4096, 1024),
+                                   (5 * 1024 + 3, 32768, 1024), (12345, 100, 12),
+                                   (3000, 640, 160), (1 << 18, 1024, 64), (999, 2000, 3)])
+def test_branch_sums_are_bit_exact(n: int, k: int, m: int) -> None:
+    # rfx_channelize_branches against the reference's float32 branch arithmetic, bit for bit.
+    rng = np.random.default_rng(7 * n + k + m)
+    x = signals.to_cf32(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    h = (rng.standard_normal(k) / np.sqrt(k)).astype(np.float32)
+    u = rfx.channelize_branches(dev(x), dev(h), m)
+    torch.cuda.synchronize()
+    want = orc.channelize_branch_f32_seq(x, h, m)
+    assert np.array_equal(u.cpu().numpy().view(np.uint32), want.view(np.uint32))
