@@ -253,7 +253,8 @@ class Arm:
         else:
             self.outs = [torch.empty_like(self.xs[0]) for _ in range(2)]
             self.launches_per_step = 1
-        self.dtype = "f16x3->f32" if impl == "tc_split" else "f32"
+        uses_tc = impl == "tc_split" or (impl == "auto" and auto_picks_tc(w.taps.size, n))
+        self.dtype = "f16x3->f32" if uses_tc else "f32"
 
     def launch(self, i: int) -> None:
         if self.w.channels:
@@ -314,9 +315,17 @@ class BatchArm:
                                          hd.numel(), 0)
         self.impl_v = rfx.parse_fir_impl(impl)
         count = len(self.caps)
-        self.launches_per_step = (-(-count // 192) if impl == "tc_split"
-                                  else sum(1 for x, _ in w.captures if x.size))
-        self.dtype = "f16x3->f32" if impl == "tc_split" else "f32"
+        sizes = [(int(x.size), int(h.size)) for x, h in w.captures if x.size]
+        if impl == "tc_split":
+            self.launches_per_step = -(-count // 192)
+            self.dtype = "f16x3->f32"
+        elif impl == "auto":
+            tc = sum(1 for m, k in sizes if auto_picks_tc(k, m))
+            self.launches_per_step = -(-(len(sizes) - tc) // 256) + -(-tc // 192)
+            self.dtype = "f16x3->f32 (taps >= 160) + f32"
+        else:
+            self.launches_per_step = len(sizes)
+            self.dtype = "f32"
 
     def launch(self, i: int) -> None:
         self.rfx._check(self.rfx.load().rfx_fir_batch_launch(self.impl_v, self.arr, len(self.caps),
@@ -339,6 +348,11 @@ class BatchArm:
 
     def release(self) -> None:
         self.caps = self.arr = self.X = self.Y = None
+
+
+def auto_picks_tc(num_taps: int, n: int) -> bool:
+    """The library's built-in auto rule (tuning.cu): tensor core from 160 taps and 2^16 samples."""
+    return num_taps >= 160 and n >= (1 << 16)
 
 
 def make_arm(rfx, w, impl: str, device):
@@ -582,8 +596,10 @@ def run_ours(args) -> None:
             useful = 4.0 * n * (-(-w.taps.size // w.channels))  # branch FIR flops
         else:
             useful = 4.0 * n * w.taps.size                       # FIR flops
-    arms, clocks = measure_arms(rfx, w, ["tc_split", "plain"], args, dist, device,
-                                sample_clocks=True)
+    # auto first where it is not simply the tensor-core form: it is the arm a user runs.
+    order = (["auto", "tc_split", "plain"] if w.captures or (not w.channels and w.taps.size < 160)
+             else ["tc_split", "plain"])
+    arms, clocks = measure_arms(rfx, w, order, args, dist, device, sample_clocks=True)
     impl = next(iter(arms))
     prim = arms[impl]
     value = prim["msamples_s"]

@@ -228,6 +228,28 @@ fir_plain_batched_kernel(PlainBatch batch, const float* __restrict__ taps, int n
                    n, num_taps, blockIdx.x, smem);
 }
 
+// Captures with their own taps: block b takes tile b - tile0[c] of the capture c whose tiles
+// contain it (same arithmetic per capture as fir_plain_kernel, so the same bits).
+__global__ void __launch_bounds__(kThreads, 3)
+fir_plain_caps_kernel(const __grid_constant__ PlainCaps caps)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int block = static_cast<int>(blockIdx.x);
+    int lo = 0;
+    int hi = caps.count;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (caps.tile0[mid] <= block) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    fir_plain_tile(static_cast<const float2*>(caps.x[lo]), caps.taps[lo],
+                   static_cast<float2*>(caps.y[lo]), caps.num_samples[lo], caps.num_taps[lo],
+                   block - caps.tile0[lo], smem);
+}
+
 size_t fir_plain_smem_bytes(int num_taps) { return plain_layout(num_taps).bytes; }
 
 static cudaError_t ensure_smem_attr(const void* fn, size_t bytes)
@@ -285,6 +307,26 @@ cudaError_t fir_plain_batched_launch(const PlainBatch& batch, int count, const f
     }
     const dim3 grid(static_cast<unsigned>((longest + kTile - 1) / kTile), count);
     fir_plain_batched_kernel<<<grid, kThreads, bytes, stream>>>(batch, taps, num_taps);
+    return cudaGetLastError();
+}
+
+cudaError_t fir_plain_caps_launch(const PlainCaps& caps, cudaStream_t stream)
+{
+    const int tiles = caps.tile0[caps.count];
+    if (caps.count == 0 || tiles == 0) {
+        return cudaSuccess;
+    }
+    int kmax = 1;
+    for (int c = 0; c < caps.count; ++c) {
+        kmax = caps.num_taps[c] > kmax ? caps.num_taps[c] : kmax;
+    }
+    const size_t bytes = fir_plain_smem_bytes(kmax);
+    cudaError_t err =
+        ensure_smem_attr(reinterpret_cast<const void*>(fir_plain_caps_kernel), bytes);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    fir_plain_caps_kernel<<<static_cast<unsigned>(tiles), kThreads, bytes, stream>>>(caps);
     return cudaGetLastError();
 }
 

@@ -19,11 +19,26 @@ struct PlainBatch {
     long long num_samples[kPlainBatchMax];
 };
 
+// Captures with their own taps, one launch for all: blocks take the captures' tiles in order
+// (tile0[c] = first block of capture c). Passed by value as one kernel argument.
+constexpr int kPlainCapsMax = 256;
+struct PlainCaps {
+    const void* x[kPlainCapsMax];
+    void* y[kPlainCapsMax];
+    const float* taps[kPlainCapsMax];
+    long long num_samples[kPlainCapsMax];
+    int num_taps[kPlainCapsMax];
+    int tile0[kPlainCapsMax + 1];
+    int count;
+};
+
 size_t fir_plain_smem_bytes(int num_taps);
 cudaError_t fir_plain_launch(const void* x, const float* taps, void* y, long long n,
                              int num_taps, cudaStream_t stream);
 cudaError_t fir_plain_batched_launch(const PlainBatch& batch, int count, const float* taps,
                                      int num_taps, cudaStream_t stream);
+// Up to kPlainCapsMax captures (non-empty), each with its own taps, in one launch.
+cudaError_t fir_plain_caps_launch(const PlainCaps& caps, cudaStream_t stream);
 cudaError_t fir_plain_take_fault(unsigned int* code);
 
 }  // namespace rfx

@@ -43,11 +43,14 @@
 #include "fir_tc.cuh"
 #include "fir_plain.cuh"
 #include "fir_tc2.cuh"
+#include "tuning.hpp"
 #include "tc_common.cuh"
 #include "tmap.hpp"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <vector>
 
 namespace rfx {
 
@@ -788,8 +791,52 @@ cudaError_t fir_tc_take_fault(unsigned int* code)
 cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
                              cudaStream_t stream)
 {
-    if (impl == RFX_FIR_TC || impl == RFX_FIR_AUTO) {
+    if (impl == RFX_FIR_TC) {
         return fir_batch_tc_launch(captures, count, stream);
+    }
+    if (impl == RFX_FIR_AUTO) {
+        // Each capture where the tuned rule puts it: the tensor-core captures in one persistent
+        // launch, the others in one plain launch per 256 captures.
+        std::vector<rfx_fir_capture> tc;
+        PlainCaps* plain = new PlainCaps{};
+        cudaError_t err = cudaSuccess;
+        auto flush = [&]() {
+            if (plain->count > 0 && err == cudaSuccess) {
+                err = fir_plain_caps_launch(*plain, stream);
+            }
+            plain->count = 0;
+            plain->tile0[0] = 0;
+        };
+        for (int c = 0; c < count && err == cudaSuccess; ++c) {
+            const rfx_fir_capture& cap = captures[c];
+            if (cap.num_samples == 0) {
+                continue;
+            }
+            if (tuned_fir_impl(cap.num_taps, cap.num_samples) == RFX_FIR_TC) {
+                tc.push_back(cap);
+                continue;
+            }
+            const int i = plain->count;
+            plain->x[i] = cap.x;
+            plain->y[i] = cap.y;
+            plain->taps[i] = cap.taps;
+            plain->num_samples[i] = cap.num_samples;
+            plain->num_taps[i] = cap.num_taps;
+            plain->tile0[i + 1] = plain->tile0[i] + static_cast<int>((cap.num_samples +
+                                                                       kPlainTileOutputs - 1) /
+                                                                      kPlainTileOutputs);
+            plain->count = i + 1;
+            if (plain->count == kPlainCapsMax) {
+                flush();
+            }
+        }
+        flush();
+        delete plain;
+        if (err != cudaSuccess) {
+            return err;
+        }
+        return tc.empty() ? cudaSuccess
+                          : fir_batch_tc_launch(tc.data(), static_cast<int>(tc.size()), stream);
     }
     // The plain kernel: one launch per capture, as the project runs a batch.
     for (int c = 0; c < count; ++c) {

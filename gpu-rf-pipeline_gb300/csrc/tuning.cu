@@ -5,6 +5,7 @@
 #include "rfx.h"
 #include "tuning.hpp"
 #include "fir_plain.cuh"
+#include "fir_tc.cuh"
 
 #include <cuda_runtime.h>
 
@@ -53,16 +54,21 @@ bool lookup(int num_taps, long long n, Entry* out)
 
 }  // namespace
 
-// Built-in rule before tuning: the tensor-core form once it exists and the filter is long
-// enough for FP32 FMA throughput to dominate; the plain kernel otherwise.
+// Built-in rule before tuning: the tensor-core form once the filter is long enough for FP32
+// FMA throughput to bound the plain kernel (measured on GB300: plain is HBM-bound and faster up
+// to about 130 taps, the tensor-core form from about 250) and the input fills the GPU; the
+// plain kernel otherwise.
 int tuned_fir_impl(int num_taps, long long n)
 {
     Entry e;
     if (lookup(num_taps, n, &e)) {
         return e.impl;
     }
-    (void)num_taps;
-    return RFX_FIR_PLAIN;
+    constexpr int kTcMinTaps = 160;
+    constexpr long long kTcMinSamples = 1LL << 16;
+    return num_taps >= kTcMinTaps && n >= kTcMinSamples && fir_tc_supported(num_taps)
+               ? RFX_FIR_TC
+               : RFX_FIR_PLAIN;
 }
 
 TcConfig tuned_fir_tc_config(int num_taps, long long n)

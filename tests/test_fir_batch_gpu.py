@@ -118,3 +118,24 @@ def test_batch_workload_shape() -> None:
     dev = to_dev(caps)
     rfx.fir_batch(dev, impl="tc_split")
     check(caps, dev, exact=False)
+
+
+def test_auto_batch_routes_short_filters_to_the_exact_plain_kernel() -> None:
+    # auto: filters under 160 taps run the plain FP32 kernel (one launch for all of them), so
+    # their outputs are bit-exact; the longer ones go to the tensor-core launch (2e-6).
+    rng = np.random.default_rng(46)
+    caps = []
+    for n, k in [(70000, 31), (3000, 63), (1 << 17, 127), (200000, 1025), (5, 63), (4096, 2),
+                 (1 << 16, 255), (2305, 159), (90001, 160)]:
+        x = signals.to_cf32(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+        h = (rng.standard_normal(k) / np.sqrt(k)).astype(np.float32)
+        caps.append((x, h))
+    dev = to_dev(caps)
+    rfx.fir_batch(dev, impl="auto")
+    torch.cuda.synchronize()
+    for (x, h), (_, y, _) in zip(caps, dev):
+        got = y.cpu().numpy()
+        if h.size < 160 or x.size < (1 << 16):
+            assert np.array_equal(got.view(np.uint32), orc.fir_f32_seq(x, h).view(np.uint32))
+        else:
+            assert orc.normwise_error(got, orc.fir_fast(x, h)) <= TC_NORMWISE
