@@ -14,8 +14,11 @@ taps), pfb1024 (1024-channel channelizer, 2^26 samples, 32768 taps), batch256 (2
 Timing: W untimed steps, then exactly K steps between a barrier + device synchronize on both
 sides, measured with CUDA events on the launching stream; max over ranks. Two input/output
 buffer pairs alternate, so each step touches 536 MB (more than the 129 MB L2) and nothing is
-served from L2 across steps. `value` = all ranks' samples / time; `e2e` = the same metric
-through rfx_fir_host (pinned host buffers, upload + compute + download per step).
+served from L2 across steps. `value` = all ranks' samples / time; `e2e` = the same metric from
+host buffers through the library's host-facing calls: the FIRs through rfx_fir_stream (the
+project's streaming path: pinned capture, chunks whose upload, kernel and download overlap),
+the channelizers through rfx_channelize_host (upload + compute + download), the batch as one
+upload, the batch launch and one download per step.
 
 --impl reference: the oracle's float64 restatement of the project's tools/reference.py FIR,
 threaded over every host core, on a bounded sample of the same workload (rank 0 only).
@@ -480,6 +483,45 @@ def config_of(w, impl: str, n: int) -> dict:
             "seed": w.meta.get("seed")}
 
 
+STREAM_CHUNK = 1 << 21
+STREAM_DEPTH = 4
+
+
+def fir_stream_e2e(rfx, w, impl: str, args) -> dict:
+    """The FIR end to end through rfx_fir_stream (the project's streaming path): the capture
+    in pinned host memory, chunks of 2^21 samples through a ring of four CUDA streams, upload,
+    kernel and download of different chunks overlapping; each pass is timed by the library from
+    the first chunk to the last output on the host. Bytes moved: every chunk with its history."""
+    import torch
+
+    n = int(w.x.size)
+    xp = torch.from_numpy(w.x).pin_memory()
+    yp = torch.empty_like(xp).pin_memory()
+    times = []
+    chunks = 0
+    for i in range(args.warmup + args.steps):
+        _, ms, chunks = rfx.fir_stream(xp, w.taps, impl=impl, chunk=STREAM_CHUNK,
+                                       depth=STREAM_DEPTH, memory="registered", out=yp)
+        if i >= args.warmup:
+            times.append(ms)
+    step_ms = statistics.median(times)
+    # Upload per chunk: its outputs widened to the kernel's tile plus one tile (tensor core)
+    # or K - 1 samples (plain) of history.
+    tc = impl == "tc_split" or (impl == "auto" and auto_picks_tc(w.taps.size, n))
+    tile = 96 * 128 if tc else 1
+    hist = tile if tc else w.taps.size - 1
+    up = 0
+    for start in range(0, n, STREAM_CHUNK):
+        end = min(n, start + STREAM_CHUNK)
+        c0 = start // tile * tile
+        c1 = min(n, -(-end // tile) * tile)
+        up += c1 - max(0, c0 - hist)
+    return {"value": n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
+            "h2d_bytes_per_step": up * 8 + w.taps.size * 4, "d2h_bytes_per_step": n * 8,
+            "step_ms": step_ms, "via": f"rfx_fir_stream (registered pinned buffers, "
+                                     f"{chunks} chunks of {STREAM_CHUNK}, depth {STREAM_DEPTH})"}
+
+
 def batch_e2e(rfx, w, impl: str, args, device) -> dict:
     """The batch end to end: every step copies the packed captures from pinned host memory,
     runs rfx_fir_batch_launch and copies every output back, timed with CUDA events."""
@@ -670,12 +712,8 @@ def run_ours(args) -> None:
                                                zp.data_ptr(), rfx.ctypes.byref(b)))
             d2h = zp.numel() * 8
         else:
-            yp = torch.empty_like(xp).pin_memory()
-            rfx._check(lib.rfx_fir_host(rfx.parse_fir_impl(impl), xp.data_ptr(), n,
-                                        w.taps.ctypes.data, w.taps.size, 256, yp.data_ptr(),
-                                        rfx.ctypes.byref(b)))
-            d2h = n * 8
-        if not w.captures:
+            e2e = fir_stream_e2e(rfx, w, impl, args)
+        if w.channels:
             step_ms = b.h2d_ms_mean + b.kernel_ms_mean + b.d2h_ms_mean
             e2e = {"value": n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
                    "h2d_bytes_per_step": n * 8 + w.taps.size * 4, "d2h_bytes_per_step": d2h,

@@ -778,6 +778,17 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
     return cudaErrorInvalidValue;
 }
 
+long long fir_tc_tile_outputs(int num_taps, long long n, TcConfig config)
+{
+    if (n <= 0 || !fir_tc_supported(num_taps)) {
+        return 1;
+    }
+    if (config.tile_blocks == kTcPairTile && n >= 2 * kB && fir_tc2_supported(num_taps)) {
+        return 96LL * 256;
+    }
+    return n < kB ? 1 : static_cast<long long>(kNB) * kB;
+}
+
 cudaError_t fir_tc_take_fault(unsigned int* code)
 {
     unsigned int zero = 0;

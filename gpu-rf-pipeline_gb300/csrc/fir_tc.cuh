@@ -25,6 +25,13 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
                           TcConfig config, cudaStream_t stream);
 cudaError_t fir_tc_take_fault(unsigned int* code);
 
+// Outputs per tile of the form fir_tc_launch picks for (num_taps, n, config): tiles start at
+// multiples of this, and each tile's results depend only on the samples from one tile before
+// its start to its end (its window reaches back C blocks, C * 128 <= 3456 < one tile), so a
+// run over any tile-aligned stretch with one tile of history reproduces the whole run's bits
+// there. 1 when the plain kernel runs instead.
+long long fir_tc_tile_outputs(int num_taps, long long n, TcConfig config);
+
 // Per-capture-taps batch: tensor core (or auto) = one persistent launch of fir_batch.cu per
 // 192 captures; plain = one launch per capture.
 cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,

@@ -1,6 +1,10 @@
 #include "io.hpp"
 
 #include <cstdio>
+#include <cstdlib>
+#include <filesystem>
+#include <fstream>
+#include <iterator>
 #include <stdexcept>
 
 namespace {
@@ -65,4 +69,21 @@ void write_cf32(const std::string& path, const std::vector<cf32>& x)
 void write_f32(const std::string& path, const std::vector<float>& x)
 {
     write_bytes(path, x.data(), x.size() * sizeof(float));
+}
+
+double sample_rate(const std::string& path)
+{
+    const std::string meta = std::filesystem::path(path).replace_extension(".json").string();
+    std::ifstream in(meta);
+    if (!in) {
+        return 0.0;
+    }
+    const std::string text((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+    const std::string key = "\"sample_rate\"";
+    const std::size_t at = text.find(key);
+    if (at == std::string::npos) {
+        return 0.0;
+    }
+    const std::size_t colon = text.find(':', at + key.size());
+    return colon == std::string::npos ? 0.0 : std::strtod(text.c_str() + colon + 1, nullptr);
 }

@@ -3,16 +3,21 @@
 //
 //   rfgpu fir        --in X.cf32 --taps H.f32 --out Y.cf32 [--impl NAME] [--block B]
 //   rfgpu channelize --in X.cf32 --taps H.f32 --channels M --out Z.cf32 [--impl NAME]
+//   rfgpu stream     --in X.cf32 --taps H.f32 --out Y.cf32 [--impl NAME] [--chunk N]
+//                    [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]
 //   rfgpu info
-//   (fir and channelize: [--bench N [--warmup W]] prints phase timings as JSON)
+//   (fir and channelize: [--bench N [--warmup W]] prints phase timings as JSON; stream: the
+//    wall-clock time of whole streamed passes, with the throughput against the sample rate)
 //
 // Exit status: 0 on success, 1 on a runtime error (file, CUDA, cuFFT), 2 on a usage error.
 #include "bench.hpp"
 #include "check.hpp"
 #include "io.hpp"
 #include "ops.hpp"
+#include "stream.hpp"
 
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <exception>
@@ -58,9 +63,13 @@ void print_usage()
                  "[--block B]\n"
                  "  rfgpu channelize --in X.cf32 --taps H.f32 --channels M --out OUT.cf32 "
                  "[--impl NAME]\n"
+                 "  rfgpu stream     --in X.cf32 --taps H.f32 --out OUT.cf32 [--impl NAME] "
+                 "[--chunk N]\n"
+                 "                  [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]\n"
+                 "                  FIR in chunks through a ring of D pinned buffers and CUDA streams\n"
                  "  rfgpu info       GPU, CUDA versions and implementations as JSON\n"
                  "\n"
-                 "benchmark options (fir, channelize):\n"
+                 "benchmark options (fir, channelize, stream):\n"
                  "  --bench N      time N runs with CUDA events and print the result as JSON\n"
                  "  --warmup W     untimed runs before measuring (default 3, needs --bench)\n"
                  "\n"
@@ -233,6 +242,77 @@ int run_channelize(int argc, char** argv)
     return 0;
 }
 
+// Streamed FIR (stream.hpp). Without --bench: one pass, written to --out. With --bench N: W
+// untimed passes, then N timed ones, reported as JSON with the throughput against --rate (or
+// the input's sample rate from its metadata).
+int run_stream(int argc, char** argv)
+{
+    const Args args(argc, argv, {"--in", "--taps", "--out", "--impl", "--chunk", "--depth",
+                                 "--memory", "--rate", "--bench", "--warmup"});
+    args.required("--out");
+    StreamConfig config;
+    const std::string impl = args.optional("--impl", "tiled");
+    if (!parse_fir_impl(impl.c_str(), config.impl)) {
+        throw UsageError("unknown --impl '" + impl + "' for stream (available: " +
+                         impl_names(fir_impls(), ", ") + ")");
+    }
+    const std::string memory = args.optional("--memory", "copy");
+    if (!parse_stream_memory(memory, config.memory)) {
+        throw UsageError("unknown --memory '" + memory +
+                         "' (available: copy, registered, zero-copy)");
+    }
+    config.chunk = args.integer("--chunk", config.chunk, 1);
+    config.depth = args.integer("--depth", config.depth, 1);
+    const BenchConfig bench = bench_config(args);
+    const std::vector<cf32> x = read_cf32(args.required("--in"));
+    const std::vector<float> taps = read_f32(args.required("--taps"));
+    if (taps.empty()) {
+        throw std::runtime_error(args.required("--taps") + ": no taps");
+    }
+    require_int_range(x.size(), "stream input");
+    require_int_range(static_cast<std::size_t>(config.chunk) + taps.size(), "chunk with history");
+    double rate = sample_rate(args.required("--in"));
+    if (args.has("--rate")) {
+        rate = std::stod(args.required("--rate"));
+    }
+    std::vector<double> times;
+    std::vector<cf32> y;
+    StreamTiming timing;
+    const int passes = args.has("--bench") ? bench.warmup + bench.runs : 1;
+    for (int i = 0; i < passes; ++i) {
+        y = fir_stream(x, taps, config, timing);
+        if (i >= passes - bench.runs) {
+            times.push_back(timing.total_ms);
+        }
+    }
+    write_cf32(args.required("--out"), y);
+    if (!args.has("--bench")) {
+        std::printf("stream[%s]: %zu samples in %d chunks of %d, depth %d -> %s\n", impl.c_str(),
+                    x.size(), timing.chunks, config.chunk, config.depth,
+                    args.required("--out").c_str());
+        return 0;
+    }
+    double mean = 0.0;
+    for (double t : times) {
+        mean += t / static_cast<double>(times.size());
+    }
+    double var = 0.0;
+    for (double t : times) {
+        var += (t - mean) * (t - mean);
+    }
+    const double std_ms =
+        times.size() > 1 ? std::sqrt(var / static_cast<double>(times.size() - 1)) : 0.0;
+    const double msps = mean > 0 ? static_cast<double>(x.size()) / (mean * 1e3) : 0.0;
+    std::printf("{\"op\": \"stream\", \"impl\": \"%s\", \"memory\": \"%s\", \"gpu\": \"%s\", "
+                "\"num_in\": %zu, \"chunk\": %d, \"depth\": %d, \"chunks\": %d, \"runs\": %d, "
+                "\"warmup\": %d, \"total_ms\": {\"mean\": %.6f, \"std\": %.6f}, \"msps\": %.3f, "
+                "\"sample_rate\": %.1f, \"realtime_factor\": %.3f}\n",
+                impl.c_str(), memory.c_str(), gpu_name().c_str(), x.size(), config.chunk,
+                config.depth, timing.chunks, bench.runs, bench.warmup, mean, std_ms, msps, rate,
+                rate > 0 ? msps * 1e6 / rate : 0.0);
+    return 0;
+}
+
 std::string version_string(int packed)
 {
     return std::to_string(packed / 1000) + "." + std::to_string((packed % 1000) / 10);
@@ -269,6 +349,7 @@ int main(int argc, char** argv)
         const std::string op = argc > 1 ? argv[1] : "";
         if (op == "fir") return run_fir(argc, argv);
         if (op == "channelize") return run_channelize(argc, argv);
+        if (op == "stream") return run_stream(argc, argv);
         if (op == "info") return run_info(argc, argv);
         if (op == "--help" || op == "-h" || op == "help") {
             print_usage();

@@ -39,6 +39,14 @@ class Bench(ctypes.Structure):
                 ("d2h_ms_mean", ctypes.c_double), ("d2h_ms_std", ctypes.c_double)]
 
 
+class StreamConfig(ctypes.Structure):
+    _fields_ = [("impl", ctypes.c_int), ("memory", ctypes.c_int), ("chunk", ctypes.c_int64),
+                ("depth", ctypes.c_int)]
+
+
+STREAM_MEMORY = {"copy": 0, "registered": 1, "zero-copy": 2}
+
+
 # name -> (restype, argtypes); every symbol include/rfx.h declares.
 _VP, _I, _I64, _SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_size_t
 SIGNATURES = {
@@ -61,6 +69,8 @@ SIGNATURES = {
     "rfx_channelize_launch": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _VP]),
     "rfx_channelize_branches": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
     "rfx_channelize_tc_static": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
+    "rfx_fir_stream": (_I, [_VP, _I64, _VP, _I, ctypes.POINTER(StreamConfig), _VP,
+                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
     "rfx_fir_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_channelize_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_autotune_fir": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),
@@ -265,6 +275,30 @@ def channelize_host(impl, x, taps, channels: int, warmup: int = 0, runs: int = 1
     _check(load().rfx_channelize_host(impl_v, x.ctypes.data, x.size, taps.ctypes.data,
                                       taps.size, channels, z.ctypes.data, ctypes.byref(b)))
     return z.reshape(f, channels), b
+
+
+def fir_stream(x, taps, impl="plain", chunk: int = 1 << 20, depth: int = 3,
+               memory: str = "copy", out=None):
+    """The streamed FIR of a host capture (numpy complex64 or a CPU tensor; pinned tensors are
+    used in place in "registered" mode). Returns (y, total_ms, chunks)."""
+    import numpy as np
+
+    if hasattr(x, "data_ptr"):
+        x_ptr, n = x.data_ptr(), x.numel()
+        y = out if out is not None else x.new_empty(x.shape)
+        y_ptr = y.data_ptr()
+    else:
+        x = np.ascontiguousarray(x, dtype=np.complex64)
+        x_ptr, n = x.ctypes.data, x.size
+        y = out if out is not None else np.empty_like(x)
+        y_ptr = y.ctypes.data if not hasattr(y, "data_ptr") else y.data_ptr()
+    taps = np.ascontiguousarray(taps, dtype=np.float32)
+    cfg = StreamConfig(_impl(impl), STREAM_MEMORY[memory], chunk, depth)
+    ms = ctypes.c_double()
+    chunks = ctypes.c_int()
+    _check(load().rfx_fir_stream(x_ptr, n, taps.ctypes.data, taps.size, ctypes.byref(cfg), y_ptr,
+                                 ctypes.byref(ms), ctypes.byref(chunks)))
+    return y, ms.value, chunks.value
 
 
 def autotune_fir(impl, num_taps: int, num_samples: int) -> float:

@@ -174,6 +174,33 @@ int rfx_channelize_branches(const void* x, const float* taps, void* u, int64_t n
 int rfx_channelize_tc_static(const void* x, const float* taps, void* out, int64_t num_samples,
                              int num_taps, int channels, cudaStream_t stream);
 
+/* ---- streaming ------------------------------------------------------------------------ */
+
+/* Host memory of a stream run (the project's StreamMemory, src/stream.hpp:34-38). */
+typedef enum rfx_stream_memory {
+    RFX_STREAM_COPY = 0,        /* samples copied into and out of a pinned ring on the host */
+    RFX_STREAM_REGISTERED = 1,  /* x and y page-locked in place (already pinned memory as is) */
+    RFX_STREAM_ZERO_COPY = 2    /* chunks moved through mapped pinned memory by GPU kernels */
+} rfx_stream_memory;
+
+/* The project's StreamConfig (src/stream.hpp:40-45). */
+typedef struct rfx_stream_config {
+    int impl;          /* rfx_fir_impl (auto is resolved once, for the whole capture) */
+    int memory;        /* rfx_stream_memory */
+    int64_t chunk;     /* samples per chunk, >= 1 */
+    int depth;         /* slots in the ring (and CUDA streams), >= 1 */
+} rfx_stream_config;
+
+/* The FIR of a HOST capture in chunks through a ring of `depth` slots, each chunk's upload,
+ * kernel and download on the slot's own stream. `y_iq` receives exactly the bits one
+ * rfx_fir_launch of the same implementation over the whole capture would give (each chunk is
+ * computed with history: K - 1 samples for the plain kernel, one tile at tile-aligned positions
+ * for the tensor-core form). Allocation and the tap upload come before the clock; `total_ms`
+ * (may be NULL) is the wall clock from the first chunk to the last output, `chunks` (may be
+ * NULL) the number of chunks. Replaces fir_stream (src/stream.hpp:50-53, src/stream.cu:135-222). */
+int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float* taps, int num_taps,
+                   const rfx_stream_config* config, void* y_iq, double* total_ms, int* chunks);
+
 /* ---- host-buffer operations (timed like the project's Bench) --------------------------- */
 
 /* Phase timings of a host-buffer call, as the project's BenchResult (src/bench.hpp:17-32). */

@@ -251,3 +251,50 @@ def test_channelize_puts_a_tone_in_its_channel(fixtures: Path, tmp_path: Path) -
     assert np.argmax(power) == 3
     assert power[3] > 1000 * np.max(np.delete(power, 3))
     np.testing.assert_allclose(np.abs(z[:, 3]), 1.0, atol=0.02)
+
+
+# --- stream ----------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("args", [["--chunk", "0"], ["--depth", "0"], ["--memory", "disk"]])
+def test_bad_stream_options_are_usage_errors(fixtures: Path, tmp_path: Path, args) -> None:
+    proc = rfgpu("stream", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", *args, check=False)
+    assert proc.returncode == 2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", ["tiled", "tc_split", "auto"])
+@pytest.mark.parametrize("chunk,depth", [(1000, 3), (4096, 2), (100000, 1)])
+@pytest.mark.parametrize("memory", ["copy", "registered", "zero-copy"])
+def test_stream_matches_fir_exactly(fixtures: Path, tmp_path: Path, impl: str, chunk: int,
+                                    depth: int, memory: str) -> None:
+    rfgpu("fir", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass_long.f32",
+          "--out", tmp_path / "fir.cf32", "--impl", impl)
+    rfgpu("stream", "--in", fixtures / "tone.cf32", "--taps", fixtures / "lowpass_long.f32",
+          "--out", tmp_path / "stream.cf32", "--impl", impl, "--chunk", chunk, "--depth", depth,
+          "--memory", memory)
+    assert (tmp_path / "fir.cf32").read_bytes() == (tmp_path / "stream.cf32").read_bytes()
+
+
+@pytest.mark.gpu
+def test_stream_of_short_input(fixtures: Path, tmp_path: Path) -> None:
+    rfgpu("stream", "--in", fixtures / "short.cf32", "--taps", fixtures / "lowpass.f32",
+          "--out", tmp_path / "y.cf32", "--chunk", 3)
+    expected = orc.fir_fast(signals.fixture_signal("short"), signals.fixture_taps("lowpass"))
+    np.testing.assert_allclose(read_cf32(tmp_path / "y.cf32"), expected, rtol=FIR_RTOL,
+                               atol=FIR_ATOL)
+
+
+@pytest.mark.gpu
+def test_stream_bench_reports_throughput_against_the_sample_rate(fixtures: Path,
+                                                                  tmp_path: Path) -> None:
+    data = tmp_path / "tone.cf32"
+    data.write_bytes((fixtures / "tone.cf32").read_bytes())
+    (tmp_path / "tone.json").write_text(json.dumps({"sample_rate": 2.4e6}))
+    proc = rfgpu("stream", "--in", data, "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", "--chunk", 8192, "--bench", 10)
+    report = json.loads(proc.stdout)
+    assert report["op"] == "stream" and report["chunks"] == 8 and report["runs"] == 10
+    assert report["sample_rate"] == 2.4e6
+    assert report["msps"] > 0
+    assert report["realtime_factor"] == pytest.approx(report["msps"] * 1e6 / 2.4e6, rel=1e-3)
