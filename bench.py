@@ -223,6 +223,16 @@ def load_workload(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of it on the
+# workload (dram__bytes_read.sum + dram__bytes_write.sum); writes still in L2 at the kernel's end
+# are not counted by that capture.
+NCU_TRAFFIC_BYTES = {
+    ("fir1025_tones", "tc_split"): 134.4e6 + 79.7e6,
+    ("fir63_white", "plain"): 134.2e6 + 89.1e6,
+    ("pfb64", "tc_split"): 135.7e6 + 76.5e6,
+}
+
+
 def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -672,6 +682,13 @@ def run_ours(args) -> None:
         roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"],
                     "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None}
     roofline["peak_source"] = pk["source"]
+    kernel_impl = impl
+    if impl == "auto" and not w.captures and not w.channels:
+        kernel_impl = "tc_split" if auto_picks_tc(w.taps.size, n) else "plain"
+    traffic = NCU_TRAFFIC_BYTES.get((w.name, kernel_impl))
+    if traffic is not None:
+        roofline["traffic"] = traffic
+        roofline["traffic_unit"] = "bytes per launch (ncu, one capture)"
     if "plain" in arms and not w.channels and not w.captures:
         sm_mhz = (clocks or {}).get("sm_mhz") or 1900.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
