@@ -8,7 +8,7 @@
 // capture), so a launch allocates nothing and can be captured in a CUDA graph.
 //
 // The per-tile pipeline is the one of fir_tc.cu (worker warps convert scaled FP16 hi/lo sample
-// planes; h_hi x_hi goes to accumulator H in groups of at most 12 MMAs, each drained into FP32
+// planes; h_hi x_hi goes to accumulator H in groups of at most 18 MMAs, each drained into FP32
 // running sums in registers, the cross products to accumulator X, drained once per tile; one
 // thread issues the MMAs from a lean loop), with two differences: samples are loaded from global
 // memory by the workers (one tensor map per capture would not fit the parameter space), and when
@@ -40,7 +40,7 @@ constexpr int kWorkers = kWorkerWarps * 32;
 constexpr int kMmaWarp = 16;
 constexpr int kThreads = 17 * 32;
 constexpr int kCols = kN / 4;
-constexpr int kHGroup = 12;       // MMAs per H accumulation, at most
+constexpr int kHGroup = 18;       // MMAs per H accumulation, at most
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kXCol = kN;
 constexpr uint32_t kIdesc = idesc_f16(kB, kN);
@@ -113,8 +113,8 @@ __device__ __forceinline__ int capture_of(const BatchParams& p, int item, int cu
     return cursor;
 }
 
-// H groups of a tile of a capture with P chunks: `ksg` whole K-steps (P <= 12), or `gpk`
-// groups of at most `cpg` chunks per K-step (P > 12); see fir_tc.cu.
+// H groups of a tile of a capture with P chunks: `ksg` whole K-steps (P <= 18), or `gpk`
+// groups of at most `cpg` chunks per K-step (P > 18); see fir_tc.cu.
 struct HGroups {
     int ksg;
     int gpk;

@@ -25,11 +25,13 @@
 // Accumulation: the tensor core adds each MMA's products into its FP32 accumulator with
 // round-toward-zero, so the error of an accumulator grows with the number of MMAs it takes, in
 // units of its own magnitude. The large product h_hi x_hi therefore goes to accumulator H in
-// GROUPS of 12 consecutive (K-step, chunk) steps (a group may straddle K-steps); the worker
+// GROUPS of at most 18 MMAs (whole K-steps; at 1025 taps two K-steps of 9 chunks); the worker
 // warps add each group's sum into FP32 running sums in registers (round-to-nearest). The two
 // cross products, 2^-11 smaller, go to accumulator X for the whole tile and are drained once.
-// Per group the MMA thread issues the 12 H MMAs, commits, then the group's 24 X MMAs, during
-// which the workers drain H.
+// Per group the MMA thread issues the H MMAs, commits, then the group's X MMAs (twice as many),
+// during which the workers drain H. Larger groups mean fewer commits and hand-offs for the
+// issuing thread (which bounds the MMA rate) at an error that grows with the group: 5e-7 at 9
+// MMAs, 8e-7 at 18 (1025 taps).
 //
 // Roles (544 threads): warps 0-15 are workers and warp 16 owns tensor memory and issues the MMAs
 // (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 48 (w / 4) .. +47 of H
@@ -69,7 +71,7 @@ constexpr int kWorkers = kWorkerWarps * 32;
 constexpr int kMmaWarp = 16;
 constexpr int kThreads = 17 * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
-constexpr int kHGroup = 12;              // MMAs per H accumulation, at most
+constexpr int kHGroup = 18;              // MMAs per H accumulation, at most
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
 constexpr int kScanBufsMax = 4;          // scan slice ring depth: 4 (2 for the longest filters);
                                          // slices are copied depth - 1 K-steps ahead
@@ -134,13 +136,13 @@ struct Ctrl {
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
-// H groups of a tile. For P <= 12 chunks a group is `ksg` whole K-steps (at most 12 MMAs, and
+// H groups of a tile. For P <= 18 chunks a group is `ksg` whole K-steps (at most 18 MMAs, and
 // fewer K-steps than operand stages, since a group holds its stages until its X MMAs); for
-// P > 12 each K-step splits into `gpk` groups of at most `cpg` chunks.
+// P > 18 each K-step splits into `gpk` groups of at most `cpg` chunks.
 struct HGroups {
-    int ksg;        // K-steps per group (P <= 12)
-    int gpk;        // groups per K-step (P > 12), else 1
-    int cpg;        // chunks per group (P > 12), else P
+    int ksg;        // K-steps per group (P <= 18)
+    int gpk;        // groups per K-step (P > 18), else 1
+    int cpg;        // chunks per group (P > 18), else P
     int per_tile;
 };
 

@@ -24,7 +24,7 @@
 // Split precision, accumulation and roles as in the single-CTA form: x' = 2^ex x (ex per tile,
 // common to the pair: each CTA scans its window and the two maxima are exchanged through
 // distributed shared memory) and h' = 2^eh h split into FP16 hi + lo; h_hi x_hi goes to
-// accumulator H in groups of at most 12 MMAs, each group added into FP32 running sums in
+// accumulator H in groups of at most 18 MMAs, each group added into FP32 running sums in
 // registers (the tensor core rounds toward zero); the cross products go to accumulator X, drained
 // once per tile. Warps 0-15 of each CTA convert samples, drain their CTA's 128 rows and write
 // outputs; warp 16 of the even CTA issues the MMAs for the pair; warp 17 of each CTA issues its
@@ -62,7 +62,7 @@ constexpr int kMmaWarp = 16;
 constexpr int kTmaWarp = 17;
 constexpr int kThreads = 18 * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
-constexpr int kHGroup = 12;              // MMAs per H accumulation, at most
+constexpr int kHGroup = 18;              // MMAs per H accumulation, at most
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
 constexpr int kScanBufsMax = 4;          // scan slice ring depth (slices copied depth-2 ahead)
 constexpr int kMaxStages = 8;
@@ -129,9 +129,9 @@ struct Ctrl {
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
-// H groups of a tile: `ksg` whole K-steps (P <= 12 chunks; fewer K-steps than operand stages,
+// H groups of a tile: `ksg` whole K-steps (P <= 18 chunks; fewer K-steps than operand stages,
 // since a group holds its stages until its X MMAs), or `gpk` groups of at most `cpg` chunks
-// per K-step (P > 12).
+// per K-step (P > 18).
 struct HGroups {
     int ksg;
     int gpk;
