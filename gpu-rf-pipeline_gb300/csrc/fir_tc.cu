@@ -33,13 +33,14 @@
 // issuing thread (which bounds the MMA rate) at an error that grows with the group: 5e-7 at 9
 // MMAs, 8e-7 at 18 (1025 taps).
 //
-// Roles (544 threads): warps 0-15 are workers and warp 16 owns tensor memory and issues the MMAs
-// (one thread). A worker warp w drains TMEM lane quarter w % 4, columns 48 (w / 4) .. +47 of H
-// and of X, holds
-// those 48 running sums (96 registers per thread: one SM sub-partition hosts five of the 17 warps), writes those outputs, and shares the producing: each K-step's fp32
-// samples arrive by a 2-D TMA copy (zero fill outside the input) and are converted into the
-// FP16 planes; the next tile's scale is a max over its input window, copied by TMA in eight
-// slices, one per K-step of the current tile, and read a K-step later.
+// Roles (768 threads): warps 0-15 hold the running sums: a drain warp w drains TMEM lane quarter
+// w % 4, columns 48 (w / 4) .. +47 of H and of X, and writes those outputs (48 running sums per
+// thread); warps 16-22 produce: each K-step's fp32 samples arrive by a 2-D TMA copy (zero fill
+// outside the input) and are converted into the FP16 planes, the next tile's scale is a max
+// over its input window, copied by TMA in eight slices three K-steps ahead; warp 23 owns tensor
+// memory and issues the MMAs (one thread). The drains never wait behind production, and the
+// producer count balances the MMA rate (measured: 3 producer warps 173 us, 5 154 us, 7 144 us at
+// 1025 taps; beyond 7 no gain). 24 warps: one SM sub-partition holds six, so 80 registers.
 // Every wait is an mbarrier wait bounded in time; a give-up sets the fault word and every role
 // stops.
 #include "fir_tc.cuh"
@@ -66,10 +67,12 @@ constexpr int kB = 128;                  // outputs per block = MMA M
 constexpr int kNB = 96;                  // blocks per tile; MMA N = 2 * kNB = 192
 constexpr int kN = 2 * kNB;
 constexpr int kStagesPerTile = kB / 16;  // K-steps of 16 samples
-constexpr int kWorkerWarps = 16;
-constexpr int kWorkers = kWorkerWarps * 32;
-constexpr int kMmaWarp = 16;
-constexpr int kThreads = 17 * 32;
+constexpr int kDrainWarps = 16;          // hold the running sums, drain, store
+constexpr int kProducerWarps = 7;        // scan, convert, issue the copies
+constexpr int kProducers = kProducerWarps * 32;
+constexpr int kFirstProducerWarp = kDrainWarps;
+constexpr int kMmaWarp = kDrainWarps + kProducerWarps;
+constexpr int kThreads = (kMmaWarp + 1) * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
 constexpr int kHGroup = 18;              // MMAs per H accumulation, at most
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
@@ -124,14 +127,15 @@ struct Ctrl {
     unsigned long long scan_full[kScanBufsMax];
     unsigned long long scan_empty[kScanBufsMax];
     unsigned long long pfull;     // H group summed (tcgen05.commit)
-    unsigned long long pempty;    // H drained (every worker warp)
+    unsigned long long pempty;    // H drained (every drain warp)
     unsigned long long xfull;     // X of a tile summed
     unsigned long long xempty;    // X drained
-    unsigned long long reduce[2];
+    unsigned long long sready[4]; // the scale of tile k is in ex[k % 4]
     unsigned long long teardown;
     uint32_t tmem_base;
     int abort;
-    uint32_t warp_max[2][kWorkerWarps];
+    uint32_t pmax[2][kProducerWarps];
+    int ex[4];
     uint32_t tap_max;
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
@@ -214,24 +218,24 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
     // ---- setup: barriers, tensor memory, first raw copies, tap strip -----------------------
     if (threadIdx.x == 0) {
         for (int i = 0; i < S; ++i) {
-            mbar_init(smem_u32(&ctl.full[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.full[i]), kProducerWarps);
             mbar_init(smem_u32(&ctl.empty[i]), 1);
         }
         for (int i = 0; i < kRaw; ++i) {
             mbar_init(smem_u32(&ctl.raw_full[i]), 1);
-            mbar_init(smem_u32(&ctl.raw_empty[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.raw_empty[i]), kProducerWarps);
         }
-        for (int i = 0; i < 2; ++i) {
-            mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
+        for (int i = 0; i < 4; ++i) {
+            mbar_init(smem_u32(&ctl.sready[i]), 1);
         }
         for (int i = 0; i < sbufs; ++i) {
             mbar_init(smem_u32(&ctl.scan_full[i]), 1);
-            mbar_init(smem_u32(&ctl.scan_empty[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.scan_empty[i]), kProducerWarps);
         }
         mbar_init(smem_u32(&ctl.pfull), 1);
-        mbar_init(smem_u32(&ctl.pempty), kWorkerWarps);
+        mbar_init(smem_u32(&ctl.pempty), kDrainWarps);
         mbar_init(smem_u32(&ctl.xfull), 1);
-        mbar_init(smem_u32(&ctl.xempty), kWorkerWarps);
+        mbar_init(smem_u32(&ctl.xempty), kDrainWarps);
         mbar_init(smem_u32(&ctl.teardown), 1);
         ctl.abort = 0;
         ctl.tap_max = 0;
@@ -302,14 +306,80 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
     fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    if (warp < kWorkerWarps) {
-        // ---- workers ------------------------------------------------------------------------
+    if (warp < kDrainWarps) {
+        // ---- drain warps: running sums, outputs ----------------------------------------------
         const int quarter = warp & 3;
         const int slice = warp >> 2;                       // columns kCols * slice .. +kCols-1
         const int r = kB - 1 - (quarter * 32 + lane);      // output row of this TMEM lane
         const uint32_t lane_addr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
                                    static_cast<uint32_t>(slice * kCols);
-        const int wtid = threadIdx.x;                      // 0 .. kWorkers-1
+        float acc[kCols];
+#pragma unroll
+        for (int i = 0; i < kCols; ++i) {
+            acc[i] = 0.0f;
+        }
+        // Adds accumulator columns col .. col + kCols - 1 of this lane into acc.
+        auto drain = [&](uint32_t col) {
+            fence_after();
+#pragma unroll
+            for (int c16 = 0; c16 < kCols / 16; ++c16) {
+                uint32_t t[16];
+                tmem_ld16(lane_addr + col + static_cast<uint32_t>(c16 * 16), t);
+                tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    acc[c16 * 16 + i] += __uint_as_float(t[i]);
+                }
+            }
+            fence_before();
+            __syncwarp();
+        };
+        bool ok = true;
+        int g = 0;   // H groups drained so far
+        for (int k = 0; k < my_tiles && ok && !*abort; ++k) {
+            for (int gi = 0; gi < grp.per_tile; ++gi, ++g) {
+                if (!mbar_wait_bounded(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
+                                       abort)) {
+                    ok = false;
+                    break;
+                }
+                drain(0);
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(&ctl.pempty));
+                }
+            }
+            if (!ok ||
+                !mbar_wait_bounded(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull, abort)) {
+                break;
+            }
+            drain(kXCol);
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&ctl.xempty));
+            }
+            // The tile's sample scale (written by the producers before its first K-step).
+            if (!mbar_wait_bounded(smem_u32(&ctl.sready[k & 3]), (k >> 2) & 1, fault,
+                                   kFaultScale, abort)) {
+                break;
+            }
+            const int ex = *reinterpret_cast<volatile int*>(&ctl.ex[k & 3]);
+            const int shift = -(ex + eh);
+            const float fa = exp2i(shift / 2);
+            const float fb = exp2i(shift - shift / 2);
+            const long long jb0 = static_cast<long long>(tile_of(k)) * kNB + slice * (kCols / 2);
+#pragma unroll
+            for (int b = 0; b < kCols / 2; ++b) {
+                const long long o = (jb0 + b) * kB + r;
+                if (o < n) {
+                    y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
+                }
+                acc[2 * b] = 0.0f;
+                acc[2 * b + 1] = 0.0f;
+            }
+        }
+    } else if (warp < kFirstProducerWarp + kProducerWarps) {
+        // ---- producers: scales, operand stages, copies ---------------------------------------
+        const int pw = warp - kFirstProducerWarp;
+        const int ptid = static_cast<int>(threadIdx.x) - kFirstProducerWarp * 32;
         int ex_even = 0;                                   // scale exponents of even, odd tiles
         int ex_odd = 0;
         uint32_t next_max = 0;                             // running max of the next tile's scan
@@ -325,29 +395,30 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             }
             return 0u;
         };
-        // Combines every worker's partial max for tile k into its scale exponent.
-        auto reduce_scale = [&](int k, uint32_t m) -> bool {
+        // Combines the producers' partial maxima for tile k into its scale exponent and
+        // publishes it to the drain warps.
+        auto reduce_scale = [&](int k, uint32_t m) {
             m = __reduce_max_sync(0xFFFFFFFFu, m);
             const int rb = k & 1;
             if (lane == 0) {
-                ctl.warp_max[rb][warp] = m;
-                mbar_arrive(smem_u32(&ctl.reduce[rb]));
+                ctl.pmax[rb][pw] = m;
             }
-            if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (k >> 1) & 1, fault,
-                                   kFaultStageEmpty, abort)) {
-                return false;
-            }
+            asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory");
             uint32_t tmax = 0;
 #pragma unroll
-            for (int w = 0; w < kWorkerWarps; ++w) {
-                tmax = max(tmax, ctl.warp_max[rb][w]);
+            for (int w = 0; w < kProducerWarps; ++w) {
+                tmax = max(tmax, ctl.pmax[rb][w]);
             }
+            const int ex = scale_exponent(tmax);
             if (k & 1) {
-                ex_odd = scale_exponent(tmax);
+                ex_odd = ex;
             } else {
-                ex_even = scale_exponent(tmax);
+                ex_even = ex;
             }
-            return true;
+            if (ptid == 0) {
+                ctl.ex[k & 3] = ex;
+                mbar_arrive(smem_u32(&ctl.sready[k & 3]));
+            }
         };
         // Scan slice q, copied by TMA sbufs - 1 K-steps earlier: rows past the window are
         // ignored; the partial last block lies outside the tensor map (the copy reads zeros
@@ -364,12 +435,13 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
             const int quads = min(lay.srows, lay.rows - r0) * 64;   // float4 in the window
             uint32_t m = next_max;
-            for (int f = wtid; f < quads; f += kWorkers) {
+#pragma unroll 4
+            for (int f = ptid; f < quads; f += kProducers) {
                 m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
             }
             const long long tail_row = full_blocks - (j0 - C) - r0;
-            if (tail_row >= 0 && tail_row * 64 < quads && wtid < 64) {
-                m = max(m, load_pair(full_blocks * kB + 2 * wtid, n));
+            if (tail_row >= 0 && tail_row * 64 < quads && ptid < 64) {
+                m = max(m, load_pair(full_blocks * kB + 2 * ptid, n));
             }
             next_max = m;
             __syncwarp();
@@ -377,9 +449,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                 mbar_arrive(smem_u32(&ctl.scan_empty[qb]));
             }
             if (q % kStagesPerTile == kStagesPerTile - 1) {
-                if (!reduce_scale(k, next_max)) {
-                    return false;
-                }
+                reduce_scale(k, next_max);
                 next_max = 0;
             }
             return true;
@@ -411,7 +481,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             // Window row of the input's last, partial block (outside the tensor maps), if any.
             const long long tail_rel = full_blocks - (j0 - C);
             const int b_tail = tail_rel >= 0 && tail_rel < lay.rows ? static_cast<int>(tail_rel) : -1;
-            for (int f = wtid; f < items; f += kWorkers) {
+#pragma unroll 2
+            for (int f = ptid; f < items; f += kProducers) {
                 const int b = f >> 3;
                 const int q = f & 7;
                 float4 v4;
@@ -446,8 +517,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                 mbar_arrive(smem_u32(&ctl.full[slot]));
                 mbar_arrive(smem_u32(&ctl.raw_empty[rslot]));
             }
-            if (wtid == 0) {
-                // Refill this raw slot with K-step v + kRaw once every warp has converted it.
+            if (ptid == 0) {
+                // Refill this raw slot with K-step v + kRaw once every producer has converted it.
                 if (v + kRaw < my_steps) {
                     if (!mbar_wait_bounded(smem_u32(&ctl.raw_empty[rslot]), (v / kRaw) & 1,
                                            fault, kFaultStageEmpty, abort)) {
@@ -482,11 +553,11 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             const long long hi0 = (j0 + kNB) * kB < n ? (j0 + kNB) * kB : n;
             const long long pairs = (hi0 - lo0 + 1) / 2;
             uint32_t m = 0;
-            for (long long base = 0; base < pairs; base += 8 * kWorkers) {
+            for (long long base = 0; base < pairs; base += 8 * kProducers) {
                 uint32_t part[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const long long idx = base + wtid + i * kWorkers;
+                    const long long idx = base + ptid + i * kProducers;
                     part[i] = idx < pairs ? load_pair(lo0 + 2 * idx, hi0) : 0u;
                 }
 #pragma unroll
@@ -494,87 +565,13 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                     m = max(m, part[i]);
                 }
             }
-            ok = reduce_scale(0, m);
+            reduce_scale(0, m);
         }
-        for (int v = 0; v < S && v < my_steps && ok; ++v) {
+        for (int v = 0; v < my_steps && ok && !*abort; ++v) {
             ok = produce(v);
         }
-        float acc[kCols];
-#pragma unroll
-        for (int i = 0; i < kCols; ++i) {
-            acc[i] = 0.0f;
-        }
-        int gi = 0;  // next tile-local group to drain
-        for (int u = 0; u < my_steps && ok && !*abort; ++u) {
-            const int k = u / kStagesPerTile;
-            const int st = u % kStagesPerTile;
-            // Adds accumulator columns col .. col + kCols - 1 of this lane into acc.
-            auto drain = [&](uint32_t col) {
-                fence_after();
-#pragma unroll
-                for (int c16 = 0; c16 < kCols / 16; ++c16) {
-                    uint32_t t[16];
-                    tmem_ld16(lane_addr + col + static_cast<uint32_t>(c16 * 16), t);
-                    tmem_wait_ld();
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        acc[c16 * 16 + i] += __uint_as_float(t[i]);
-                    }
-                }
-                fence_before();
-                __syncwarp();
-            };
-            // Drain the H groups whose last (K-step, chunk) step lies in K-step u.
-            while (gi < grp.per_tile &&
-                   (grp.gpk == 1 ? min(kStagesPerTile, (gi + 1) * grp.ksg) - 1 : gi / grp.gpk) <=
-                       st) {
-                const int g = k * grp.per_tile + gi;
-                if (!mbar_wait_bounded(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
-                                       abort)) {
-                    ok = false;
-                    break;
-                }
-                drain(0);
-                if (lane == 0) {
-                    mbar_arrive(smem_u32(&ctl.pempty));
-                }
-                ++gi;
-            }
-            if (!ok) {
-                break;
-            }
-            if (st == kStagesPerTile - 1) {
-                // The tile's cross products.
-                if (!mbar_wait_bounded(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull,
-                                       abort)) {
-                    break;
-                }
-                drain(kXCol);
-                if (lane == 0) {
-                    mbar_arrive(smem_u32(&ctl.xempty));
-                }
-                // Last K-step of tile k: scale and store this thread's outputs.
-                const int shift = -(((k & 1) ? ex_odd : ex_even) + eh);
-                const float fa = exp2i(shift / 2);
-                const float fb = exp2i(shift - shift / 2);
-                const long long jb0 = static_cast<long long>(tile_of(k)) * kNB + slice * (kCols / 2);
-#pragma unroll
-                for (int b = 0; b < kCols / 2; ++b) {
-                    const long long o = (jb0 + b) * kB + r;
-                    if (o < n) {
-                        y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
-                    }
-                    acc[2 * b] = 0.0f;
-                    acc[2 * b + 1] = 0.0f;
-                }
-                gi = 0;
-            }
-            if (u + S < my_steps) {
-                ok = produce(u + S);
-            }
-        }
-    } else if (lane == 0) {
-        // ---- MMA issuer (warp 16, one thread) ----------------------------------------------
+    } else if (warp == kMmaWarp && lane == 0) {
+        // ---- MMA issuer (warp 23, one thread) ----------------------------------------------
         const uint32_t taps_hi = sbase + lay.taps_hi;
         const uint32_t taps_lo = sbase + lay.taps_lo;
         // The issue loop is latency-bound in this one thread, so it is kept lean: per MMA one
@@ -619,14 +616,25 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                         fence_after();
                         ready = u + 1;
                     }
-                    uint32_t a = a_hi0 + static_cast<uint32_t>(2 * st - 16 * c0) * 8u;
-                    uint32_t b = b_base + static_cast<uint32_t>(slot) * stage_units -
-                                 static_cast<uint32_t>(2 * c0);
-                    for (int c = c0; c < c1; ++c) {
-                        mma_f16<kIdesc>(h_acc, a_desc | a, b_desc | b, acc);
+                    // 64-bit descriptors stepped in their start-address field (no borrow
+                    // leaves it: addresses stay positive).
+                    unsigned long long da =
+                        a_desc | (a_hi0 + static_cast<uint32_t>(2 * st - 16 * c0) * 8u);
+                    unsigned long long db =
+                        b_desc | (b_base + static_cast<uint32_t>(slot) * stage_units -
+                                  static_cast<uint32_t>(2 * c0));
+                    int c = c0;
+                    if (acc == 0) {
+                        mma_f16<kIdesc>(h_acc, da, db, 0u);
                         acc = 1;
-                        a -= 128;
-                        b -= 2;
+                        da -= 128;
+                        db -= 2;
+                        ++c;
+                    }
+                    for (; c < c1; ++c) {
+                        mma_f16_acc<kIdesc>(h_acc, da, db);
+                        da -= 128;
+                        db -= 2;
                     }
                 }
                 if (stop) {
@@ -646,17 +654,30 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                 for (int st = st0; st < st1; ++st) {
                     const int slot = (k * kStagesPerTile + st) % S;
                     const uint32_t off = static_cast<uint32_t>(2 * st - 16 * c0) * 8u;
-                    uint32_t ah = a_hi0 + off;
-                    uint32_t al = a_lo0 + off;
-                    uint32_t b = b_base + static_cast<uint32_t>(slot) * stage_units -
-                                 static_cast<uint32_t>(2 * c0);
-                    for (int c = c0; c < c1; ++c) {
-                        mma_f16<kIdesc>(x_acc, a_desc | ah, b_desc | (b + split_units), acc);
-                        mma_f16<kIdesc>(x_acc, a_desc | al, b_desc | b, 1u);
+                    unsigned long long dah = a_desc | (a_hi0 + off);
+                    unsigned long long dal = a_desc | (a_lo0 + off);
+                    unsigned long long dbh =
+                        b_desc | (b_base + static_cast<uint32_t>(slot) * stage_units -
+                                  static_cast<uint32_t>(2 * c0));
+                    unsigned long long dbl = dbh + split_units;
+                    int c = c0;
+                    if (acc == 0) {
+                        mma_f16<kIdesc>(x_acc, dah, dbl, 0u);
+                        mma_f16_acc<kIdesc>(x_acc, dal, dbh);
                         acc = 1;
-                        ah -= 128;
-                        al -= 128;
-                        b -= 2;
+                        dah -= 128;
+                        dal -= 128;
+                        dbh -= 2;
+                        dbl -= 2;
+                        ++c;
+                    }
+                    for (; c < c1; ++c) {
+                        mma_f16_acc<kIdesc>(x_acc, dah, dbl);
+                        mma_f16_acc<kIdesc>(x_acc, dal, dbh);
+                        dah -= 128;
+                        dal -= 128;
+                        dbh -= 2;
+                        dbl -= 2;
                     }
                     if (c1 == P) {
                         // Every MMA reading this K-step's operand stage has been issued.

@@ -38,6 +38,18 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, unsigned long long a,
         : "memory");
 }
 
+// The same with the accumulate flag fixed at 1 (D += A B): no predicate set-up from a register.
+template <uint32_t kIdesc>
+__device__ __forceinline__ void mma_f16_acc(uint32_t d_tmem, unsigned long long a,
+                                            unsigned long long b)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.eq.u32 p, 1, 1;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(kIdesc)
+        : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar)
 {
     asm volatile(
