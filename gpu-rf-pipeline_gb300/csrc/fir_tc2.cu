@@ -26,11 +26,11 @@
 // distributed shared memory) and h' = 2^eh h split into FP16 hi + lo; h_hi x_hi goes to
 // accumulator H in groups of at most 18 MMAs, each group added into FP32 running sums in
 // registers (the tensor core rounds toward zero); the cross products go to accumulator X, drained
-// once per tile. Warps 0-15 of each CTA convert samples, drain their CTA's 128 rows and write
-// outputs; warp 16 of the even CTA issues the MMAs for the pair; warp 17 of each CTA issues its
-// copies (raw stages and scan slices) as the workers free their buffers. Stage and accumulator
-// handshakes go to the even CTA's mbarriers (the odd CTA arrives remotely); the MMA commits
-// arrive on both CTAs' mbarriers (multicast). Every wait is bounded in time.
+// once per tile. Roles per CTA: warps 0-15 drain (running sums, outputs), warps 16-21 produce (scan,
+// convert), warp 22 issues the copies, warp 23 issues the MMAs for the pair (even CTA) or
+// forwards the odd CTA's hand-offs (stage full, accumulators drained) as one cross-CTA arrive
+// each on the even CTA's mbarriers; the MMA commits arrive on both CTAs' mbarriers
+// (multicast). Every wait is bounded in time.
 #include "fir_tc2.cuh"
 #include "tc_common.cuh"
 #include "tc_pair.cuh"
@@ -56,11 +56,13 @@ constexpr int kN = 2 * kNB;              // MMA N
 constexpr int kStepsPerTile = kB / 16;   // K-steps of 16 samples
 constexpr int kStepsPerStage = 2;        // an operand stage holds 32 samples of each block
 constexpr int kStagesPerTile = kStepsPerTile / kStepsPerStage;
-constexpr int kWorkerWarps = 16;
-constexpr int kWorkers = kWorkerWarps * 32;
-constexpr int kMmaWarp = 16;
-constexpr int kTmaWarp = 17;
-constexpr int kThreads = 18 * 32;
+constexpr int kDrainWarps = 16;          // hold the running sums, drain, store
+constexpr int kProducerWarps = 6;        // scan, convert
+constexpr int kProducers = kProducerWarps * 32;
+constexpr int kFirstProducerWarp = kDrainWarps;
+constexpr int kTmaWarp = kDrainWarps + kProducerWarps;
+constexpr int kMmaWarp = kTmaWarp + 1;
+constexpr int kThreads = (kMmaWarp + 1) * 32;
 constexpr int kCols = kN / 4;            // running sums per worker thread
 constexpr int kHGroup = 18;              // MMAs per H accumulation, at most
 constexpr int kRaw = 3;                  // TMA raw-sample ring depth
@@ -108,7 +110,7 @@ __host__ __device__ inline Layout tc2_layout(int num_taps, int stages, int sbufs
 
 // Control block at the start of shared memory (same offsets in both CTAs).
 struct Ctrl {
-    unsigned long long full[kMaxStages];      // even CTA: 32 worker-warp arrivals (both CTAs)
+    unsigned long long full[kMaxStages];      // even CTA: producer-warp arrivals of both CTAs
     unsigned long long empty[kMaxStages];     // both: MMA commit
     unsigned long long raw_full[kRaw];
     unsigned long long raw_empty[kRaw];
@@ -118,12 +120,13 @@ struct Ctrl {
     unsigned long long pempty;                // even CTA: H drained by both
     unsigned long long xfull;                 // both: X of a tile summed
     unsigned long long xempty;                // even CTA: X drained by both
-    unsigned long long reduce[2];             // this CTA's workers, per tile parity
+    unsigned long long sready[4];             // this CTA: the scale of tile k is in ex[k % 4]
     unsigned long long xchg[2];               // the other CTA's maximum has arrived
     unsigned long long teardown;
     uint32_t tmem_base;
     int abort;
-    uint32_t warp_max[2][kWorkerWarps];
+    uint32_t pmax[2][kProducerWarps];
+    int ex[4];
     uint32_t peer_max[2];                     // written by the other CTA
     uint32_t tap_max;
 };
@@ -214,24 +217,26 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
     // ---- setup ------------------------------------------------------------------------------
     if (threadIdx.x == 0) {
         for (int i = 0; i < S; ++i) {
-            mbar_init(smem_u32(&ctl.full[i]), 2 * kWorkerWarps);
+            mbar_init(smem_u32(&ctl.full[i]), kProducerWarps + (rank == 0 ? 1 : 0));
             mbar_init(smem_u32(&ctl.empty[i]), 1);
         }
         for (int i = 0; i < kRaw; ++i) {
             mbar_init(smem_u32(&ctl.raw_full[i]), 1);
-            mbar_init(smem_u32(&ctl.raw_empty[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.raw_empty[i]), kProducerWarps);
         }
         for (int i = 0; i < sbufs; ++i) {
             mbar_init(smem_u32(&ctl.scan_full[i]), 1);
-            mbar_init(smem_u32(&ctl.scan_empty[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.scan_empty[i]), kProducerWarps);
         }
         mbar_init(smem_u32(&ctl.pfull), 1);
-        mbar_init(smem_u32(&ctl.pempty), 2 * kWorkerWarps);
+        mbar_init(smem_u32(&ctl.pempty), kDrainWarps + (rank == 0 ? 1 : 0));
         mbar_init(smem_u32(&ctl.xfull), 1);
-        mbar_init(smem_u32(&ctl.xempty), 2 * kWorkerWarps);
+        mbar_init(smem_u32(&ctl.xempty), kDrainWarps + (rank == 0 ? 1 : 0));
         for (int i = 0; i < 2; ++i) {
-            mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
             mbar_init(smem_u32(&ctl.xchg[i]), 1);
+        }
+        for (int i = 0; i < 4; ++i) {
+            mbar_init(smem_u32(&ctl.sready[i]), 1);
         }
         mbar_init(smem_u32(&ctl.teardown), 1);
         ctl.abort = 0;
@@ -301,17 +306,83 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
     fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    if (warp < kWorkerWarps) {
-        // ---- workers ------------------------------------------------------------------------
+    if (warp < kDrainWarps) {
+        // ---- drain warps: running sums, outputs ----------------------------------------------
         const int quarter = warp & 3;
         const int slice = warp >> 2;                       // columns kCols * slice .. +kCols-1
         const int r = kB - 1 - kRowsPerCta * static_cast<int>(rank) - (quarter * 32 + lane);
         const uint32_t lane_addr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
                                    static_cast<uint32_t>(slice * kCols);
-        const int wtid = threadIdx.x;
-        const uint32_t full0 = map_to(smem_u32(&ctl.full[0]), 0);
-        const uint32_t pempty_lead = map_to(smem_u32(&ctl.pempty), 0);
-        const uint32_t xempty_lead = map_to(smem_u32(&ctl.xempty), 0);
+        float acc[kCols];
+#pragma unroll
+        for (int i = 0; i < kCols; ++i) {
+            acc[i] = 0.0f;
+        }
+        auto drain = [&](uint32_t col) {
+            fence_after();
+#pragma unroll
+            for (int c16 = 0; c16 < kCols / 16; ++c16) {
+                uint32_t t[16];
+                tmem_ld16(lane_addr + col + static_cast<uint32_t>(c16 * 16), t);
+                tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    acc[c16 * 16 + i] += __uint_as_float(t[i]);
+                }
+            }
+            fence_before();
+            __syncwarp();
+        };
+        // Drained-accumulator hand-offs: local arrivals (the odd CTA's are forwarded to the
+        // even CTA by warp 23).
+        auto arrive_lead = [&](unsigned long long* local) {
+            if (lane == 0) {
+                mbar_arrive(smem_u32(local));
+            }
+        };
+        bool ok = true;
+        int g = 0;
+        for (int k = 0; k < my_tiles && ok && !*abort; ++k) {
+            for (int gi = 0; gi < grp.per_tile; ++gi, ++g) {
+                if (!mbar_wait_cluster(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
+                                       abort)) {
+                    ok = false;
+                    break;
+                }
+                drain(0);
+                arrive_lead(&ctl.pempty);
+            }
+            if (!ok ||
+                !mbar_wait_cluster(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull, abort)) {
+                break;
+            }
+            drain(kXCol);
+            arrive_lead(&ctl.xempty);
+            // The tile's sample scale (common to the pair), published by this CTA's producers.
+            if (!mbar_wait_bounded(smem_u32(&ctl.sready[k & 3]), (k >> 2) & 1, fault, kFaultScale,
+                                   abort)) {
+                break;
+            }
+            const int ex = *reinterpret_cast<volatile int*>(&ctl.ex[k & 3]);
+            const int shift = -(ex + eh);
+            const float fa = exp2i(shift / 2);
+            const float fb = exp2i(shift - shift / 2);
+            // Row r of blocks 24 slice .. +23.
+            const long long jb0 = static_cast<long long>(tile_of(k)) * kNB + slice * (kCols / 2);
+#pragma unroll
+            for (int b = 0; b < kCols / 2; ++b) {
+                const long long o = (jb0 + b) * kB + r;
+                if (o < n) {
+                    y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
+                }
+                acc[2 * b] = 0.0f;
+                acc[2 * b + 1] = 0.0f;
+            }
+        }
+    } else if (warp < kFirstProducerWarp + kProducerWarps) {
+        // ---- producers: scales, operand stages -----------------------------------------------
+        const int pw = warp - kFirstProducerWarp;
+        const int ptid = static_cast<int>(threadIdx.x) - kFirstProducerWarp * 32;
         int ex_even = 0;
         int ex_odd = 0;
         uint32_t next_max = 0;
@@ -326,24 +397,21 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
             }
             return 0u;
         };
-        // Tile k's scale: this CTA's workers' maxima, then the other CTA's.
+        // Tile k's scale: this CTA's producers' maxima, then the other CTA's; published to the
+        // drain warps.
         auto reduce_scale = [&](int k, uint32_t m) -> bool {
             m = __reduce_max_sync(0xFFFFFFFFu, m);
             const int rb = k & 1;
             if (lane == 0) {
-                ctl.warp_max[rb][warp] = m;
-                mbar_arrive(smem_u32(&ctl.reduce[rb]));
+                ctl.pmax[rb][pw] = m;
             }
-            if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (k >> 1) & 1, fault,
-                                   kFaultStageEmpty, abort)) {
-                return false;
-            }
+            asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory");
             uint32_t tmax = 0;
 #pragma unroll
-            for (int w = 0; w < kWorkerWarps; ++w) {
-                tmax = max(tmax, ctl.warp_max[rb][w]);
+            for (int w = 0; w < kProducerWarps; ++w) {
+                tmax = max(tmax, ctl.pmax[rb][w]);
             }
-            if (wtid == 0) {
+            if (ptid == 0) {
                 st_cluster_u32(map_to(smem_u32(&ctl.peer_max[rb]), rank ^ 1u), tmax);
                 mbar_arrive_cluster(map_to(smem_u32(&ctl.xchg[rb]), rank ^ 1u));
             }
@@ -352,10 +420,15 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 return false;
             }
             tmax = max(tmax, *reinterpret_cast<volatile uint32_t*>(&ctl.peer_max[rb]));
+            const int ex = scale_exponent(tmax);
             if (k & 1) {
-                ex_odd = scale_exponent(tmax);
+                ex_odd = ex;
             } else {
-                ex_even = scale_exponent(tmax);
+                ex_even = ex;
+            }
+            if (ptid == 0) {
+                ctl.ex[k & 3] = ex;
+                mbar_arrive(smem_u32(&ctl.sready[k & 3]));
             }
             return true;
         };
@@ -372,12 +445,12 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
             const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
             const int quads = min(lay.srows, 2 * lay.rows - r0) * 64;
             uint32_t m = next_max;
-            for (int f = wtid; f < quads; f += kWorkers) {
+            for (int f = ptid; f < quads; f += kProducers) {
                 m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
             }
             const long long tail_row = full_halves - 2 * win0(k) - r0;
-            if (tail_row >= 0 && tail_row * 64 < quads && wtid < 64) {
-                m = max(m, load_pair(full_halves * (kB / 2) + 2 * wtid, n));
+            if (tail_row >= 0 && tail_row * 64 < quads && ptid < 64) {
+                m = max(m, load_pair(full_halves * (kB / 2) + 2 * ptid, n));
             }
             next_max = m;
             __syncwarp();
@@ -421,7 +494,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
             const long long tail_rel = full_blocks - win0(k);
             const int b_tail =
                 tail_rel >= 0 && tail_rel < lay.rows ? static_cast<int>(tail_rel) : -1;
-            for (int f = wtid; f < 2 * half_items; f += kWorkers) {
+            for (int f = ptid; f < 2 * half_items; f += kProducers) {
                 const int h = f >= half_items ? 1 : 0;
                 const int g = f - h * half_items;
                 const int b = g >> 3;
@@ -455,11 +528,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {
-                if (rank == 0) {
-                    mbar_arrive(smem_u32(&ctl.full[slot]));
-                } else {
-                    mbar_arrive_cluster(full0 + static_cast<uint32_t>(slot) * 8u);
-                }
+                mbar_arrive(smem_u32(&ctl.full[slot]));  // forwarded to the even CTA by warp 23
                 mbar_arrive(smem_u32(&ctl.raw_empty[rslot]));
             }
             return true;
@@ -473,11 +542,11 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
             const long long hi_s = end_s < n ? end_s : n;
             const long long npairs = hi_s > lo_s ? (hi_s - lo_s + 1) / 2 : 0;
             uint32_t m = 0;
-            for (long long base = 0; base < npairs; base += 8 * kWorkers) {
+            for (long long base = 0; base < npairs; base += 8 * kProducers) {
                 uint32_t part[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const long long idx = base + wtid + i * kWorkers;
+                    const long long idx = base + ptid + i * kProducers;
                     part[i] = idx < npairs ? load_pair(lo_s + 2 * idx, hi_s) : 0u;
                 }
 #pragma unroll
@@ -487,91 +556,11 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
             }
             ok = reduce_scale(0, m);
         }
-        for (int v = 0; v < S && v < my_steps && ok; ++v) {
+        for (int v = 0; v < my_steps && ok && !*abort; ++v) {
             ok = produce(v);
         }
-        float acc[kCols];
-#pragma unroll
-        for (int i = 0; i < kCols; ++i) {
-            acc[i] = 0.0f;
-        }
-        auto drain = [&](uint32_t col) {
-            fence_after();
-#pragma unroll
-            for (int c16 = 0; c16 < kCols / 16; ++c16) {
-                uint32_t t[16];
-                tmem_ld16(lane_addr + col + static_cast<uint32_t>(c16 * 16), t);
-                tmem_wait_ld();
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    acc[c16 * 16 + i] += __uint_as_float(t[i]);
-                }
-            }
-            fence_before();
-            __syncwarp();
-        };
-        int gi = 0;
-        for (int u = 0; u < my_steps && ok && !*abort; ++u) {
-            const int k = u / kStagesPerTile;
-            const int st = u % kStagesPerTile;
-            // Drain the H groups whose last K-step lies in stage u.
-            while (gi < grp.per_tile &&
-                   (grp.gpk == 1 ? min(kStepsPerTile, (gi + 1) * grp.ksg) - 1 : gi / grp.gpk) <
-                       kStepsPerStage * (st + 1)) {
-                const int g = k * grp.per_tile + gi;
-                if (!mbar_wait_cluster(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
-                                       abort)) {
-                    ok = false;
-                    break;
-                }
-                drain(0);
-                if (lane == 0) {
-                    if (rank == 0) {
-                        mbar_arrive(smem_u32(&ctl.pempty));
-                    } else {
-                        mbar_arrive_cluster(pempty_lead);
-                    }
-                }
-                ++gi;
-            }
-            if (!ok) {
-                break;
-            }
-            if (st == kStagesPerTile - 1) {
-                if (!mbar_wait_cluster(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull,
-                                       abort)) {
-                    break;
-                }
-                drain(kXCol);
-                if (lane == 0) {
-                    if (rank == 0) {
-                        mbar_arrive(smem_u32(&ctl.xempty));
-                    } else {
-                        mbar_arrive_cluster(xempty_lead);
-                    }
-                }
-                // Scale and store this thread's outputs: row r of blocks 24 slice .. +23.
-                const int shift = -(((k & 1) ? ex_odd : ex_even) + eh);
-                const float fa = exp2i(shift / 2);
-                const float fb = exp2i(shift - shift / 2);
-                const long long jb0 = static_cast<long long>(tile_of(k)) * kNB + slice * (kCols / 2);
-#pragma unroll
-                for (int b = 0; b < kCols / 2; ++b) {
-                    const long long o = (jb0 + b) * kB + r;
-                    if (o < n) {
-                        y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
-                    }
-                    acc[2 * b] = 0.0f;
-                    acc[2 * b + 1] = 0.0f;
-                }
-                gi = 0;
-            }
-            if (u + S < my_steps) {
-                ok = produce(u + S);
-            }
-        }
     } else if (warp == kTmaWarp) {
-        // ---- copy issuer (warp 17, one thread) ----------------------------------------------
+        // ---- copy issuer (warp 22, one thread) ----------------------------------------------
         // Scan slice v + sbufs - 2 once slice v - 2 is read, then raw stage v + kRaw once stage
         // v is converted (the first ones were issued during setup).
         if (lane == 0) {
@@ -600,8 +589,44 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 }
             }
         }
-    } else if (rank == 0 && lane == 0) {
-        // ---- MMA issuer for the pair (even CTA, warp 16, one thread) ------------------------
+    } else if (warp == kMmaWarp && rank == 1 && lane < 3) {
+        // ---- forwarders (odd CTA, warp 23, lanes 0-2) ---------------------------------------
+        // Each of the odd CTA's hand-off sequences (stage full, H drained, X drained) collects
+        // its own warps on the local copy of the barrier; one lane per sequence turns each
+        // completed phase into ONE release-arrive on the even CTA's barrier, instead of one
+        // cross-CTA arrive per warp. Independent lanes, so no sequence waits behind another.
+        if (lane == 0) {
+            const uint32_t lead = map_to(smem_u32(&ctl.full[0]), 0);
+            for (int v = 0; v < my_steps && !*abort; ++v) {
+                const int slot = v % S;
+                if (!mbar_wait_bounded(smem_u32(&ctl.full[slot]), (v / S) & 1, fault,
+                                       kFaultStageFull, abort)) {
+                    break;
+                }
+                mbar_arrive_cluster(lead + static_cast<uint32_t>(slot) * 8u);
+            }
+        } else if (lane == 1) {
+            const uint32_t lead = map_to(smem_u32(&ctl.pempty), 0);
+            const int groups = my_tiles * grp.per_tile;
+            for (int g = 0; g < groups && !*abort; ++g) {
+                if (!mbar_wait_bounded(smem_u32(&ctl.pempty), g & 1, fault, kFaultAccumEmpty,
+                                       abort)) {
+                    break;
+                }
+                mbar_arrive_cluster(lead);
+            }
+        } else {
+            const uint32_t lead = map_to(smem_u32(&ctl.xempty), 0);
+            for (int k = 0; k < my_tiles && !*abort; ++k) {
+                if (!mbar_wait_bounded(smem_u32(&ctl.xempty), k & 1, fault, kFaultAccumEmpty,
+                                       abort)) {
+                    break;
+                }
+                mbar_arrive_cluster(lead);
+            }
+        }
+    } else if (warp == kMmaWarp && rank == 0 && lane == 0) {
+        // ---- MMA issuer for the pair (even CTA, warp 23, one thread) ------------------------
         // Lean issue loop: per MMA one descriptor step and the MMA. The strip descriptor of
         // (K-step st, chunk c) starts 2 st + 32 (C - c) core matrices in, the sample descriptor
         // 2 (C - c) rows into the stage's planes; each next chunk is 256 (strip) and 2 (planes)
