@@ -41,17 +41,36 @@ constexpr int kGuard = 16;  // zero samples in front of the tile: the last windo
 struct Layout {
     uint32_t taps_off;   // (h, h) pairs, K entries
     uint32_t tile_off;   // guard + tile samples
+    uint32_t raw_off;    // integer input formats: the tile's raw components as copied
     uint32_t bytes;
 };
 
-__host__ __device__ inline Layout plain_layout(int num_taps)
+// Bytes per sample of each input format (rfx_sample_format): cf32, ci16, ci8.
+__host__ __device__ constexpr uint32_t sample_bytes(int fmt) { return fmt == 0 ? 8u : fmt == 1 ? 4u : 2u; }
+
+__host__ __device__ inline Layout plain_layout(int num_taps, int fmt = 0)
 {
     Layout l;
     l.taps_off = 16;
     l.tile_off = (l.taps_off + 8u * static_cast<uint32_t>(num_taps) + 15u) & ~15u;
-    const uint32_t tile_samples = kGuard + kTile + static_cast<uint32_t>(num_taps) + 2u;
-    l.bytes = l.tile_off + 8u * tile_samples;
+    const uint32_t tile_samples = kGuard + kTile + static_cast<uint32_t>(num_taps) + 8u;
+    l.raw_off = (l.tile_off + 8u * tile_samples + 15u) & ~15u;
+    l.bytes = l.raw_off + (fmt == 0 ? 0u : sample_bytes(fmt) * (kTile + static_cast<uint32_t>(num_taps) + 8u));
     return l;
+}
+
+// Sample i of an integer-format input, decoded as the project's SigMF reader does
+// (src/io.cpp:110-124): component x (1/32768) for ci16_le, x (1/128) for ci8.
+template <int kFmt>
+__device__ __forceinline__ f32x2 decode_sample(const void* raw, long long i)
+{
+    if (kFmt == 1) {
+        const short2 v = static_cast<const short2*>(raw)[i];
+        return pack2(static_cast<float>(v.x) * (1.0f / 32768.0f),
+                     static_cast<float>(v.y) * (1.0f / 32768.0f));
+    }
+    const char2 v = static_cast<const char2*>(raw)[i];
+    return pack2(static_cast<float>(v.x) * (1.0f / 128.0f), static_cast<float>(v.y) * (1.0f / 128.0f));
 }
 
 // Nine taps 9g + q (q < nq) against output window blocks: cur = S_g, nxt = S_{g+1}.
@@ -116,14 +135,17 @@ __device__ __forceinline__ void compute_outputs(f32x2 (&acc)[kR], const f32x2* t
 
 }  // namespace
 
-// One tile of one capture. Shared by the single-capture and the batched kernels.
-__device__ __forceinline__ void fir_plain_tile(const float2* __restrict__ x,
+// One tile of one capture. Shared by the single-capture and the batched kernels. kFmt: the
+// input's sample format (0 cf32; 1 ci16, 2 ci8: decoded into cf32 in shared memory).
+template <int kFmt = 0>
+__device__ __forceinline__ void fir_plain_tile(const void* __restrict__ xv,
                                                const float* __restrict__ taps,
                                                float2* __restrict__ y, long long n,
                                                int num_taps, long long tile_index,
                                                unsigned char* smem)
 {
-    const Layout lay = plain_layout(num_taps);
+    const float2* x = static_cast<const float2*>(xv);
+    const Layout lay = plain_layout(num_taps, kFmt);
     const uint32_t sbase = smem_u32(smem);
     const uint32_t bar = sbase;  // mbarrier at offset 0
     f32x2* taps2 = reinterpret_cast<f32x2*>(smem + lay.taps_off);
@@ -132,8 +154,10 @@ __device__ __forceinline__ void fir_plain_tile(const float2* __restrict__ x,
     const int tid = threadIdx.x;
 
     const long long t0 = tile_index * kTile;
-    const long long base = (t0 - (num_taps - 1)) & ~1ll;      // even: 16-byte aligned copy
-    const int tile_len = static_cast<int>(t0 + kTile - base); // even
+    // First staged sample: a multiple of 2 (cf32) or 8 (integer formats) so that the copy
+    // starts on a 16-byte boundary; the length is then a multiple of 16 bytes too.
+    const long long base = (t0 - (num_taps - 1)) & (kFmt == 0 ? ~1ll : ~7ll);
+    const int tile_len = static_cast<int>(t0 + kTile - base);
     const bool interior = base >= 0 && t0 + kTile <= n;
 
     if (tid == 0) {
@@ -142,9 +166,14 @@ __device__ __forceinline__ void fir_plain_tile(const float2* __restrict__ x,
     }
     __syncthreads();
     if (interior && tid == 0) {
-        const uint32_t bytes = 8u * static_cast<uint32_t>(tile_len);
+        const uint32_t bytes = sample_bytes(kFmt) * static_cast<uint32_t>(tile_len);
         mbar_arrive_expect_tx(bar, bytes);
-        bulk_g2s(smem_u32(tile), x + base, bytes, bar);
+        if (kFmt == 0) {
+            bulk_g2s(smem_u32(tile), x + base, bytes, bar);
+        } else {
+            bulk_g2s(sbase + lay.raw_off,
+                     static_cast<const unsigned char*>(xv) + sample_bytes(kFmt) * base, bytes, bar);
+        }
     }
     // Taps (duplicated into both lanes) and the guard while the copy is in flight.
     for (int k = tid; k < num_taps; k += kThreads) {
@@ -159,8 +188,12 @@ __device__ __forceinline__ void fir_plain_tile(const float2* __restrict__ x,
             const long long m = base + i;
             f32x2 v = 0ull;
             if (m >= 0 && m < n) {
-                const float2 s = x[m];
-                v = pack2(s.x, s.y);
+                if (kFmt == 0) {
+                    const float2 s = x[m];
+                    v = pack2(s.x, s.y);
+                } else {
+                    v = decode_sample<kFmt>(xv, m);
+                }
             }
             tile[i] = v;
         }
@@ -169,6 +202,14 @@ __device__ __forceinline__ void fir_plain_tile(const float2* __restrict__ x,
     bool ok = true;
     if (interior) {
         ok = mbar_wait_bounded(bar, 0, &g_fault_fir_plain, kFaultTileLoad, nullptr);
+        if (kFmt != 0) {
+            // Decode the staged components into the sample tile.
+            const unsigned char* raw = smem + lay.raw_off;
+            for (int i = tid; i < tile_len; i += kThreads) {
+                tile[i] = decode_sample<kFmt>(raw, i);
+            }
+            __syncthreads();
+        }
     }
 
     const long long n0 = t0 + static_cast<long long>(kR) * tid;
@@ -250,6 +291,16 @@ fir_plain_caps_kernel(const __grid_constant__ PlainCaps caps)
                    block - caps.tile0[lo], smem);
 }
 
+// Integer I/Q input (ci16, ci8), decoded in the load stage.
+template <int kFmt>
+__global__ void __launch_bounds__(kThreads, 3)
+fir_plain_fmt_kernel(const void* __restrict__ x, const float* __restrict__ taps,
+                     float2* __restrict__ y, long long n, int num_taps)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    fir_plain_tile<kFmt>(x, taps, y, n, num_taps, blockIdx.x, smem);
+}
+
 size_t fir_plain_smem_bytes(int num_taps) { return plain_layout(num_taps).bytes; }
 
 static cudaError_t ensure_smem_attr(const void* fn, size_t bytes)
@@ -307,6 +358,33 @@ cudaError_t fir_plain_batched_launch(const PlainBatch& batch, int count, const f
     }
     const dim3 grid(static_cast<unsigned>((longest + kTile - 1) / kTile), count);
     fir_plain_batched_kernel<<<grid, kThreads, bytes, stream>>>(batch, taps, num_taps);
+    return cudaGetLastError();
+}
+
+cudaError_t fir_plain_launch_format(int format, const void* x, const float* taps, void* y,
+                                    long long n, int num_taps, cudaStream_t stream)
+{
+    if (format == 0) {
+        return fir_plain_launch(x, taps, y, n, num_taps, stream);
+    }
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    const size_t bytes = plain_layout(num_taps, format).bytes;
+    const void* fn = format == 1 ? reinterpret_cast<const void*>(fir_plain_fmt_kernel<1>)
+                                 : reinterpret_cast<const void*>(fir_plain_fmt_kernel<2>);
+    cudaError_t err = ensure_smem_attr(fn, bytes);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    const long long tiles = (n + kTile - 1) / kTile;
+    if (format == 1) {
+        fir_plain_fmt_kernel<1><<<static_cast<unsigned>(tiles), kThreads, bytes, stream>>>(
+            x, taps, static_cast<float2*>(y), n, num_taps);
+    } else {
+        fir_plain_fmt_kernel<2><<<static_cast<unsigned>(tiles), kThreads, bytes, stream>>>(
+            x, taps, static_cast<float2*>(y), n, num_taps);
+    }
     return cudaGetLastError();
 }
 

@@ -37,6 +37,11 @@ cudaError_t fir_plain_launch(const void* x, const float* taps, void* y, long lon
                              int num_taps, cudaStream_t stream);
 cudaError_t fir_plain_batched_launch(const PlainBatch& batch, int count, const float* taps,
                                      int num_taps, cudaStream_t stream);
+// The FIR of integer I/Q input decoded in the load stage: format 1 = ci16 (components x / 32768),
+// 2 = ci8 (x / 128), 0 = cf32 (fir_plain_launch). Same bits as decoding first.
+cudaError_t fir_plain_launch_format(int format, const void* x, const float* taps, void* y,
+                                    long long n, int num_taps, cudaStream_t stream);
+
 // Up to kPlainCapsMax captures (non-empty), each with its own taps, in one launch.
 cudaError_t fir_plain_caps_launch(const PlainCaps& caps, cudaStream_t stream);
 cudaError_t fir_plain_take_fault(unsigned int* code);

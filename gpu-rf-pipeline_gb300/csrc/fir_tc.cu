@@ -89,14 +89,17 @@ struct Layout {
     uint32_t pitch;      // bytes per plane (2 rows * 16 B per block + 16)
     uint32_t split;      // bytes of one split (hi or lo) of a stage: 2 planes
     uint32_t stage;      // bytes per operand stage: hi + lo
-    uint32_t raw;        // bytes per raw stage: rows * 16 samples * 8 B
-    uint32_t scan;       // bytes per scan slice: srows * 128 samples * 8 B
+    uint32_t raw_tx;     // bytes one raw copy delivers: rows * 32 components * es
+    uint32_t scan_tx;    // bytes one scan copy delivers: srows * 256 components * es
+    uint32_t raw;        // raw stage pitch (raw_tx rounded up to 128 B)
+    uint32_t scan;       // scan slice pitch (scan_tx rounded up to 128 B)
     int tcount;          // core matrices of the tap strip
     int sbufs;           // scan slice buffers
     uint32_t taps_hi, taps_lo, raw0, scan0, stages0, bytes;
 };
 
-__host__ __device__ inline Layout tc_layout(int num_taps, int stages, int sbufs)
+// es: bytes per input component (4 cf32, 2 ci16, 1 ci8).
+__host__ __device__ inline Layout tc_layout(int num_taps, int stages, int sbufs, int es = 4)
 {
     Layout l;
     l.sbufs = sbufs;
@@ -106,8 +109,11 @@ __host__ __device__ inline Layout tc_layout(int num_taps, int stages, int sbufs)
     l.pitch = static_cast<uint32_t>(2 * l.rows) * 16u + 16u;
     l.split = 2u * l.pitch;
     l.stage = 2u * l.split;
-    l.raw = static_cast<uint32_t>(l.rows) * 128u;
-    l.scan = static_cast<uint32_t>(l.srows) * 1024u;
+    // Each copy's destination 128-byte aligned.
+    l.raw_tx = static_cast<uint32_t>(l.rows) * 32u * static_cast<uint32_t>(es);
+    l.scan_tx = static_cast<uint32_t>(l.srows) * 256u * static_cast<uint32_t>(es);
+    l.raw = (l.raw_tx + 127u) & ~127u;
+    l.scan = (l.scan_tx + 127u) & ~127u;
     l.tcount = 16 * l.C + 31;
     l.taps_hi = 1024;
     l.taps_lo = l.taps_hi + 128u * static_cast<uint32_t>(l.tcount);
@@ -185,19 +191,89 @@ __device__ __forceinline__ void h_group_range(const HGroups& g, int P, int gi, i
     }
 }
 
+__host__ __device__ constexpr int component_bytes(int fmt) { return fmt == 0 ? 4 : fmt == 1 ? 2 : 1; }
+
+// Sample formats of x: 0 = cf32; 1 = ci16 and 2 = ci8, whose components decode as the
+// project's SigMF reader converts them (src/io.cpp:110-148): v / 32768 and v / 128, both exact
+// in float32, so a decoded run has the bits of a run over the converted samples.
+__device__ __forceinline__ float4 decode_ci16x2(uint2 w)
+{
+    constexpr float k = 1.0f / 32768.0f;
+    return make_float4(static_cast<float>(static_cast<int>(w.x << 16) >> 16) * k,
+                       static_cast<float>(static_cast<int>(w.x) >> 16) * k,
+                       static_cast<float>(static_cast<int>(w.y << 16) >> 16) * k,
+                       static_cast<float>(static_cast<int>(w.y) >> 16) * k);
+}
+
+__device__ __forceinline__ float4 decode_ci8x2(uint32_t w)
+{
+    constexpr float k = 1.0f / 128.0f;
+    return make_float4(static_cast<float>(static_cast<int>(w << 24) >> 24) * k,
+                       static_cast<float>(static_cast<int>(w << 16) >> 24) * k,
+                       static_cast<float>(static_cast<int>(w << 8) >> 24) * k,
+                       static_cast<float>(static_cast<int>(w) >> 24) * k);
+}
+
+// Samples s, s + 1 (s even) from shared memory holding components in format fmt at `addr`
+// (the first of the pair): re0, im0, re1, im1.
+__device__ __forceinline__ float4 lds_pair(uint32_t addr, int fmt)
+{
+    if (fmt == 0) {
+        return lds128(addr);
+    }
+    if (fmt == 1) {
+        uint2 w;
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(w.x), "=r"(w.y) : "r"(addr) : "memory");
+        return decode_ci16x2(w);
+    }
+    uint32_t w;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(addr) : "memory");
+    return decode_ci8x2(w);
+}
+
+// Samples s, s + 1 of x (s even, s + 1 < n), and sample s alone, from global memory.
+__device__ __forceinline__ float4 ldg_pair(const void* x, int fmt, long long s)
+{
+    if (fmt == 0) {
+        return __ldg(reinterpret_cast<const float4*>(static_cast<const float2*>(x) + s));
+    }
+    if (fmt == 1) {
+        return decode_ci16x2(__ldg(reinterpret_cast<const uint2*>(static_cast<const short2*>(x) + s)));
+    }
+    return decode_ci8x2(__ldg(reinterpret_cast<const unsigned int*>(static_cast<const char2*>(x) + s)));
+}
+
+__device__ __forceinline__ float2 ldg_one(const void* x, int fmt, long long s)
+{
+    if (fmt == 0) {
+        return __ldg(static_cast<const float2*>(x) + s);
+    }
+    if (fmt == 1) {
+        const short2 v = __ldg(static_cast<const short2*>(x) + s);
+        return make_float2(static_cast<float>(v.x) * (1.0f / 32768.0f),
+                           static_cast<float>(v.y) * (1.0f / 32768.0f));
+    }
+    const char2 v = __ldg(static_cast<const char2*>(x) + s);
+    return make_float2(static_cast<float>(v.x) * (1.0f / 128.0f),
+                       static_cast<float>(v.y) * (1.0f / 128.0f));
+}
+
 }  // namespace
 
-// xmap: x as rows of 256 floats (one block), boxes of 32 floats x `rows` (one K-step's samples
-// of a tile window). smap: the same rows, boxes of 256 floats x `srows` (a scan slice).
+// xmap: x as rows of 256 components (one block), boxes of 32 components x `rows` (one K-step's
+// samples of a tile window). smap: the same rows, boxes of 256 components x `srows` (a scan
+// slice). fmt: x's sample format (0 cf32, 1 ci16, 2 ci8); the copies move the components as
+// stored and the producers decode them.
 template <int S>
 __global__ void __launch_bounds__(kThreads, 1)
 fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap smap,
-              const float2* __restrict__ x, const float* __restrict__ taps,
-              float2* __restrict__ y, long long n, int num_taps, int num_tiles, int sbufs)
+              const void* __restrict__ x, const float* __restrict__ taps,
+              float2* __restrict__ y, long long n, int num_taps, int num_tiles, int sbufs, int fmt)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
-    const Layout lay = tc_layout(num_taps, S, sbufs);
+    const int es = component_bytes(fmt);
+    const Layout lay = tc_layout(num_taps, S, sbufs, es);
     const int C = lay.C;
     const int P = C + 1;                       // chunks per K-step
     const HGroups grp = h_groups(P, S);
@@ -249,7 +325,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
     auto issue_scan = [&](int q) {
         const int kn = q / kStagesPerTile + 1;
         const uint32_t bar = smem_u32(&ctl.scan_full[q % sbufs]);
-        mbar_arrive_expect_tx(bar, lay.scan);
+        mbar_arrive_expect_tx(bar, lay.scan_tx);
         tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(q % sbufs) * lay.scan, &smap,
                     0, tile_of(kn) * kNB - C + (q % kStagesPerTile) * lay.srows, bar);
     };
@@ -258,7 +334,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
     if (threadIdx.x == 0) {
         for (int u = 0; u < kRaw && u < my_steps; ++u) {
             const uint32_t bar = smem_u32(&ctl.raw_full[u]);
-            mbar_arrive_expect_tx(bar, lay.raw);
+            mbar_arrive_expect_tx(bar, lay.raw_tx);
             tma_load_2d(sbase + lay.raw0 + u * lay.raw, &xmap, 32 * (u % kStagesPerTile),
                         tile_of(u / kStagesPerTile) * kNB - C, bar);
         }
@@ -387,10 +463,10 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
         // Max of |samples| in [s, s + 2) clipped to hi_s (plain loads, for the partial block).
         auto load_pair = [&](long long s, long long hi_s) -> uint32_t {
             if (s + 1 < hi_s) {
-                return absmax4(__ldg(reinterpret_cast<const float4*>(x + s)));
+                return absmax4(ldg_pair(x, fmt, s));
             }
             if (s < hi_s) {
-                const float2 w2 = __ldg(x + s);
+                const float2 w2 = ldg_one(x, fmt, s);
                 return max(absbits(w2.x), absbits(w2.y));
             }
             return 0u;
@@ -433,11 +509,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             const long long j0 = static_cast<long long>(tile_of(k)) * kNB;
             const int r0 = (q % kStagesPerTile) * lay.srows;
             const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
-            const int quads = min(lay.srows, lay.rows - r0) * 64;   // float4 in the window
+            const int quads = min(lay.srows, lay.rows - r0) * 64;   // sample pairs in the window
+            const uint32_t pair_bytes = 4u * static_cast<uint32_t>(es);
             uint32_t m = next_max;
 #pragma unroll 4
             for (int f = ptid; f < quads; f += kProducers) {
-                m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
+                m = max(m, absmax4(lds_pair(buf + static_cast<uint32_t>(f) * pair_bytes, fmt)));
             }
             const long long tail_row = full_blocks - (j0 - C) - r0;
             if (tail_row >= 0 && tail_row * 64 < quads && ptid < 64) {
@@ -477,7 +554,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             }
             const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
             const uint32_t raw = sbase + lay.raw0 + static_cast<uint32_t>(rslot) * lay.raw;
-            const int items = lay.rows * 8;  // float4 (two samples) per window row
+            const int items = lay.rows * 8;  // sample pairs: 8 per window row
+            const uint32_t pair_bytes = 4u * static_cast<uint32_t>(es);
             // Window row of the input's last, partial block (outside the tensor maps), if any.
             const long long tail_rel = full_blocks - (j0 - C);
             const int b_tail = tail_rel >= 0 && tail_rel < lay.rows ? static_cast<int>(tail_rel) : -1;
@@ -487,15 +565,16 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                 const int q = f & 7;
                 float4 v4;
                 if (b != b_tail) {
-                    v4 = lds128(raw + static_cast<uint32_t>(f) * 16u);  // zero outside [0, n)
+                    // zero outside [0, n)
+                    v4 = lds_pair(raw + static_cast<uint32_t>(f) * pair_bytes, fmt);
                 } else {
                     // The partial block: plain loads.
                     const long long sidx = full_blocks * kB + 16 * st + 2 * q;
                     v4 = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (sidx + 1 < n) {
-                        v4 = __ldg(reinterpret_cast<const float4*>(x + sidx));
+                        v4 = ldg_pair(x, fmt, sidx);
                     } else if (sidx < n) {
-                        const float2 w2 = __ldg(x + sidx);
+                        const float2 w2 = ldg_one(x, fmt, sidx);
                         v4.x = w2.x;
                         v4.y = w2.y;
                     }
@@ -526,7 +605,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                     }
                     const int vn = v + kRaw;
                     const uint32_t bar = smem_u32(&ctl.raw_full[rslot]);
-                    mbar_arrive_expect_tx(bar, lay.raw);
+                    mbar_arrive_expect_tx(bar, lay.raw_tx);
                     tma_load_2d(raw, &xmap, 32 * (vn % kStagesPerTile),
                                 tile_of(vn / kStagesPerTile) * kNB - C, bar);
                 }
@@ -715,10 +794,11 @@ bool fir_tc_supported(int num_taps)
 }
 
 template <int S>
-static cudaError_t launch_stages(const void* x, const float* taps, void* y, long long n,
+static cudaError_t launch_stages(int fmt, const void* x, const float* taps, void* y, long long n,
                                  int num_taps, int sbufs, cudaStream_t stream)
 {
-    const Layout lay = tc_layout(num_taps, S, sbufs);
+    const int es = component_bytes(fmt);
+    const Layout lay = tc_layout(num_taps, S, sbufs, es);
     int device = 0;
     cudaError_t err = cudaGetDevice(&device);
     if (err != cudaSuccess) {
@@ -750,13 +830,13 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
     if (err != cudaSuccess) {
         return err;
     }
-    // x viewed as rows of 256 floats (one 128-sample block per row), full blocks only; boxes
-    // of 32 floats (16 samples) by the tile's window rows.
+    // x viewed as rows of 256 components (one 128-sample block per row), full blocks only;
+    // boxes of 32 components (16 samples) by the tile's window rows.
     CUtensorMap map;
     CUtensorMap smap;
-    err = encode_rows_f32(&map, x, n / kB, 2 * kB, 32, static_cast<uint32_t>(lay.rows));
+    err = encode_rows(&map, x, es, n / kB, 2 * kB, 32, static_cast<uint32_t>(lay.rows));
     if (err == cudaSuccess) {
-        err = encode_rows_f32(&smap, x, n / kB, 2 * kB, 2 * kB, static_cast<uint32_t>(lay.srows));
+        err = encode_rows(&smap, x, es, n / kB, 2 * kB, 2 * kB, static_cast<uint32_t>(lay.srows));
     }
     if (err != cudaSuccess) {
         return err;
@@ -765,9 +845,28 @@ static cudaError_t launch_stages(const void* x, const float* taps, void* y, long
     const int tiles = static_cast<int>((blocks + kNB - 1) / kNB);
     const int grid = tiles < sms ? tiles : sms;
     fir_tc_kernel<S><<<grid, kThreads, bytes, stream>>>(
-        map, smap, static_cast<const float2*>(x), taps, static_cast<float2*>(y), n, num_taps,
-        tiles, sbufs);
+        map, smap, x, taps, static_cast<float2*>(y), n, num_taps, tiles, sbufs, fmt);
     return cudaGetLastError();
+}
+
+// The single-CTA form over x in format fmt (n >= one block).
+static cudaError_t launch_single(int fmt, const void* x, const float* taps, void* y, long long n,
+                                 int num_taps, int max_stages, cudaStream_t stream)
+{
+    const int es = component_bytes(fmt);
+    // The deep scan ring first (it hides the scan copies' latency), then the most stages.
+    for (int sbufs = kScanBufsMax; sbufs >= 2; sbufs -= 2) {
+        if (max_stages >= 6 && tc_layout(num_taps, 6, sbufs, es).bytes <= 227u * 1024u) {
+            return launch_stages<6>(fmt, x, taps, y, n, num_taps, sbufs, stream);
+        }
+        if (max_stages >= 4 && tc_layout(num_taps, 4, sbufs, es).bytes <= 227u * 1024u) {
+            return launch_stages<4>(fmt, x, taps, y, n, num_taps, sbufs, stream);
+        }
+        if (tc_layout(num_taps, 2, sbufs, es).bytes <= 227u * 1024u) {
+            return launch_stages<2>(fmt, x, taps, y, n, num_taps, sbufs, stream);
+        }
+    }
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n, int num_taps,
@@ -786,19 +885,30 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
         // Shorter than one block: the tensor map would be empty; the plain kernel is exact.
         return fir_plain_launch(x, taps, y, n, num_taps, stream);
     }
-    // The deep scan ring first (it hides the scan copies' latency), then the most stages.
-    for (int sbufs = kScanBufsMax; sbufs >= 2; sbufs -= 2) {
-        if (config.stages >= 6 && tc_layout(num_taps, 6, sbufs).bytes <= 227u * 1024u) {
-            return launch_stages<6>(x, taps, y, n, num_taps, sbufs, stream);
-        }
-        if (config.stages >= 4 && tc_layout(num_taps, 4, sbufs).bytes <= 227u * 1024u) {
-            return launch_stages<4>(x, taps, y, n, num_taps, sbufs, stream);
-        }
-        if (tc_layout(num_taps, 2, sbufs).bytes <= 227u * 1024u) {
-            return launch_stages<2>(x, taps, y, n, num_taps, sbufs, stream);
-        }
+    return launch_single(0, x, taps, y, n, num_taps, config.stages, stream);
+}
+
+cudaError_t fir_tc_launch_format(int format, const void* x, const float* taps, void* y,
+                                 long long n, int num_taps, TcConfig config, cudaStream_t stream)
+{
+    if (format == 0) {
+        return fir_tc_launch(x, taps, y, n, num_taps, config, stream);
     }
-    return cudaErrorInvalidValue;
+    if (format != 1 && format != 2) {
+        return cudaErrorInvalidValue;
+    }
+    if (n <= 0) {
+        return cudaSuccess;
+    }
+    if (!fir_tc_supported(num_taps)) {
+        return cudaErrorInvalidValue;
+    }
+    if (n < kB) {
+        return fir_plain_launch_format(format, x, taps, y, n, num_taps, stream);
+    }
+    // Integer input runs in the single-CTA form, whichever form the tuner chose for cf32.
+    return launch_single(format, x, taps, y, n, num_taps,
+                         config.tile_blocks == kTcPairTile ? 6 : config.stages, stream);
 }
 
 long long fir_tc_tile_outputs(int num_taps, long long n, TcConfig config)
@@ -810,6 +920,14 @@ long long fir_tc_tile_outputs(int num_taps, long long n, TcConfig config)
         return 96LL * 256;
     }
     return n < kB ? 1 : static_cast<long long>(kNB) * kB;
+}
+
+long long fir_tc_tile_outputs_format(int format, int num_taps, long long n, TcConfig config)
+{
+    if (format == 0) {
+        return fir_tc_tile_outputs(num_taps, n, config);
+    }
+    return n <= 0 || n < kB || !fir_tc_supported(num_taps) ? 1 : static_cast<long long>(kNB) * kB;
 }
 
 cudaError_t fir_tc_take_fault(unsigned int* code)

@@ -25,6 +25,14 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
                           TcConfig config, cudaStream_t stream);
 cudaError_t fir_tc_take_fault(unsigned int* code);
 
+// The same FIR over integer I/Q input decoded in the load stage (format 1 = ci16, 2 = ci8; 0 =
+// cf32, fir_tc_launch): the copies move the stored components, the producers convert them as
+// the project's SigMF reader does. Results have the bits of fir_tc_launch over the converted
+// samples in the single-CTA form (the form integer input always takes).
+cudaError_t fir_tc_launch_format(int format, const void* x, const float* taps, void* y,
+                                 long long n, int num_taps, TcConfig config, cudaStream_t stream);
+long long fir_tc_tile_outputs_format(int format, int num_taps, long long n, TcConfig config);
+
 // Outputs per tile of the form fir_tc_launch picks for (num_taps, n, config): tiles start at
 // multiples of this, and each tile's results depend only on the samples from one tile before
 // its start to its end (its window reaches back C blocks, C * 128 <= 3456 < one tile), so a

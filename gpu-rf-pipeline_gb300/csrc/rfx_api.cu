@@ -115,6 +115,29 @@ int resolve_fir_impl(int impl, int num_taps, int64_t n)
     return impl;
 }
 
+size_t format_sample_bytes(int format) { return format == RFX_FORMAT_CF32 ? 8 : format == RFX_FORMAT_CI16 ? 4 : 2; }
+
+int check_format(int format)
+{
+    if (format < RFX_FORMAT_CF32 || format > RFX_FORMAT_CI8) {
+        return fail(RFX_ERR_INVALID, "fir: unknown sample format %d", format);
+    }
+    return RFX_OK;
+}
+
+int launch_fir_format(int impl, int format, const void* x, const float* taps, void* y, int64_t n,
+                      int num_taps, cudaStream_t stream)
+{
+    cudaError_t err;
+    if (impl == RFX_FIR_TC) {
+        err = rfx::fir_tc_launch_format(format, x, taps, y, n, num_taps,
+                                        rfx::tuned_fir_tc_config(num_taps, n), stream);
+        return err == cudaSuccess ? RFX_OK : cuda_fail(err, "fir_tc_launch_format");
+    }
+    err = rfx::fir_plain_launch_format(format, x, taps, y, n, num_taps, stream);
+    return err == cudaSuccess ? RFX_OK : cuda_fail(err, "fir_plain_launch_format");
+}
+
 int launch_fir(int impl, const void* x, const float* taps, void* y, int64_t n, int num_taps,
                cudaStream_t stream)
 {
@@ -257,6 +280,20 @@ int rfx_fir_launch(int impl, const void* x, const float* taps, void* y, int64_t 
     }
     return launch_fir(resolve_fir_impl(impl, num_taps, num_samples), x, taps, y, num_samples,
                       num_taps, stream);
+}
+
+int rfx_fir_launch_format(int impl, int format, const void* x, const float* taps, void* y,
+                          int64_t num_samples, int num_taps, cudaStream_t stream)
+{
+    int rc = check_format(format);
+    if (rc == RFX_OK) {
+        rc = check_fir_args(impl, x, taps, y, num_samples, num_taps);
+    }
+    if (rc != RFX_OK || num_samples == 0) {
+        return rc;
+    }
+    return launch_fir_format(resolve_fir_impl(impl, num_taps, num_samples), format, x, taps, y,
+                             num_samples, num_taps, stream);
 }
 
 int rfx_fir_device(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
@@ -632,18 +669,29 @@ extern "C" {
 int rfx_fir_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
                  int num_taps, int block, void* y_iq, rfx_bench* bench)
 {
+    return rfx_fir_host_format(impl, RFX_FORMAT_CF32, x_iq, num_samples, taps, num_taps, block,
+                               y_iq, bench);
+}
+
+int rfx_fir_host_format(int impl, int format, const void* x_iq, int64_t num_samples,
+                        const float* taps, int num_taps, int block, void* y_iq, rfx_bench* bench)
+{
     if (block < 32 || block > 1024 || block % 32 != 0) {
         return fail(RFX_ERR_INVALID, "--block needs a multiple of 32 up to 1024, got %d", block);
+    }
+    if (check_format(format) != RFX_OK) {
+        return RFX_ERR_INVALID;
     }
     if (num_samples > 0 && (x_iq == nullptr || y_iq == nullptr || taps == nullptr)) {
         return fail(RFX_ERR_INVALID, "fir: null host pointer");
     }
     DeviceMem dx, dy, dh;
-    const size_t xbytes = static_cast<size_t>(num_samples) * 8;
+    const size_t xbytes = static_cast<size_t>(num_samples) * format_sample_bytes(format);
+    const size_t ybytes = static_cast<size_t>(num_samples) * 8;
     cudaError_t err;
     if (num_samples > 0) {
         if ((err = cudaMalloc(&dx.p, xbytes)) != cudaSuccess ||
-            (err = cudaMalloc(&dy.p, xbytes)) != cudaSuccess) {
+            (err = cudaMalloc(&dy.p, ybytes)) != cudaSuccess) {
             return cuda_fail(err, "cudaMalloc");
         }
     }
@@ -664,10 +712,10 @@ int rfx_fir_host(int impl, const void* x_iq, int64_t num_samples, const float* t
                                       cudaMemcpyHostToDevice);
         },
         [&] {
-            return rfx_fir_launch(impl, dx.p, static_cast<const float*>(dh.p), dy.p, num_samples,
-                                  num_taps, nullptr);
+            return rfx_fir_launch_format(impl, format, dx.p, static_cast<const float*>(dh.p),
+                                         dy.p, num_samples, num_taps, nullptr);
         },
-        [&] { return copy(y_iq, dy.p, xbytes, cudaMemcpyDeviceToHost); });
+        [&] { return copy(y_iq, dy.p, ybytes, cudaMemcpyDeviceToHost); });
 }
 
 int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,

@@ -13,4 +13,9 @@ namespace rfx {
 cudaError_t encode_rows_f32(CUtensorMap* map, const void* base, long long rows, int row_floats,
                             unsigned box_x, unsigned box_y);
 
+// The same view over elements of `elem_bytes` bytes (4: float32, 2: int16, 1: int8 / raw bytes):
+// the copy moves the bits, zero outside the view. elem_bytes * row_elems a multiple of 16.
+cudaError_t encode_rows(CUtensorMap* map, const void* base, int elem_bytes, long long rows,
+                        int row_elems, unsigned box_x, unsigned box_y);
+
 }  // namespace rfx

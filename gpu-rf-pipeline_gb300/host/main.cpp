@@ -6,7 +6,8 @@
 //   rfgpu stream     --in X.cf32 --taps H.f32 --out Y.cf32 [--impl NAME] [--chunk N]
 //                    [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]
 //   rfgpu info
-//   (fir and channelize: [--bench N [--warmup W]] prints phase timings as JSON; stream: the
+//   (every X input may be a SigMF recording, NAME.sigmf-meta or NAME.sigmf-data, in cf32_le,
+//    ci16_le or ci8; fir and channelize: [--bench N [--warmup W]] prints phase timings as JSON; stream: the
 //    wall-clock time of whole streamed passes, with the throughput against the sample rate)
 //
 // Exit status: 0 on success, 1 on a runtime error (file, CUDA, cuFFT), 2 on a usage error.
@@ -68,6 +69,10 @@ void print_usage()
                  "                  [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]\n"
                  "                  FIR in chunks through a ring of D pinned buffers and CUDA streams\n"
                  "  rfgpu info       GPU, CUDA versions and implementations as JSON\n"
+                 "\n"
+                 "Every .cf32 input may also be a SigMF recording (NAME.sigmf-meta or "
+                 "NAME.sigmf-data)\n"
+                 "in cf32_le, ci16_le or ci8; fir converts integer recordings on the GPU.\n"
                  "\n"
                  "benchmark options (fir, channelize, stream):\n"
                  "  --bench N      time N runs with CUDA events and print the result as JSON\n"
@@ -208,15 +213,25 @@ int run_fir(int argc, char** argv)
                          std::to_string(block));
     }
     Bench bench(bench_config(args));
-    const std::vector<cf32> x = read_cf32(args.required("--in"));
+    // Integer recordings go to the device as stored and are converted there (a half or a
+    // quarter of the upload); the results are those of converting on the host first.
+    StoredSamples stored = read_stored(args.required("--in"));
     const std::vector<float> taps = read_f32(args.required("--taps"));
     if (taps.empty()) {
         throw std::runtime_error(args.required("--taps") + ": no taps");
     }
-    require_int_range(x.size(), "fir input");
+    require_int_range(stored.count, "fir input");
     require_int_range(taps.size(), "tap array");
-    const std::vector<cf32> y = x.empty() ? std::vector<cf32>() : impl.fn(x, taps, block, bench);
-    finish(args, "fir", impl.name, x.size(), y, bench);
+    const std::size_t num_in = stored.count;
+    std::vector<cf32> y;
+    if (num_in > 0 && stored.format != SampleFormat::Cf32) {
+        y = fir_stored(impl.name, stored, taps, block, bench);
+    } else if (num_in > 0) {
+        const std::vector<cf32> x = to_cf32(stored);
+        stored.bytes = std::vector<std::uint8_t>();
+        y = impl.fn(x, taps, block, bench);
+    }
+    finish(args, "fir", impl.name, num_in, y, bench);
     return 0;
 }
 

@@ -150,6 +150,42 @@ RFX_FIR_ENTRY(fir_tiled, FirImpl::Tiled)
 RFX_FIR_ENTRY(fir_tiled_const, FirImpl::TiledConst)
 RFX_FIR_ENTRY(fir_register, FirImpl::Register)
 
+}  // namespace
+
+std::vector<cf32> fir_stored(const char* impl_name, const StoredSamples& x,
+                             const std::vector<float>& taps, int block, Bench& bench)
+{
+    if (block < 32 || block > 1024 || block % 32 != 0) {
+        throw std::runtime_error("fir: block " + std::to_string(block) +
+                                 " is not a multiple of 32 up to 1024");
+    }
+    FirImpl impl;
+    if (!parse_fir_impl(impl_name, impl)) {
+        throw std::runtime_error(std::string("fir: unknown implementation ") + impl_name);
+    }
+    const int num_samples = static_cast<int>(x.count);
+    const int num_taps = static_cast<int>(taps.size());
+    std::vector<cf32> y(x.count);
+    RFX_CHECK(rfx_fir_load_const_taps(taps.data(), num_taps, nullptr));  // capacity check only
+    DeviceBuffer<std::uint8_t> d_x(x.bytes.size());
+    DeviceBuffer<cf32> d_y(y.size());
+    DeviceBuffer<float> d_h(taps.size());
+    bench.run(
+        [&] {
+            d_x.upload(x.bytes.data(), x.bytes.size());
+            d_h.upload(taps.data(), taps.size());
+        },
+        [&] {
+            RFX_CHECK(rfx_fir_launch_format(to_rfx_impl(impl), static_cast<int>(x.format),
+                                            d_x.get(), d_h.get(), d_y.get(), num_samples,
+                                            num_taps, nullptr));
+        },
+        [&] { d_y.download(y.data(), y.size()); });
+    return y;
+}
+
+namespace {
+
 std::vector<cf32> channelize_impl(int impl, const std::vector<cf32>& x,
                                   const std::vector<float>& taps, int channels, Bench& bench)
 {

@@ -5,6 +5,7 @@
 // compute / download phases handed to Bench::run(), host data out.
 
 #include "bench.hpp"
+#include "io.hpp"
 #include "types.hpp"
 
 #include <vector>
@@ -22,6 +23,12 @@ using FirFn = std::vector<cf32> (*)(const std::vector<cf32>& x, const std::vecto
                                     int block, Bench& bench);
 constexpr int kDefaultFirBlock = 256;
 const std::vector<Impl<FirFn>>& fir_impls();  // first entry is the default
+
+// The FIR of samples as stored (ci16 / ci8 SigMF recordings): the stored bytes are uploaded and
+// converted in the kernels' load stage (rfx_fir_launch_format), with the results of converting
+// on the host and running the implementation named `impl` (a fir_impls() name).
+std::vector<cf32> fir_stored(const char* impl, const StoredSamples& x,
+                             const std::vector<float>& taps, int block, Bench& bench);
 
 // Polyphase channelizer: ceil(x.size() / channels) frames of `channels` values,
 // z[t][k] = sum_l taps[l] * x[t*M - l] * exp(+2j*pi*k*l / M).

@@ -58,6 +58,7 @@ SIGNATURES = {
     "rfx_parse_fir_impl": (_I, [ctypes.c_char_p, ctypes.POINTER(_I)]),
     "rfx_parse_chan_impl": (_I, [ctypes.c_char_p, ctypes.POINTER(_I)]),
     "rfx_fir_launch": (_I, [_I, _VP, _VP, _VP, _I64, _I, _VP]),
+    "rfx_fir_launch_format": (_I, [_I, _I, _VP, _VP, _VP, _I64, _I, _VP]),
     "rfx_fir_device": (_I, [_I, _VP, _VP, _VP, _I64, _I]),
     "rfx_fir_load_const_taps": (_I, [_VP, _I, _VP]),
     "rfx_fir_batched_device": (_I, [_I, ctypes.POINTER(_VP), ctypes.POINTER(_VP),
@@ -72,6 +73,7 @@ SIGNATURES = {
     "rfx_fir_stream": (_I, [_VP, _I64, _VP, _I, ctypes.POINTER(StreamConfig), _VP,
                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
     "rfx_fir_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
+    "rfx_fir_host_format": (_I, [_I, _I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_channelize_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_autotune_fir": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),
     "rfx_autotune_save": (_I, [ctypes.c_char_p]),
@@ -151,6 +153,42 @@ def fir_launch(impl, x, taps, y, stream=None, num_samples: int | None = None) ->
     n = x.numel() if num_samples is None else int(num_samples)
     _check(load().rfx_fir_launch(_impl(impl), x.data_ptr(), taps.data_ptr(), y.data_ptr(), n,
                                  taps.numel(), _stream_ptr(stream)))
+
+
+# rfx_sample_format: the stored forms of an input (SigMF cf32_le, ci16_le, ci8).
+SAMPLE_FORMATS = {"cf32": 0, "ci16": 1, "ci8": 2}
+_COMPONENT_BYTES = {"cf32": 4, "ci16": 2, "ci8": 1}
+
+
+def _format(fmt) -> int:
+    if isinstance(fmt, str):
+        if fmt not in SAMPLE_FORMATS:
+            raise ValueError(f"unknown sample format {fmt!r} (cf32, ci16, ci8)")
+        return SAMPLE_FORMATS[fmt]
+    return int(fmt)
+
+
+def fir_launch_format(impl, fmt, x, taps, y, stream=None, num_samples: int | None = None) -> None:
+    """y[:n] = FIR(x[:n] converted from `fmt`, taps): x a CUDA tensor of interleaved I/Q
+    components as stored (int16 for ci16, int8 for ci8, float32 or complex64 for cf32), y
+    complex64. The conversion happens in the kernels' load stage."""
+    name = fmt if isinstance(fmt, str) else {v: k for k, v in SAMPLE_FORMATS.items()}[int(fmt)]
+    n = (x.numel() * x.element_size() // (2 * _COMPONENT_BYTES[name]) if num_samples is None
+         else int(num_samples))
+    _check(load().rfx_fir_launch_format(_impl(impl), _format(fmt), x.data_ptr(), taps.data_ptr(),
+                                        y.data_ptr(), n, taps.numel(), _stream_ptr(stream)))
+
+
+def fir_format(x, taps, fmt, impl="plain", stream=None):
+    """Returns a new complex64 CUDA tensor with the FIR of stored samples x (see
+    fir_launch_format)."""
+    import torch
+
+    name = fmt if isinstance(fmt, str) else {v: k for k, v in SAMPLE_FORMATS.items()}[int(fmt)]
+    n = x.numel() * x.element_size() // (2 * _COMPONENT_BYTES[name])
+    y = torch.empty(n, dtype=torch.complex64, device=x.device)
+    fir_launch_format(impl, fmt, x, taps, y, stream, n)
+    return y
 
 
 def fir(x, taps, impl="plain", stream=None):

@@ -12,6 +12,9 @@ byte for byte (tests check the SHA-256 of each against the project's own files):
   as float32.
 * a cf32 array is interleaved little-endian float32 I, Q (src/types.hpp:7-12); here it is a
   NumPy ``complex64`` array, which has that memory layout.
+* the SigMF recording ``tone_ci16`` follows tools/gen_fixtures.py:109-128 and :188-193: the
+  tone_odd signal (before float32 rounding) scaled to half of full scale, each component
+  rounded to int16 of v * 32767, interleaved little-endian.
 
 The benchmark workloads have no generator in the project; their definitions (sizes, seeds,
 tap designs, tone and noise statistics) are this library's and are documented per function.
@@ -60,7 +63,8 @@ def to_cf32(x: np.ndarray) -> np.ndarray:
 
 def fixture_signal(name: str) -> np.ndarray:
     """The project's test fixture signals as complex64: tone (65536), tone_odd (10007),
-    short (7), zeros (4096)."""
+    short (7), zeros (4096), and tone_ci16 (10007) as the pipeline reads that SigMF recording
+    (each int16 component times 1/32768, exact in float32)."""
     if name == "tone":
         return to_cf32(tones_plus_noise(np.random.default_rng(1001), 65536, FIXTURE_TONES, 0.05))
     if name == "tone_odd":
@@ -69,6 +73,12 @@ def fixture_signal(name: str) -> np.ndarray:
         return to_cf32(tones_plus_noise(np.random.default_rng(1003), 7, FIXTURE_TONES, 0.05))
     if name == "zeros":
         return np.zeros(4096, dtype=np.complex64)
+    if name == "tone_ci16":
+        v = tone_ci16().astype(np.float32) * np.float32(1.0 / 32768.0)
+        out = np.empty(v.size // 2, dtype=np.complex64)
+        out.real = v[0::2]
+        out.imag = v[1::2]
+        return out
     raise KeyError(name)
 
 
@@ -86,6 +96,39 @@ def fixture_taps(name: str) -> np.ndarray:
     if name == "identity":
         return np.array([1.0], dtype=np.float32)
     raise KeyError(name)
+
+
+def tone_ci16() -> np.ndarray:
+    """The project's SigMF fixture ``tone_ci16``: interleaved little-endian int16 I/Q
+    components (2 * 10007 values), the contents of tone_ci16.sigmf-data."""
+    x = tones_plus_noise(np.random.default_rng(1002), 10007, FIXTURE_TONES, 0.05)
+    x = 0.5 * x / np.max(np.abs(x))
+    iq = np.empty(2 * len(x), dtype="<i2")
+    iq[0::2] = np.round(x.real * 32767)
+    iq[1::2] = np.round(x.imag * 32767)
+    return iq
+
+
+def write_sigmf(stem, components: np.ndarray, datatype: str,
+                sample_rate: float = SAMPLE_RATE, num_channels: int = 1) -> None:
+    """Writes STEM.sigmf-data (the interleaved components as given) and STEM.sigmf-meta with
+    the SigMF core fields the pipeline reads (datatype, sample rate, channel count)."""
+    import json
+    from pathlib import Path
+
+    stem = Path(stem)
+    np.ascontiguousarray(components).tofile(stem.with_name(stem.name + ".sigmf-data"))
+    meta = {
+        "global": {
+            "core:datatype": datatype,
+            "core:sample_rate": sample_rate,
+            "core:version": "1.2.0",
+            "core:num_channels": num_channels,
+        },
+        "captures": [{"core:sample_start": 0}],
+        "annotations": [],
+    }
+    stem.with_name(stem.name + ".sigmf-meta").write_text(json.dumps(meta, indent=2) + "\n")
 
 
 # --- benchmark workloads ------------------------------------------------------------------

@@ -102,6 +102,24 @@ int rfx_fir_launch(int impl, const void* x, const float* taps, void* y, int64_t 
 int rfx_fir_device(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
                    int num_taps);
 
+/* Sample formats of an input buffer: the SigMF datatypes the project reads
+ * (src/io.cpp:126-148), interleaved I/Q, little-endian. */
+typedef enum rfx_sample_format {
+    RFX_FORMAT_CF32 = 0,  /* cf32_le: float32 components */
+    RFX_FORMAT_CI16 = 1,  /* ci16_le: int16 components, each read as v / 32768 */
+    RFX_FORMAT_CI8 = 2    /* ci8 / ci8_le: int8 components, each read as v / 128 */
+} rfx_sample_format;
+
+/* rfx_fir_launch over x stored in `format` (num_samples samples of 8, 4 or 2 bytes), converted
+ * in the kernels' load stage instead of on the host: the same results as converting every
+ * sample as the project's SigMF reader does (src/io.cpp:110-124) and calling rfx_fir_launch, for
+ * a quarter (ci8) or half (ci16) of the input bytes. RFX_FIR_TC runs its single-CTA form on
+ * integer input. y is cf32; x and y 16-byte aligned.
+ * No counterpart in the project, which converts on the host before the upload (src/io.cpp:175-181
+ * then fir_host). */
+int rfx_fir_launch_format(int impl, int format, const void* x, const float* taps, void* y,
+                          int64_t num_samples, int num_taps, cudaStream_t stream);
+
 /* Checks that `num_taps` fits the tap capacity. The kernels here read the taps from the pointer
  * passed to each launch, so there is no constant bank to fill: callers that load it first and
  * then launch (src/stream.cu:158-160, :195-202) get the same results.
@@ -219,6 +237,11 @@ typedef struct rfx_bench {
  * Replaces the FirFn table entries (src/ops.hpp:33-36). */
 int rfx_fir_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
                  int num_taps, int block, void* y_iq, rfx_bench* bench);
+
+/* rfx_fir_host over host samples in `format` (rfx_sample_format): the stored bytes are
+ * uploaded and converted on the device by rfx_fir_launch_format; bench->h2d covers those bytes. */
+int rfx_fir_host_format(int impl, int format, const void* x, int64_t num_samples,
+                        const float* taps, int num_taps, int block, void* y_iq, rfx_bench* bench);
 
 /* The channelizer on host buffers, as above. `z_iq` receives frames * channels cf32.
  * Replaces channelize_cuda (src/ops.hpp:40-41). */

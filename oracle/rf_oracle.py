@@ -14,6 +14,8 @@ Restated from the gpu-rf-pipeline project (file:line inside that project):
 * ``fir_f32_seq``  src/fir.cu:30-40 — the reference GPU kernels' float32 arithmetic (one fused
                    multiply-add per tap, taps in ascending order), for bit-exact comparisons.
 * ``channelize_branch_f32_seq``  src/channelize.cu:25-49 — the reference's float32 branch sums.
+* ``decode``       src/io.cpp:110-148 — SigMF integer samples to cf32: each ci16_le component
+                   v * (1 / 32768), each ci8 component v * (1 / 128), in float32.
 
 The float64 functions exist twice: in NumPy here (for small inputs and to pin the C code) and
 in C (oracle/rf_oracle.c, threaded, for the large workloads). Golden vectors produced by the
@@ -85,6 +87,29 @@ def _taps32(taps: np.ndarray) -> np.ndarray:
 
 
 # --- NumPy restatements -------------------------------------------------------------------
+
+SAMPLE_FORMATS = {"cf32": 0, "ci16": 1, "ci8": 2}  # rfx_sample_format
+
+
+def decode(components: np.ndarray, fmt: str) -> np.ndarray:
+    """Interleaved I/Q components in ``fmt`` (cf32: float32; ci16: int16; ci8: int8) as cf32
+    samples, converted as the project's SigMF reader does: the component, as float32, times
+    1/32768 (ci16) or 1/128 (ci8)."""
+    c = np.asarray(components)
+    if c.size % 2 != 0:
+        raise ValueError("odd number of components, not I/Q pairs")
+    if fmt == "cf32":
+        v = c.astype(np.float32)
+    elif fmt == "ci16":
+        v = c.astype("<i2").astype(np.float32) * np.float32(1.0 / 32768.0)
+    elif fmt == "ci8":
+        v = c.astype(np.int8).astype(np.float32) * np.float32(1.0 / 128.0)
+    else:
+        raise ValueError(f"unknown sample format {fmt!r}")
+    out = np.empty(c.size // 2, dtype=np.complex64)
+    out.real = v[0::2]
+    out.imag = v[1::2]
+    return out
 
 def fir(x: np.ndarray, taps: np.ndarray) -> np.ndarray:
     """y[n] = sum_k taps[k] x[n-k] with x[m<0] = 0, len(y) = len(x), complex128.

@@ -33,7 +33,8 @@ sys.path.insert(0, str(ROOT / "gpu-rf-pipeline_gb300"))
 from rfx import signals  # noqa: E402
 
 FIXTURE_FILES = ["tone.cf32", "tone_odd.cf32", "short.cf32", "zeros.cf32", "lowpass.f32",
-                 "lowpass_long.f32", "channelizer_proto.f32", "identity.f32"]
+                 "lowpass_long.f32", "channelizer_proto.f32", "identity.f32",
+                 "tone_ci16.sigmf-data"]
 
 FULL_LIMIT = 2048  # outputs up to this many elements are stored whole
 
@@ -97,6 +98,21 @@ def main() -> None:
         for taps in ["lowpass", "lowpass_long", "identity"]:
             record(f"fir/{sig}/{taps}", reference.fir(fixture_x(sig), fixture_h(taps)),
                    {"op": "fir", "signal": sig, "taps": taps})
+    # The SigMF ci16 recording, converted as the project's tests convert it
+    # (tests/test_pipeline.py:276-278: components / 32768 in float64, exact), through the FIR
+    # (tests/test_pipeline.py:289-295) and the channelizer.
+    meta = json.loads((fixtures / "tone_ci16.sigmf-meta").read_text())["global"]
+    raw = np.fromfile(fixtures / "tone_ci16.sigmf-data", dtype="<i2").astype(np.float64) / 32768
+    x_ci16 = raw[0::2] + 1j * raw[1::2]
+    sigmf = {"datatype": meta["core:datatype"], "sample_rate": meta["core:sample_rate"],
+             "num_channels": meta["core:num_channels"]}
+    for taps in ["lowpass", "lowpass_long", "identity"]:
+        record(f"fir/tone_ci16/{taps}", reference.fir(x_ci16, fixture_h(taps)),
+               {"op": "fir", "signal": "tone_ci16", "taps": taps, "sigmf": sigmf})
+    record("chan/tone_ci16/channelizer_proto/16",
+           reference.channelize(x_ci16, fixture_h("channelizer_proto"), 16),
+           {"op": "channelize", "signal": "tone_ci16", "taps": "channelizer_proto",
+            "channels": 16, "sigmf": sigmf})
     # Channelizer on the project's fixtures (tests/test_pipeline.py:367-373).
     for sig, taps, m in [("tone", "channelizer_proto", 16), ("tone_odd", "channelizer_proto", 16),
                          ("tone", "lowpass_long", 64), ("short", "lowpass", 4),

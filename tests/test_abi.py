@@ -113,3 +113,17 @@ def test_host_block_size_is_checked(lib) -> None:
     for block in (0, 48, 2048):
         assert lib.rfx_fir_host(0, None, 0, None, 1, block, None, None) == 1
         assert b"--block" in lib.rfx_last_error()
+
+
+def test_fir_format_argument_errors(lib) -> None:
+    buf = ctypes.create_string_buffer(64)
+    p = (ctypes.addressof(buf) + 15) & ~15
+    for fmt in (-1, 3, 7):
+        assert lib.rfx_fir_launch_format(0, fmt, p, p, p, 10, 3, None) == 1
+        assert b"format" in lib.rfx_last_error()
+    # The same checks as rfx_fir_launch, before any device work.
+    assert lib.rfx_fir_launch_format(0, 1, p + 4, p, p, 10, 3, None) == 3
+    assert lib.rfx_fir_launch_format(0, 2, p, p, p, 10, 0, None) == 1
+    assert lib.rfx_fir_launch_format(5, 1, p, p, p, 10, 3, None) == 1
+    assert lib.rfx_fir_launch_format(0, 1, None, None, None, 0, 3, None) == 0
+    assert lib.rfx_fir_host_format(0, 9, None, 0, None, 1, 256, None, None) == 1

@@ -32,7 +32,18 @@ def fixtures(tmp_path_factory) -> Path:
         signals.fixture_signal(name).astype("<c8").tofile(d / f"{name}.cf32")
     for name in ["lowpass", "lowpass_long", "channelizer_proto", "identity"]:
         signals.fixture_taps(name).astype("<f4").tofile(d / f"{name}.f32")
+    # SigMF recordings: the project's ci16 fixture, the same signal in ci8, and the converted
+    # ci16 samples as a plain .cf32 file for byte comparisons.
+    signals.write_sigmf(d / "tone_ci16", signals.tone_ci16(), "ci16_le")
+    signals.write_sigmf(d / "tone_ci8", tone_ci8(), "ci8")
+    signals.fixture_signal("tone_ci16").astype("<c8").tofile(d / "tone_ci16.cf32")
+    orc.decode(tone_ci8(), "ci8").astype("<c8").tofile(d / "tone_ci8.cf32")
     return d
+
+
+def tone_ci8() -> np.ndarray:
+    """The ci16 fixture's signal at 8 bits: components round(v / 256), int8."""
+    return np.round(signals.tone_ci16().astype(np.float64) / 256).astype(np.int8)
 
 
 def rfgpu(*args, check: bool = True) -> subprocess.CompletedProcess:
@@ -298,3 +309,90 @@ def test_stream_bench_reports_throughput_against_the_sample_rate(fixtures: Path,
     assert report["sample_rate"] == 2.4e6
     assert report["msps"] > 0
     assert report["realtime_factor"] == pytest.approx(report["msps"] * 1e6 / 2.4e6, rel=1e-3)
+
+
+# --- SigMF recordings (tests/test_pipeline.py:272-307) ------------------------------------------
+# Every input may be a SigMF pair named by either file. `fir` uploads integer recordings as
+# stored and converts them on the GPU; the result must be the bytes of the FIR of the samples
+# converted on the host (the project's read path), for every implementation.
+
+@pytest.mark.parametrize("command", ["fir", "channelize", "stream"])
+@pytest.mark.parametrize("meta,message", [
+    ({"core:datatype": "cf64_le"}, "cf64_le"),
+    ({"core:datatype": "ci16_le", "core:num_channels": 2}, "channels"),
+])
+def test_unsupported_sigmf_is_a_runtime_error(tmp_path: Path, fixtures: Path, command: str,
+                                              meta: dict, message: str) -> None:
+    (tmp_path / "rec.sigmf-meta").write_text(json.dumps({"global": meta}))
+    (tmp_path / "rec.sigmf-data").write_bytes(bytes(16))
+    extra = ["--channels", "4"] if command == "channelize" else []
+    proc = rfgpu(command, "--in", tmp_path / "rec.sigmf-meta", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", *extra, check=False)
+    assert proc.returncode == 1
+    assert message in proc.stderr
+
+
+def test_sigmf_with_a_partial_sample_is_a_runtime_error(tmp_path: Path, fixtures: Path) -> None:
+    (tmp_path / "rec.sigmf-meta").write_text(json.dumps({"global": {"core:datatype": "ci16_le"}}))
+    (tmp_path / "rec.sigmf-data").write_bytes(bytes(6))  # one and a half ci16 samples
+    proc = rfgpu("fir", "--in", tmp_path / "rec.sigmf-data", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", check=False)
+    assert proc.returncode == 1
+    assert "rec.sigmf-data" in proc.stderr
+
+
+def test_sigmf_without_its_data_file_is_a_runtime_error(tmp_path: Path, fixtures: Path) -> None:
+    (tmp_path / "rec.sigmf-meta").write_text(json.dumps({"global": {"core:datatype": "ci8"}}))
+    proc = rfgpu("fir", "--in", tmp_path / "rec.sigmf-meta", "--taps", fixtures / "lowpass.f32",
+                 "--out", tmp_path / "y.cf32", check=False)
+    assert proc.returncode == 1
+    assert "rec.sigmf-data" in proc.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("suffix", [".sigmf-meta", ".sigmf-data"])  # either file of the pair
+@pytest.mark.parametrize("impl", ["plain", "tc_split", "auto"])
+def test_sigmf_ci16_reads_as_scaled_cf32(fixtures: Path, tmp_path: Path, suffix: str,
+                                         impl: str) -> None:
+    out = tmp_path / "fir.cf32"
+    rfgpu("fir", "--in", fixtures / f"tone_ci16{suffix}", "--taps", fixtures / "identity.f32",
+          "--out", out, "--impl", impl)
+    raw = signals.tone_ci16().astype(np.float64) / 32768
+    np.testing.assert_array_equal(read_cf32(out), raw[0::2] + 1j * raw[1::2])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rec", ["tone_ci16", "tone_ci8"])
+@pytest.mark.parametrize("taps", ["lowpass", "lowpass_long"])
+@pytest.mark.parametrize("impl", ["plain", "tc_split", "auto", "register"])
+def test_sigmf_fir_is_the_fir_of_the_converted_samples(fixtures: Path, tmp_path: Path, rec: str,
+                                                       taps: str, impl: str) -> None:
+    rfgpu("fir", "--in", fixtures / f"{rec}.sigmf-meta", "--taps", fixtures / f"{taps}.f32",
+          "--out", tmp_path / "sigmf.cf32", "--impl", impl)
+    rfgpu("fir", "--in", fixtures / f"{rec}.cf32", "--taps", fixtures / f"{taps}.f32",
+          "--out", tmp_path / "cf32.cf32", "--impl", impl)
+    assert (tmp_path / "sigmf.cf32").read_bytes() == (tmp_path / "cf32.cf32").read_bytes()
+    x = np.fromfile(fixtures / f"{rec}.cf32", dtype="<c8")
+    expected = orc.fir(x, signals.fixture_taps(taps))
+    np.testing.assert_allclose(read_cf32(tmp_path / "sigmf.cf32"), expected, rtol=FIR_RTOL,
+                               atol=FIR_ATOL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", ["plain", "auto"])
+def test_sigmf_channelize_and_stream_read_the_recording(fixtures: Path, tmp_path: Path,
+                                                        impl: str) -> None:
+    for src, name in [(fixtures / "tone_ci16.sigmf-meta", "a"), (fixtures / "tone_ci16.cf32", "b")]:
+        rfgpu("channelize", "--in", src, "--taps", fixtures / "channelizer_proto.f32",
+              "--channels", 16, "--out", tmp_path / f"chan_{name}.cf32", "--impl", impl)
+        rfgpu("stream", "--in", src, "--taps", fixtures / "lowpass_long.f32",
+              "--out", tmp_path / f"stream_{name}.cf32", "--chunk", 4096)
+    assert (tmp_path / "chan_a.cf32").read_bytes() == (tmp_path / "chan_b.cf32").read_bytes()
+    assert (tmp_path / "stream_a.cf32").read_bytes() == (tmp_path / "stream_b.cf32").read_bytes()
+
+
+@pytest.mark.gpu
+def test_sigmf_sample_rate_comes_from_the_recording(fixtures: Path, tmp_path: Path) -> None:
+    proc = rfgpu("stream", "--in", fixtures / "tone_ci16.sigmf-data", "--taps",
+                 fixtures / "lowpass.f32", "--out", tmp_path / "y.cf32", "--bench", 3)
+    assert json.loads(proc.stdout)["sample_rate"] == signals.SAMPLE_RATE

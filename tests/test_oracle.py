@@ -45,6 +45,33 @@ def test_fixture_taps_bytes_match_the_project(name: str) -> None:
     assert hashlib.sha256(h.astype("<f4").tobytes()).hexdigest() == SHAS[f"{name}.f32"]
 
 
+def test_sigmf_fixture_bytes_match_the_project() -> None:
+    iq = signals.tone_ci16()
+    assert iq.dtype == np.dtype("<i2") and iq.size == 2 * 10007
+    assert hashlib.sha256(iq.tobytes()).hexdigest() == SHAS["tone_ci16.sigmf-data"]
+    # Half of full scale: no component clips (tests/test_fixtures.py:85-92).
+    assert 0.45 * 32767 < np.max(np.abs(iq)) <= 0.5 * 32767 + 1
+
+
+def test_decode_converts_as_the_sigmf_reader() -> None:
+    # ci16: v / 32768, exact in float32; the extremes included.
+    c16 = np.array([-32768, 32767, 0, -1, 1, 12345], dtype="<i2")
+    z = orc.decode(c16, "ci16")
+    assert z.dtype == np.complex64
+    np.testing.assert_array_equal(z.real, c16[0::2].astype(np.float64) / 32768)
+    np.testing.assert_array_equal(z.imag, c16[1::2].astype(np.float64) / 32768)
+    # ci8: every value, v / 128.
+    c8 = np.arange(-128, 128, dtype=np.int8)
+    z = orc.decode(c8, "ci8")
+    np.testing.assert_array_equal(z.real, c8[0::2].astype(np.float64) / 128)
+    np.testing.assert_array_equal(z.imag, c8[1::2].astype(np.float64) / 128)
+    # cf32 as is; the SigMF fixture through decode is the fixture signal.
+    assert np.array_equal(orc.decode(signals.tone_ci16(), "ci16"),
+                          signals.fixture_signal("tone_ci16"))
+    with pytest.raises(ValueError):
+        orc.decode(c16[:3], "ci16")
+
+
 # --- golden vectors from tools/reference.py ------------------------------------------------
 
 def case_inputs(case: dict) -> tuple[np.ndarray, np.ndarray]:
