@@ -23,11 +23,14 @@
 //     The tensor core accumulates FP32 with round-toward-zero, so two TMEM accumulators take
 //     twelve MMAs each and are summed in FP32 registers; the accumulators are double-buffered
 //     (2 tiles x 2 x 128 columns) so the MMAs of tile k + 1 run while tile k is drained.
-//  5. Scale back by 2^-(eu + ew) and store each frame's 64 channels.
+//  5. Scale back by 2^-(eu + ew) and store each frame's 64 channels. The accumulator columns
+//     are ordered (column_to_channel) so that 16x256b tensor-memory loads hand four adjacent
+//     lanes a frame's channels in pairs: each store instruction writes 64 contiguous bytes of
+//     eight frames (whole 32-byte sectors) instead of 16 bytes of 32 frames.
 //
 // Roles (576 threads): warps 0-15 compute branch sums, write operands and drain the
-// accumulators (warp w: TMEM lane quarter w % 4 = frames 32 (w % 4) .. +31, channels
-// 16 (w / 4) .. +15); warp 16 owns tensor memory and issues the MMAs; warp 17 refills the
+// accumulators (warp w: TMEM lane quarter w % 4 = frames 32 (w % 4) .. +31, accumulator
+// columns 32 (w / 4) .. +31 = channels 16 (w / 4) .. +15); warp 16 owns tensor memory and issues the MMAs; warp 17 refills the
 // half-windows as the workers release them. The loop runs the branch
 // sums of tile k + 1 and stages its operand before draining tile k, so the MMAs of tile k hide
 // behind the branch sums and those of tile k + 1 behind the drain. Every wait is a bounded
@@ -64,6 +67,20 @@ constexpr uint32_t kIdesc = idesc_f16(kFrames, kK);
 constexpr int kWExp = 14;              // W' = 2^14 W, |W| <= 1
 constexpr int kMaxPerBranch = 32;      // taps per branch the kernel takes
 constexpr int kSmemTapsMax = 26;       // taps per branch up to which the taps sit in smem too
+constexpr int kColsPerSlice = 32;      // accumulator columns a drain warp reads: 16 channels
+
+// The GEMM's N index (accumulator column) -> output channel and part (0 Re, 1 Im). Column
+// 32 s + 8 j + 2 q + b holds part b of channel 16 s + 8 (j / 2) + 2 q + j % 2, so that the
+// drain's 16x256b loads give thread q of a frame (Re, Im) of channels c and c + 1 side by
+// side (c = 16 s + 8 (j / 2) + 2 q): one 16-byte store.
+__host__ __device__ inline void column_to_channel(int n, int& ch, int& part)
+{
+    const int s = n >> 5;
+    const int j = (n >> 3) & 3;
+    const int q = (n >> 1) & 3;
+    part = n & 1;
+    ch = 16 * s + 8 * (j >> 1) + 2 * q + (j & 1);
+}
 
 // The GEMM's K index of Re u (k < 64; Im u at 64 + k) -> branch. Lane l owns K indices 2l and
 // 2l + 1, i.e. branches (64 - l) % 64 and 32 - l, whose window columns (64 - m) % 64 are l and
@@ -396,25 +413,29 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
                 break;
             }
             fence_after();
-            float re[16];
-            float im[16];
+            // v[r]: lanes 32 quarter + 16 r .. + 15 (frames), columns 32 slice .. + 31
+            // (channels 16 slice .. + 15, Re and Im), in the 16x256b fragment order.
+            float v[2][16];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                re[i] = 0.0f;
-                im[i] = 0.0f;
+            for (int r = 0; r < 2; ++r) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    v[r][i] = 0.0f;
+                }
             }
 #pragma unroll
             for (int part = 0; part < kParts; ++part) {
-                uint32_t tr[16];
-                uint32_t ti[16];
-                const uint32_t col = static_cast<uint32_t>((db * kParts + part) * kK + 16 * slice);
-                tmem_ld16(lane_addr + col, tr);
-                tmem_ld16(lane_addr + col + kM, ti);
+                uint32_t t0[16];
+                uint32_t t1[16];
+                const uint32_t col =
+                    static_cast<uint32_t>((db * kParts + part) * kK + kColsPerSlice * slice);
+                tmem_ld_16x256b_x4(lane_addr + col, t0);
+                tmem_ld_16x256b_x4(lane_addr + (16u << 16) + col, t1);
                 tmem_wait_ld();
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
-                    re[i] += __uint_as_float(tr[i]);
-                    im[i] += __uint_as_float(ti[i]);
+                    v[0][i] += __uint_as_float(t0[i]);
+                    v[1][i] += __uint_as_float(t1[i]);
                 }
             }
             fence_before();
@@ -425,13 +446,26 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             const int shift = -(((k & 1) ? eu_odd : eu_even) + kWExp);
             const float fa = exp2i(shift / 2);
             const float fb = exp2i(shift - shift / 2);
-            const long long t = static_cast<long long>(tile_of(k)) * kFrames + quarter * 32 + lane;
-            if (t < frames) {
-                float4* dst = reinterpret_cast<float4*>(z + t * kM + 16 * slice);
+            // Four lanes per frame write its channels 16 slice + 8 jj + 2 (lane % 4), + 1: each
+            // store fills 64 contiguous bytes of eight frames.
+            const long long t_base = static_cast<long long>(tile_of(k)) * kFrames + quarter * 32 +
+                                     (lane >> 2);
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    dst[i] = make_float4(re[2 * i] * fa * fb, im[2 * i] * fa * fb,
-                                         re[2 * i + 1] * fa * fb, im[2 * i + 1] * fa * fb);
+            for (int r = 0; r < 2; ++r) {
+#pragma unroll
+                for (int s = 0; s < 2; ++s) {
+                    const long long t = t_base + 16 * r + 8 * s;
+                    if (t < frames) {
+#pragma unroll
+                        for (int jj = 0; jj < 2; ++jj) {
+                            const float* a = &v[r][4 * (2 * jj) + 2 * s];
+                            const float* b = &v[r][4 * (2 * jj + 1) + 2 * s];
+                            *reinterpret_cast<float4*>(z + t * kM + 16 * slice + 8 * jj +
+                                                       2 * (lane & 3)) =
+                                make_float4(a[0] * fa * fb, a[1] * fa * fb, b[0] * fa * fb,
+                                            b[1] * fa * fb);
+                        }
+                    }
                 }
             }
         }
@@ -498,8 +532,8 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
 }
 
 // Builds the twiddle operand image in FP64: B row n (output column), K index k (input
-// column), n, k < 128: rows 0-63 give Re z, rows 64-127 Im z; K 0-63 multiply Re u, 64-127
-// Im u. Element value 2^14 W split into FP16 hi/lo, stored at the operand layout's offsets.
+// column), n, k < 128: row n gives part `part` of channel `ch` (column_to_channel); K 0-63
+// multiply Re u, 64-127 Im u. Element value 2^14 W split into FP16 hi/lo, stored at the operand layout's offsets.
 __global__ void chan_twiddle_kernel(uint16_t* img)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -508,12 +542,14 @@ __global__ void chan_twiddle_kernel(uint16_t* img)
     }
     const int nrow = idx / kK;
     const int kcol = idx % kK;
-    const int ch = nrow % kM;
+    int ch = 0;
+    int part = 0;
+    column_to_channel(nrow, ch, part);
     const int br = k_to_branch(kcol % kM);
     double s, c;
     sincospi(2.0 * static_cast<double>((ch * br) % kM) / kM, &s, &c);
     double v;
-    if (nrow < kM) {
+    if (part == 0) {
         v = kcol < kM ? c : -s;    // Re z = Re u cos - Im u sin
     } else {
         v = kcol < kM ? s : c;     // Im z = Re u sin + Im u cos

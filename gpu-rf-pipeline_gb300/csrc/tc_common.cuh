@@ -91,6 +91,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&t)[16])
         : "r"(taddr));
 }
 
+// 16 lanes x 256 bits, four times along the columns: for 8-column group j (registers 4j .. 4j+3)
+// thread t holds (lane t/4: columns 2 (t%4), +1) and (lane t/4 + 8: the same columns) of the 16
+// lanes starting at taddr's lane.
+__device__ __forceinline__ void tmem_ld_16x256b_x4(uint32_t taddr, uint32_t (&t)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.16x256b.x4.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]),
+          "=r"(t[7]), "=r"(t[8]), "=r"(t[9]), "=r"(t[10]), "=r"(t[11]), "=r"(t[12]), "=r"(t[13]),
+          "=r"(t[14]), "=r"(t[15])
+        : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_wait_ld()
 {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
