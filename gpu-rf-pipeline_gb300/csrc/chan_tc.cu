@@ -8,13 +8,15 @@
 //     input) in two half-windows: frames [t0 + 64 h, +64) need rows t0 + 64 h - P .. +63
 //     (P = taps per branch), i.e. 64 + P rows per half, double-buffered so the next tile's
 //     samples stream in while this tile is finished.
-//  2. Branch sums on CUDA cores, FP32, from shared memory: lane l owns branches (64 - l) % 64
-//     and 32 - l (window columns l and 32 + l, so a warp's loads are conflict-free) for 4
-//     consecutive frames of each half. For one branch the frames form a FIR over the
-//     decimated sequence s_d = x[(t0 + d) M - m] with taps g_p = h[pM + m] (from shared memory
-//     up to 26 taps per branch, else the L1 cache); two alternating 4-sample register blocks,
-//     taps in ascending p, one packed f32x2 fused multiply-add per tap.
-//  3. The tile's largest |u| sets a power-of-two scale; u' = u_hi + u_lo in FP16 is written as
+//  2. Branch sums on CUDA cores, FP32, from shared memory: warps 0-7 read half-window 0,
+//     warps 8-15 half-window 1; lane l owns branches (64 - l) % 64 and 32 - l (window columns
+//     l and 32 + l, so a warp's loads are conflict-free) for 8 consecutive frames. For one
+//     branch the frames form a FIR over the decimated sequence s_d = x[(t0 + d) M - m] with
+//     taps g_p = h[pM + m] (from shared memory up to 26 taps per branch, else the L1 cache);
+//     two alternating 8-sample register blocks, taps in ascending p, one packed f32x2 fused
+//     multiply-add per tap: each sample loaded serves eight frames.
+//  3. Each frame's largest |u| sets a power-of-two scale for that frame (one GEMM row; the
+//     drain undoes it row by row); u' = u_hi + u_lo in FP16 is written as
 //     the GEMM's A operand (rows = frames, K = [Re u, Im u] in the lanes' branch order:
 //     K index 2l -> branch (64 - l) % 64, 2l + 1 -> 32 - l; W's rows follow the same order).
 //  4. The DFT as a real GEMM: [Re z, Im z] (128 x 128) = A (128 x 128) W, with
@@ -30,8 +32,8 @@
 //
 // Roles (576 threads): warps 0-15 compute branch sums, write operands and drain the
 // accumulators (warp w: TMEM lane quarter w % 4 = frames 32 (w % 4) .. +31, accumulator
-// columns 32 (w / 4) .. +31 = channels 16 (w / 4) .. +15); warp 16 owns tensor memory and issues the MMAs; warp 17 refills the
-// half-windows as the workers release them. The loop runs the branch
+// columns 32 (w / 4) .. +31 = channels 16 (w / 4) .. +15); warp 16 owns tensor memory and
+// issues the MMAs; warp 17 refills the half-windows as their eight warps release them. The loop runs the branch
 // sums of tile k + 1 and stages its operand before draining tile k, so the MMAs of tile k hide
 // behind the branch sums and those of tile k + 1 behind the drain. Every wait is a bounded
 // mbarrier wait.
@@ -54,8 +56,10 @@ constexpr int kM = 64;                 // channels
 constexpr int kK = 2 * kM;             // GEMM K and N: Re and Im parts
 constexpr int kFrames = 128;           // frames per tile = MMA M
 constexpr int kHalf = kFrames / 2;     // frames per half-window
-constexpr int kR = 4;                  // frames per thread per half
-constexpr int kWorkerWarps = 16;
+constexpr int kWorkerWarpsConst = 16;
+constexpr int kR = 8;                  // frames per thread (one half-window per warp)
+constexpr int kHalfWarps = kWorkerWarpsConst / 2;  // worker warps per half-window
+constexpr int kWorkerWarps = kWorkerWarpsConst;
 constexpr int kMmaWarp = 16;
 constexpr int kTmaWarp = 17;
 constexpr int kThreads = 18 * 32;
@@ -68,6 +72,10 @@ constexpr int kWExp = 14;              // W' = 2^14 W, |W| <= 1
 constexpr int kMaxPerBranch = 32;      // taps per branch the kernel takes
 constexpr int kSmemTapsMax = 26;       // taps per branch up to which the taps sit in smem too
 constexpr int kColsPerSlice = 32;      // accumulator columns a drain warp reads: 16 channels
+// Tiles whose frame exponents are kept: tile k's are rewritten at tile k + kExpBufs, by which
+// time every worker has drained tile k (staging tile k + 4 needs the MMAs of tile k + 3, which
+// need every worker's operand of tile k + 3, staged after its drain of tile k + 1).
+constexpr int kExpBufs = 4;
 
 // The GEMM's N index (accumulator column) -> output channel and part (0 Re, 1 Im). Column
 // 32 s + 8 j + 2 q + b holds part b of channel 16 s + 8 (j / 2) + 2 q + j % 2, so that the
@@ -121,15 +129,16 @@ struct Ctrl {
     unsigned long long win_empty[2];
     unsigned long long dfull[2];
     unsigned long long dempty[2];
-    unsigned long long reduce[2];
+    unsigned long long eready[kExpBufs];  // the frame exponents of a tile are written
     unsigned long long teardown;
     uint32_t tmem_base;
     int abort;
-    uint32_t warp_max[2][kWorkerWarps];
+    signed char fexp[kExpBufs][kFrames];  // frame scale exponents (clamped to 127)
 };
+static_assert(sizeof(Ctrl) <= 1024, "control block");
 
 // Taps p0 + q (q < nq) of one branch: acc[i] += g_p s_{i - p} with cur = S_g, nxt = S_{g+1},
-// S_g[i] = s_{-4g + i}. The taps come from shared memory (tap_s: the branch's column of the
+// S_g[i] = s_{-8g + i}. The taps come from shared memory (tap_s: the branch's column of the
 // taps[p][slot] table, 256 bytes per p) or, for the longest filters, through the L1 cache.
 template <bool kTapsSmem>
 __device__ __forceinline__ void branch_group(f32x2 (&acc)[kR], const f32x2 (&cur)[kR],
@@ -190,12 +199,14 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
         mbar_init(smem_u32(&ctl.empty), 1);
         for (int i = 0; i < 2; ++i) {
             mbar_init(smem_u32(&ctl.win_full[i]), 1);
-            mbar_init(smem_u32(&ctl.win_empty[i]), kWorkerWarps);
-            mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.win_empty[i]), kHalfWarps);
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(smem_u32(&ctl.dfull[i]), 1);
             mbar_init(smem_u32(&ctl.dempty[i]), kWorkerWarps);
+        }
+        for (int i = 0; i < kExpBufs; ++i) {
+            mbar_init(smem_u32(&ctl.eready[i]), kWorkerWarps);
         }
         mbar_init(smem_u32(&ctl.teardown), 1);
         ctl.abort = 0;
@@ -243,17 +254,21 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
         const int pair = wtid & 31;                      // K indices 2 pair, 2 pair + 1
         const int m_a = k_to_branch(2 * pair);           // their branches
         const int m_b = k_to_branch(2 * pair + 1);
-        const int fgroup = wtid >> 5;                    // frames 4 fgroup .. +3 of each half
+        const uint32_t tap_a = sbase + lay.taps + static_cast<uint32_t>(pair) * 4u;
+        const uint32_t tap_b = tap_a + 32u * 4u;
+        const int hw = warp / kHalfWarps;                // the half-window this warp reads
+        const int fgroup = warp % kHalfWarps;            // frames 8 fgroup .. +7 of half hw
+        const int frow0 = kHalf * hw + kR * fgroup;      // their first tile row
         const int quarter = warp & 3;
         const int slice = warp >> 2;                     // channels 16 slice .. +15
         const uint32_t lane_addr = tmem + (static_cast<uint32_t>(quarter * 32) << 16);
-        int eu_even = 0;   // scale exponents of the even and odd tiles
-        int eu_odd = 0;
 
         // Sample s_d of branch m for the thread's frames is x[(t + d) M - m] = window row
-        // (t + d - (m > 0)) - r0, column (M - m) % M. `base` addresses d = 0; a block of four
-        // consecutive d is four loads at fixed offsets. Rows outside the input were zero-filled
-        // by the copy; the partial last frame was patched in (patch_partial_row).
+        // (t + d - (m > 0)) - r0, column (M - m) % M. `base` addresses d = 0; a block of eight
+        // consecutive d is eight loads at fixed offsets. Rows outside the input were
+        // zero-filled by the copy; the partial last frame was patched in (patch_partial_row).
+        // (The block of the last tap group may start up to 8 rows before the window; those
+        // samples are never used and lie in the operand area before it.)
         auto load_block = [&](f32x2 (&blk)[kR], uint32_t base, int d0) {
             const uint32_t a = base + static_cast<uint32_t>(d0 * kM * 8);
 #pragma unroll
@@ -261,13 +276,13 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
                 blk[i] = lds64(a + static_cast<uint32_t>(i * kM * 8));
             }
         };
-        // u[t + i][m] for i < 4 from one half-window.
+        // u[t + i][m] for the thread's 8 frames of one branch m from the warp's half-window.
         auto branch_sums = [&](f32x2 (&acc)[kR], uint32_t buf, int m, uint32_t tap_s) {
 #pragma unroll
             for (int i = 0; i < kR; ++i) {
                 acc[i] = 0ull;
             }
-            // Frame t = first row + P + 4 fgroup; d = 0 is row 4 fgroup + P - (m > 0).
+            // Frame t = first row + P + 8 fgroup; d = 0 is row 8 fgroup + P - (m > 0).
             const uint32_t base =
                 buf + static_cast<uint32_t>(((kR * fgroup + P - (m > 0 ? 1 : 0)) * kM +
                                              ((kM - m) & (kM - 1))) * 8);
@@ -296,80 +311,64 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             }
         };
         // The input's last, partial frame lies outside the tensor map (its copy reads zeros):
-        // when a half-window holds that row, the workers write its samples in, then sync.
+        // when a half-window holds that row, the half's warps write its samples in, then sync.
         const int tail = static_cast<int>(n - full_rows * kM);
+        const int htid = static_cast<int>(threadIdx.x) - hw * kHalfWarps * 32;
         auto patch_partial_row = [&](uint32_t buf, long long r0) {
             const long long rel = full_rows - r0;
             if (tail == 0 || rel < 0 || rel >= lay.wrows) {
-                return;   // uniform across the block
+                return;   // uniform across the half's warps
             }
-            if (wtid < tail) {
-                const float2 v = __ldg(x + full_rows * kM + wtid);
-                sts64(buf + static_cast<uint32_t>(rel * kM + wtid) * 8u, pack2(v.x, v.y));
+            if (htid < tail) {
+                const float2 v = __ldg(x + full_rows * kM + htid);
+                sts64(buf + static_cast<uint32_t>(rel * kM + htid) * 8u, pack2(v.x, v.y));
             }
             fence_proxy_async_smem();
-            asm volatile("bar.sync 1, %0;" ::"n"(kWorkerWarps * 32) : "memory");
+            asm volatile("bar.sync %0, %1;" ::"r"(1 + hw), "n"(kHalfWarps * 32) : "memory");
         };
-        const uint32_t tap_a = sbase + lay.taps + static_cast<uint32_t>(pair) * 4u;
-        const uint32_t tap_b = tap_a + 32u * 4u;
-        // Branch sums of tile k for this thread: u0 (branch m_a), u1 (m_b), by half.
-        f32x2 u0[2][kR];
-        f32x2 u1[2][kR];
+
+        // Branch sums of tile k for this thread: u0 (branch m_a), u1 (m_b), 8 frames.
+        f32x2 u0[kR];
+        f32x2 u1[kR];
         auto compute = [&](int k) -> bool {
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                // Half h of tile k is the (k + 1)-th fill of buffer h.
-                if (!mbar_wait_bounded(smem_u32(&ctl.win_full[h]), k & 1, fault, kFaultTileLoad,
-                                       abort)) {
-                    return false;
-                }
-                const uint32_t buf = sbase + lay.win0 + static_cast<uint32_t>(h) * lay.win;
-                patch_partial_row(buf, row0(k, h));
-                branch_sums(u0[h], buf, m_a, tap_a);
-                branch_sums(u1[h], buf, m_b, tap_b);
-                __syncwarp();
-                if (lane == 0) {
-                    mbar_arrive(smem_u32(&ctl.win_empty[h]));
-                }
+            // Half hw of tile k is the (k + 1)-th fill of buffer hw.
+            if (!mbar_wait_bounded(smem_u32(&ctl.win_full[hw]), k & 1, fault, kFaultTileLoad,
+                                   abort)) {
+                return false;
+            }
+            const uint32_t buf = sbase + lay.win0 + static_cast<uint32_t>(hw) * lay.win;
+            patch_partial_row(buf, row0(k, hw));
+            branch_sums(u0, buf, m_a, tap_a);
+            branch_sums(u1, buf, m_b, tap_b);
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&ctl.win_empty[hw]));
             }
             return true;
         };
-        // Scale of tile k, then the A operand (once the MMAs of tile k - 1 are done).
+        // The A operand of tile k (once the MMAs of tile k - 1 are done), each frame (GEMM row)
+        // scaled by its own power of two: the DFT acts on rows, so the drain undoes the scale
+        // frame by frame. A warp holds whole frames (all 64 branches of its 8 frames), so a
+        // frame's scale is one warp reduction; lane 0 publishes the exponents for the drain.
         auto stage_operand = [&](int k) -> bool {
-            uint32_t mx = 0;
+            int ef[kR];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
+            for (int i = 0; i < kR; ++i) {
+                const float2 a = unpack2(u0[i]);
+                const float2 b = unpack2(u1[i]);
+                const uint32_t mx = max(max(absbits(a.x), absbits(a.y)),
+                                        max(absbits(b.x), absbits(b.y)));
+                // Clamped to 127 (only |u| < 2^-113 would want more): the stored exponent.
+                ef[i] = min(scale_exponent(__reduce_max_sync(0xFFFFFFFFu, mx)), 127);
+            }
+            if (lane == 0) {
+                signed char* fe = ctl.fexp[k % kExpBufs];
 #pragma unroll
                 for (int i = 0; i < kR; ++i) {
-                    const float2 a = unpack2(u0[h][i]);
-                    const float2 b = unpack2(u1[h][i]);
-                    mx = max(mx, max(max(absbits(a.x), absbits(a.y)),
-                                     max(absbits(b.x), absbits(b.y))));
+                    fe[frow0 + i] = static_cast<signed char>(ef[i]);
                 }
+                mbar_arrive(smem_u32(&ctl.eready[k % kExpBufs]));
             }
-            mx = __reduce_max_sync(0xFFFFFFFFu, mx);
-            const int rb = k & 1;
-            if (lane == 0) {
-                ctl.warp_max[rb][warp] = mx;
-                mbar_arrive(smem_u32(&ctl.reduce[rb]));
-            }
-            if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (k >> 1) & 1, fault,
-                                   kFaultStageEmpty, abort)) {
-                return false;
-            }
-            uint32_t tmax = 0;
-#pragma unroll
-            for (int w = 0; w < kWorkerWarps; ++w) {
-                tmax = max(tmax, ctl.warp_max[rb][w]);
-            }
-            const int eu = scale_exponent(tmax);
-            if (k & 1) {
-                eu_odd = eu;
-            } else {
-                eu_even = eu;
-            }
-            const float fa = exp2i(eu / 2);
-            const float fb = exp2i(eu - eu / 2);
             if (!mbar_wait_bounded(smem_u32(&ctl.empty), (k & 1) ^ 1, fault, kFaultStageEmpty,
                                    abort)) {
                 return false;
@@ -379,20 +378,19 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             const uint32_t off_re = static_cast<uint32_t>(kre >> 3) * kPlane + (kre & 7) * 2u;
             const uint32_t off_im = static_cast<uint32_t>(kim >> 3) * kPlane + (kim & 7) * 2u;
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-#pragma unroll
-                for (int i = 0; i < kR; ++i) {
-                    const float2 a = unpack2(u0[h][i]);
-                    const float2 b = unpack2(u1[h][i]);
-                    uint32_t re_hi, re_lo, im_hi, im_lo;
-                    split2(a.x * fa * fb, b.x * fa * fb, re_hi, re_lo);
-                    split2(a.y * fa * fb, b.y * fa * fb, im_hi, im_lo);
-                    const uint32_t row = static_cast<uint32_t>(kHalf * h + kR * fgroup + i) * 16u;
-                    sts32(sbase + lay.a_hi + off_re + row, re_hi);
-                    sts32(sbase + lay.a_lo + off_re + row, re_lo);
-                    sts32(sbase + lay.a_hi + off_im + row, im_hi);
-                    sts32(sbase + lay.a_lo + off_im + row, im_lo);
-                }
+            for (int i = 0; i < kR; ++i) {
+                const float2 a = unpack2(u0[i]);
+                const float2 b = unpack2(u1[i]);
+                const float fa = exp2i(ef[i] / 2);
+                const float fb = exp2i(ef[i] - ef[i] / 2);
+                uint32_t re_hi, re_lo, im_hi, im_lo;
+                split2(a.x * fa * fb, b.x * fa * fb, re_hi, re_lo);
+                split2(a.y * fa * fb, b.y * fa * fb, im_hi, im_lo);
+                const uint32_t row = static_cast<uint32_t>(frow0 + i) * 16u;
+                sts32(sbase + lay.a_hi + off_re + row, re_hi);
+                sts32(sbase + lay.a_lo + off_re + row, re_lo);
+                sts32(sbase + lay.a_hi + off_im + row, im_hi);
+                sts32(sbase + lay.a_lo + off_im + row, im_lo);
             }
             fence_proxy_async_smem();
             __syncwarp();
@@ -443,9 +441,12 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             if (lane == 0) {
                 mbar_arrive(smem_u32(&ctl.dempty[db]));
             }
-            const int shift = -(((k & 1) ? eu_odd : eu_even) + kWExp);
-            const float fa = exp2i(shift / 2);
-            const float fb = exp2i(shift - shift / 2);
+            // The frames' exponents (written before the tile's operand, long since complete).
+            if (!mbar_wait_bounded(smem_u32(&ctl.eready[k % kExpBufs]), (k / kExpBufs) & 1,
+                                   fault, kFaultScale, abort)) {
+                break;
+            }
+            const volatile signed char* fe = ctl.fexp[k % kExpBufs];
             // Four lanes per frame write its channels 16 slice + 8 jj + 2 (lane % 4), + 1: each
             // store fills 64 contiguous bytes of eight frames.
             const long long t_base = static_cast<long long>(tile_of(k)) * kFrames + quarter * 32 +
@@ -455,6 +456,9 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
 #pragma unroll
                 for (int s = 0; s < 2; ++s) {
                     const long long t = t_base + 16 * r + 8 * s;
+                    const int shift = -(fe[quarter * 32 + (lane >> 2) + 16 * r + 8 * s] + kWExp);
+                    const float fa = exp2i(shift / 2);
+                    const float fb = exp2i(shift - shift / 2);
                     if (t < frames) {
 #pragma unroll
                         for (int jj = 0; jj < 2; ++jj) {
