@@ -599,6 +599,35 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def magnitude_fusion(rfx, w, args, dist, device) -> dict:
+    """Steps of |channelize(x)| on the tensor-core plan: fused (rfx_channelize_magnitude_launch,
+    4 bytes written per output) against channelize then rfx_magnitude_launch (the complex
+    outputs written, read back, and the magnitudes written)."""
+    import torch
+
+    n = int(w.x.size)
+    f = rfx.frames(n, w.channels)
+    xs = [torch.from_numpy(w.x).to(device) for _ in range(2)]
+    h = torch.from_numpy(w.taps).to(device)
+    mags = [torch.empty((f, w.channels), dtype=torch.float32, device=device) for _ in range(2)]
+    z = torch.empty((f, w.channels), dtype=torch.complex64, device=device)
+    out = {}
+    with rfx.ChanPlan(w.channels, n, "tc_split") as plan:
+        def fused(i):
+            plan.launch_magnitude(xs[i % 2], h, mags[i % 2])
+
+        def unfused(i):
+            plan.launch(xs[i % 2], h, z)
+            rfx.magnitude_launch(z, mags[i % 2])
+
+        for name, fn in (("fused", fused), ("unfused", unfused)):
+            s = time_device(fn, args.steps, args.warmup, dist, device)
+            out[name] = {"ms_per_step": s / args.steps * 1e3,
+                         "msamples_s": n * args.steps / s / 1e6}
+    out["speedup_fused"] = out["unfused"]["ms_per_step"] / out["fused"]["ms_per_step"]
+    return out
+
+
 # --- our arm ---------------------------------------------------------------------------------
 
 def measure_arms(rfx, w, impls, args, dist, device, sample_clocks=False):
@@ -700,6 +729,10 @@ def run_ours(args) -> None:
                for k, v in arms.items()}
     if "plain" in arms and impl != "plain":
         extras["speedup_vs_plain_fp32"] = value / arms["plain"]["msamples_s"]
+
+    # channelize |> magnitude: fused in the tensor-core epilogue vs the two kernels in turn.
+    if w.channels and "tc_split" in arms:
+        extras["channelize_magnitude"] = magnitude_fusion(rfx, w, args, dist, device)
 
     # The other headline workload (64-channel PFB) in the same run.
     if args.workload == "fir1025" and not args.no_secondary:

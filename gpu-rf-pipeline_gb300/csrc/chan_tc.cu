@@ -38,6 +38,7 @@
 // behind the branch sums and those of tile k + 1 behind the drain. Every wait is a bounded
 // mbarrier wait.
 #include "chan_tc.cuh"
+#include "magnitude.cuh"
 #include "tc_common.cuh"
 #include "tmap.hpp"
 
@@ -168,11 +169,13 @@ __device__ __forceinline__ void branch_group(f32x2 (&acc)[kR], const f32x2 (&cur
 
 }  // namespace
 
-template <bool kTapsSmem>
+// kMag: the output is |z| (float per channel, frames x 64) instead of z (cf32), computed from
+// the same floats z would hold.
+template <bool kTapsSmem, bool kMag>
 __global__ void __launch_bounds__(kThreads, 1)
 chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict__ x,
                const float* __restrict__ taps, const uint16_t* __restrict__ w_img,
-               float2* __restrict__ z, long long n, long long frames, int num_taps,
+               void* __restrict__ out, long long n, long long frames, int num_taps,
                int num_tiles)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -464,10 +467,19 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
                         for (int jj = 0; jj < 2; ++jj) {
                             const float* a = &v[r][4 * (2 * jj) + 2 * s];
                             const float* b = &v[r][4 * (2 * jj + 1) + 2 * s];
-                            *reinterpret_cast<float4*>(z + t * kM + 16 * slice + 8 * jj +
-                                                       2 * (lane & 3)) =
-                                make_float4(a[0] * fa * fb, a[1] * fa * fb, b[0] * fa * fb,
-                                            b[1] * fa * fb);
+                            const long long o = t * kM + 16 * slice + 8 * jj + 2 * (lane & 3);
+                            const float re0 = a[0] * fa * fb;
+                            const float im0 = a[1] * fa * fb;
+                            const float re1 = b[0] * fa * fb;
+                            const float im1 = b[1] * fa * fb;
+                            if constexpr (kMag) {
+                                // Channels c, c + 1 of the frame: 8 bytes, four lanes 32.
+                                *reinterpret_cast<float2*>(static_cast<float*>(out) + o) =
+                                    make_float2(cmag(re0, im0), cmag(re1, im1));
+                            } else {
+                                *reinterpret_cast<float4*>(static_cast<float2*>(out) + o) =
+                                    make_float4(re0, im0, re1, im1);
+                            }
                         }
                     }
                 }
@@ -585,7 +597,7 @@ cudaError_t chan_tc_build_twiddles(void* img, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-template <bool kTapsSmem>
+template <bool kTapsSmem, bool kMag>
 static cudaError_t launch_chan(const void* x, const float* taps, const void* twiddles, void* z,
                                long long n, long long frames, int num_taps, cudaStream_t stream)
 {
@@ -600,13 +612,13 @@ static cudaError_t launch_chan(const void* x, const float* taps, const void* twi
     }
     const uint32_t bytes = lay.bytes > 120u * 1024u ? lay.bytes : 120u * 1024u;
     cudaFuncAttributes attr{};
-    if ((err = cudaFuncGetAttributes(&attr, chan_tc_kernel<kTapsSmem>)) != cudaSuccess) {
+    if ((err = cudaFuncGetAttributes(&attr, chan_tc_kernel<kTapsSmem, kMag>)) != cudaSuccess) {
         return err;
     }
     if (attr.maxThreadsPerBlock < kThreads) {
         return cudaErrorLaunchOutOfResources;
     }
-    err = cudaFuncSetAttribute(chan_tc_kernel<kTapsSmem>,
+    err = cudaFuncSetAttribute(chan_tc_kernel<kTapsSmem, kMag>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(bytes));
     if (err != cudaSuccess) {
@@ -621,14 +633,14 @@ static cudaError_t launch_chan(const void* x, const float* taps, const void* twi
     }
     const int tiles = static_cast<int>((frames + kFrames - 1) / kFrames);
     const int grid = tiles < sms ? tiles : sms;
-    chan_tc_kernel<kTapsSmem><<<grid, kThreads, bytes, stream>>>(
+    chan_tc_kernel<kTapsSmem, kMag><<<grid, kThreads, bytes, stream>>>(
         map, static_cast<const float2*>(x), taps, static_cast<const uint16_t*>(twiddles),
-        static_cast<float2*>(z), n, frames, num_taps, tiles);
+        z, n, frames, num_taps, tiles);
     return cudaGetLastError();
 }
 
 cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddles, void* z,
-                           long long n, int num_taps, cudaStream_t stream)
+                           long long n, int num_taps, cudaStream_t stream, bool magnitude)
 {
     const long long frames = (n + kM - 1) / kM;
     if (frames == 0) {
@@ -637,10 +649,15 @@ cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddle
     if (n < kM) {
         return cudaErrorInvalidValue;  // the caller routes inputs shorter than a frame elsewhere
     }
-    if (chan_layout(num_taps).P <= kSmemTapsMax) {
-        return launch_chan<true>(x, taps, twiddles, z, n, frames, num_taps, stream);
+    const bool smem_taps = chan_layout(num_taps).P <= kSmemTapsMax;
+    if (magnitude) {
+        return smem_taps
+                   ? launch_chan<true, true>(x, taps, twiddles, z, n, frames, num_taps, stream)
+                   : launch_chan<false, true>(x, taps, twiddles, z, n, frames, num_taps, stream);
     }
-    return launch_chan<false>(x, taps, twiddles, z, n, frames, num_taps, stream);
+    return smem_taps
+               ? launch_chan<true, false>(x, taps, twiddles, z, n, frames, num_taps, stream)
+               : launch_chan<false, false>(x, taps, twiddles, z, n, frames, num_taps, stream);
 }
 
 cudaError_t chan_tc_take_fault(unsigned int* code)

@@ -9,6 +9,7 @@
 #include "fir_plain.cuh"
 #include "fir_tc.cuh"
 #include "fir_tc2.cuh"
+#include "magnitude.cuh"
 #include "tuning.hpp"
 
 #include <cuda_runtime.h>
@@ -159,6 +160,12 @@ int set_last_error(int status, const char* message) { return fail(status, "%s", 
 
 }  // namespace rfx
 
+struct rfx_chan_plan;
+namespace {
+int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
+                    int64_t num_samples, int num_taps, cudaStream_t stream, bool magnitude);
+}  // namespace
+
 struct rfx_chan_plan {
     int impl;
     int channels;
@@ -166,6 +173,7 @@ struct rfx_chan_plan {
     cufftHandle fft;
     bool has_fft;
     void* twiddles;       // tensor core: the DFT operand image, built once in FP64
+    void* scratch;        // plain: channel outputs before their magnitude (first such call)
 };
 
 extern "C" {
@@ -416,7 +424,7 @@ int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_p
                     static_cast<long long>(max_samples), static_cast<long long>(kMaxSamples));
     }
     auto* p = new rfx_chan_plan{impl, channels, rfx_channelize_frames(max_samples, channels), 0,
-                                false, nullptr};
+                                false, nullptr, nullptr};
     if (impl == RFX_CHAN_TC) {
         if (!rfx::chan_tc_supported(channels, 1)) {
             delete p;
@@ -465,12 +473,54 @@ int rfx_chan_plan_destroy(rfx_chan_plan* plan)
     if (plan->twiddles != nullptr) {
         cudaFree(plan->twiddles);
     }
+    if (plan->scratch != nullptr) {
+        cudaFree(plan->scratch);
+    }
     delete plan;
     return r == CUFFT_SUCCESS ? RFX_OK : cufft_fail(r, "cufftDestroy");
 }
 
 int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
                           int64_t num_samples, int num_taps, cudaStream_t stream)
+{
+    return channelize_plan(plan, x, taps, out, num_samples, num_taps, stream, false);
+}
+
+int rfx_channelize_magnitude_launch(rfx_chan_plan* plan, const void* x, const float* taps,
+                                    float* mag, int64_t num_samples, int num_taps,
+                                    cudaStream_t stream)
+{
+    return channelize_plan(plan, x, taps, mag, num_samples, num_taps, stream, true);
+}
+
+int rfx_magnitude_launch(const void* x, float* mag, int64_t num_samples, cudaStream_t stream)
+{
+    if (num_samples < 0 || num_samples > kMaxSamples) {
+        return fail(RFX_ERR_INVALID, "magnitude: %lld samples, expected 0 to %lld",
+                    static_cast<long long>(num_samples), static_cast<long long>(kMaxSamples));
+    }
+    if (num_samples == 0) {
+        return RFX_OK;
+    }
+    if (x == nullptr || mag == nullptr) {
+        return fail(RFX_ERR_INVALID, "magnitude: null pointer");
+    }
+    if (!aligned16(x) || !aligned16(mag)) {
+        return fail(RFX_ERR_ALIGNMENT, "magnitude: buffers must be 16-byte aligned");
+    }
+    const cudaError_t err = rfx::magnitude_launch(x, mag, num_samples, stream);
+    return err == cudaSuccess ? RFX_OK : cuda_fail(err, "magnitude_launch");
+}
+
+}  // extern "C"
+
+namespace {
+
+// The channelizer through a plan; with `magnitude`, `out` receives |z| (float per channel):
+// the tensor-core form computes it in its epilogue, the plain form runs the magnitude kernel
+// over the channel outputs in the plan's scratch buffer (allocated by the first such call).
+int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
+                    int64_t num_samples, int num_taps, cudaStream_t stream, bool magnitude)
 {
     if (plan == nullptr) {
         return fail(RFX_ERR_INVALID, "channelize: null plan");
@@ -504,14 +554,26 @@ int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps,
                         num_taps);
         }
         const cudaError_t err = rfx::chan_tc_launch(x, taps, plan->twiddles, out, num_samples,
-                                                    num_taps, stream);
+                                                    num_taps, stream, magnitude);
         return err == cudaSuccess ? RFX_OK : cuda_fail(err, "chan_tc_launch");
     }
     if (frames != plan->frames) {
         return fail(RFX_ERR_INVALID, "channelize: plan made for %lld frames, call has %lld",
                     static_cast<long long>(plan->frames), static_cast<long long>(frames));
     }
-    cudaError_t err = rfx::chan_branch_launch(x, taps, out, frames, plan->channels, num_taps,
+    void* z = out;
+    if (magnitude) {
+        if (plan->scratch == nullptr) {
+            const cudaError_t e = cudaMalloc(&plan->scratch, static_cast<size_t>(plan->frames) *
+                                                                 plan->channels * 8u);
+            if (e != cudaSuccess) {
+                plan->scratch = nullptr;
+                return cuda_fail(e, "cudaMalloc (channelizer scratch)");
+            }
+        }
+        z = plan->scratch;
+    }
+    cudaError_t err = rfx::chan_branch_launch(x, taps, z, frames, plan->channels, num_taps,
                                               stream);
     if (err != cudaSuccess) {
         return cuda_fail(err, "chan_branch_launch");
@@ -520,10 +582,21 @@ int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps,
     if (r != CUFFT_SUCCESS) {
         return cufft_fail(r, "cufftSetStream");
     }
-    r = cufftExecC2C(plan->fft, static_cast<cufftComplex*>(out), static_cast<cufftComplex*>(out),
+    r = cufftExecC2C(plan->fft, static_cast<cufftComplex*>(z), static_cast<cufftComplex*>(z),
                      CUFFT_INVERSE);
-    return r == CUFFT_SUCCESS ? RFX_OK : cufft_fail(r, "cufftExecC2C");
+    if (r != CUFFT_SUCCESS) {
+        return cufft_fail(r, "cufftExecC2C");
+    }
+    if (magnitude) {
+        err = rfx::magnitude_launch(z, static_cast<float*>(out), frames * plan->channels, stream);
+        return err == cudaSuccess ? RFX_OK : cuda_fail(err, "magnitude_launch");
+    }
+    return RFX_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int rfx_channelize_branches(const void* x, const float* taps, void* u, int64_t num_samples,
                             int channels, int num_taps, cudaStream_t stream)
@@ -765,6 +838,83 @@ int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const f
                                          num_samples, num_taps, nullptr);
         },
         [&] { return copy(z_iq, dz.p, zbytes, cudaMemcpyDeviceToHost); });
+}
+
+int rfx_magnitude_host(const void* x_iq, int64_t num_samples, float* mag, rfx_bench* bench)
+{
+    if (num_samples < 0 || num_samples > kMaxSamples) {
+        return fail(RFX_ERR_INVALID, "magnitude: %lld samples, expected 0 to %lld",
+                    static_cast<long long>(num_samples), static_cast<long long>(kMaxSamples));
+    }
+    if (num_samples == 0) {
+        return RFX_OK;
+    }
+    if (x_iq == nullptr || mag == nullptr) {
+        return fail(RFX_ERR_INVALID, "magnitude: null host pointer");
+    }
+    DeviceMem dx, dm;
+    const size_t xbytes = static_cast<size_t>(num_samples) * 8;
+    const size_t mbytes = static_cast<size_t>(num_samples) * 4;
+    cudaError_t err;
+    if ((err = cudaMalloc(&dx.p, xbytes)) != cudaSuccess ||
+        (err = cudaMalloc(&dm.p, mbytes)) != cudaSuccess) {
+        return cuda_fail(err, "cudaMalloc");
+    }
+    return timed_passes(
+        bench, [&] { return copy(dx.p, x_iq, xbytes, cudaMemcpyHostToDevice); },
+        [&] { return rfx_magnitude_launch(dx.p, static_cast<float*>(dm.p), num_samples, nullptr); },
+        [&] { return copy(mag, dm.p, mbytes, cudaMemcpyDeviceToHost); });
+}
+
+int rfx_channelize_magnitude_host(int impl, const void* x_iq, int64_t num_samples,
+                                  const float* taps, int num_taps, int channels, float* mag,
+                                  rfx_bench* bench)
+{
+    if (channels < 1) {
+        return fail(RFX_ERR_INVALID, "channelize: need at least one channel");
+    }
+    if (num_taps < 1) {
+        return fail(RFX_ERR_INVALID, "channelize: need at least one tap");
+    }
+    const int64_t frames = rfx_channelize_frames(num_samples, channels);
+    if (frames == 0) {
+        return RFX_OK;
+    }
+    if (x_iq == nullptr || mag == nullptr || taps == nullptr) {
+        return fail(RFX_ERR_INVALID, "channelize: null host pointer");
+    }
+    rfx_chan_plan* plan = nullptr;
+    int rc = rfx_chan_plan_create(impl, channels, num_samples, &plan);
+    if (rc != RFX_OK) {
+        return rc;
+    }
+    struct PlanGuard {
+        rfx_chan_plan* p;
+        ~PlanGuard() { rfx_chan_plan_destroy(p); }
+    } guard{plan};
+    DeviceMem dx, dm, dh;
+    const size_t xbytes = static_cast<size_t>(num_samples) * 8;
+    const size_t mbytes = static_cast<size_t>(frames) * channels * 4;
+    cudaError_t err;
+    if ((err = cudaMalloc(&dx.p, xbytes)) != cudaSuccess ||
+        (err = cudaMalloc(&dm.p, mbytes)) != cudaSuccess ||
+        (err = cudaMalloc(&dh.p, sizeof(float) * num_taps)) != cudaSuccess) {
+        return cuda_fail(err, "cudaMalloc");
+    }
+    return timed_passes(
+        bench,
+        [&] {
+            int r = copy(dx.p, x_iq, xbytes, cudaMemcpyHostToDevice);
+            return r != RFX_OK ? r
+                               : copy(dh.p, taps, sizeof(float) * num_taps,
+                                      cudaMemcpyHostToDevice);
+        },
+        [&] {
+            return rfx_channelize_magnitude_launch(plan, dx.p, static_cast<const float*>(dh.p),
+                                                   static_cast<float*>(dm.p), num_samples,
+                                                   num_taps, nullptr);
+        },
+        [&] { return copy(mag, dm.p, mbytes, cudaMemcpyDeviceToHost); });
 }
 
 }  // extern "C"

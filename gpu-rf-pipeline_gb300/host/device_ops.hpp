@@ -33,6 +33,9 @@ void fir_batched_device(FirImpl impl, const cf32* const* x, cf32* const* y,
 void fir_naive_batched_device(const cf32* const* x, cf32* const* y, const int* num_samples,
                               int count, const float* taps, int num_taps);
 
+// mag[n] = |x[n]| for n < num_samples, on the legacy default stream (src/device_ops.hpp:57).
+void magnitude_device(const cf32* x, float* mag, int num_samples);
+
 int channelize_frames(int num_samples, int channels);
 
 // The project's signature: branch sums into `out`, then `plan` (a batched FftPlan of `channels`
@@ -43,3 +46,8 @@ void channelize_device(cufftHandle plan, const cf32* x, const float* taps, cf32*
 // Any implementation through an rfx_chan_plan (rfx_chan_plan_create).
 void channelize_device(rfx_chan_plan* plan, const cf32* x, const float* taps, cf32* out,
                        int num_samples, int num_taps, cudaStream_t stream = nullptr);
+
+// channelize |> magnitude through a plan: mag is frames x channels floats.
+void channelize_magnitude_device(rfx_chan_plan* plan, const cf32* x, const float* taps,
+                                 float* mag, int num_samples, int num_taps,
+                                 cudaStream_t stream = nullptr);

@@ -3,6 +3,8 @@
 //
 //   rfgpu fir        --in X.cf32 --taps H.f32 --out Y.cf32 [--impl NAME] [--block B]
 //   rfgpu channelize --in X.cf32 --taps H.f32 --channels M --out Z.cf32 [--impl NAME]
+//                    [--output complex|magnitude]   (magnitude: |z| as float32, fused)
+//   rfgpu magnitude  --in X.cf32 --out MAG.f32
 //   rfgpu stream     --in X.cf32 --taps H.f32 --out Y.cf32 [--impl NAME] [--chunk N]
 //                    [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]
 //   rfgpu info
@@ -64,6 +66,9 @@ void print_usage()
                  "[--block B]\n"
                  "  rfgpu channelize --in X.cf32 --taps H.f32 --channels M --out OUT.cf32 "
                  "[--impl NAME]\n"
+                 "                  [--output complex|magnitude]  magnitude: |z| per channel as "
+                 "float32\n"
+                 "  rfgpu magnitude  --in X.cf32 --out OUT.f32\n"
                  "  rfgpu stream     --in X.cf32 --taps H.f32 --out OUT.cf32 [--impl NAME] "
                  "[--chunk N]\n"
                  "                  [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]\n"
@@ -74,7 +79,7 @@ void print_usage()
                  "NAME.sigmf-data)\n"
                  "in cf32_le, ci16_le or ci8; fir converts integer recordings on the GPU.\n"
                  "\n"
-                 "benchmark options (fir, channelize, stream):\n"
+                 "benchmark options (fir, channelize, magnitude, stream):\n"
                  "  --bench N      time N runs with CUDA events and print the result as JSON\n"
                  "  --warmup W     untimed runs before measuring (default 3, needs --bench)\n"
                  "\n"
@@ -180,13 +185,29 @@ std::string gpu_name()
     return prop.name;
 }
 
+void report(const Args& args, const char* op, const char* impl, std::size_t num_in,
+            std::size_t num_out, const Bench& bench);
+
 void finish(const Args& args, const char* op, const char* impl, std::size_t num_in,
             const std::vector<cf32>& out, const Bench& bench)
 {
+    write_cf32(args.required("--out"), out);
+    report(args, op, impl, num_in, out.size(), bench);
+}
+
+void finish_f32(const Args& args, const char* op, const char* impl, std::size_t num_in,
+                const std::vector<float>& out, const Bench& bench)
+{
+    write_f32(args.required("--out"), out);
+    report(args, op, impl, num_in, out.size(), bench);
+}
+
+void report(const Args& args, const char* op, const char* impl, std::size_t num_in,
+            std::size_t num_out, const Bench& bench)
+{
     const std::string& path = args.required("--out");
-    write_cf32(path, out);
     if (!args.has("--bench")) {
-        std::printf("%s[%s]: %zu samples in, %zu out -> %s\n", op, impl, num_in, out.size(),
+        std::printf("%s[%s]: %zu samples in, %zu out -> %s\n", op, impl, num_in, num_out,
                     path.c_str());
         return;
     }
@@ -196,7 +217,7 @@ void finish(const Args& args, const char* op, const char* impl, std::size_t num_
                 "\"h2d_ms\": {\"mean\": %.6f, \"std\": %.6f}, "
                 "\"kernel_ms\": {\"mean\": %.6f, \"std\": %.6f}, "
                 "\"d2h_ms\": {\"mean\": %.6f, \"std\": %.6f}}\n",
-                op, impl, gpu_name().c_str(), num_in, out.size(), bench.config().runs,
+                op, impl, gpu_name().c_str(), num_in, num_out, bench.config().runs,
                 bench.config().warmup, r.h2d.mean_ms, r.h2d.std_ms, r.kernel.mean_ms,
                 r.kernel.std_ms, r.d2h.mean_ms, r.d2h.std_ms);
 }
@@ -237,14 +258,18 @@ int run_fir(int argc, char** argv)
 
 int run_channelize(int argc, char** argv)
 {
-    const Args args(argc, argv,
-                    {"--in", "--taps", "--channels", "--out", "--impl", "--bench", "--warmup"});
+    const Args args(argc, argv, {"--in", "--taps", "--channels", "--out", "--impl", "--output",
+                                 "--bench", "--warmup"});
     args.required("--out");
     if (!args.has("--channels")) {
         throw UsageError("missing required option --channels");
     }
     const int channels = args.integer("--channels", 0, 1);
     const Impl<ChanFn>& impl = find_impl(channelize_impls(), args, "channelize");
+    const std::string output = args.optional("--output", "complex");
+    if (output != "complex" && output != "magnitude") {
+        throw UsageError("unknown --output '" + output + "' (available: complex, magnitude)");
+    }
     Bench bench(bench_config(args));
     const std::vector<cf32> x = read_cf32(args.required("--in"));
     const std::vector<float> taps = read_f32(args.required("--taps"));
@@ -253,7 +278,25 @@ int run_channelize(int argc, char** argv)
     }
     require_int_range(x.size() + static_cast<std::size_t>(channels), "padded channelizer input");
     require_int_range(taps.size(), "tap array");
+    if (output == "magnitude") {
+        finish_f32(args, "channelize", impl.name, x.size(),
+                   channelize_magnitude(impl.name, x, taps, channels, bench), bench);
+        return 0;
+    }
     finish(args, "channelize", impl.name, x.size(), impl.fn(x, taps, channels, bench), bench);
+    return 0;
+}
+
+// |x| of every sample (src/main.cpp:255-267).
+int run_magnitude(int argc, char** argv)
+{
+    const Args args(argc, argv, {"--in", "--out", "--bench", "--warmup"});
+    args.required("--out");
+    Bench bench(bench_config(args));
+    const std::vector<cf32> x = read_cf32(args.required("--in"));
+    require_int_range(x.size(), "magnitude input");
+    const std::vector<float> mag = x.empty() ? std::vector<float>() : magnitude_cuda(x, bench);
+    finish_f32(args, "magnitude", "elementwise", x.size(), mag, bench);
     return 0;
 }
 
@@ -347,7 +390,8 @@ int run_info(int argc, char** argv)
     std::printf("{\"gpu\": \"%s\", \"compute_capability\": \"%d.%d\", \"memory_mb\": %zu, "
                 "\"sms\": %d, \"cuda_runtime\": \"%s\", \"cuda_driver\": \"%s\", "
                 "\"library\": \"%s\", "
-                "\"impls\": {\"fir\": [\"%s\"], \"channelize\": [\"%s\"]}}\n",
+                "\"impls\": {\"fir\": [\"%s\"], \"channelize\": [\"%s\"], "
+                "\"magnitude\": [\"elementwise\"]}}\n",
                 prop.name, prop.major, prop.minor, prop.totalGlobalMem / (1024 * 1024),
                 prop.multiProcessorCount, version_string(runtime).c_str(),
                 version_string(driver).c_str(), rfx_version(),
@@ -365,6 +409,7 @@ int main(int argc, char** argv)
         if (op == "fir") return run_fir(argc, argv);
         if (op == "channelize") return run_channelize(argc, argv);
         if (op == "stream") return run_stream(argc, argv);
+        if (op == "magnitude") return run_magnitude(argc, argv);
         if (op == "info") return run_info(argc, argv);
         if (op == "--help" || op == "-h" || op == "help") {
             print_usage();

@@ -107,6 +107,67 @@ void channelize_device(rfx_chan_plan* plan, const cf32* x, const float* taps, cf
     RFX_CHECK(rfx_channelize_launch(plan, x, taps, out, num_samples, num_taps, stream));
 }
 
+void channelize_magnitude_device(rfx_chan_plan* plan, const cf32* x, const float* taps,
+                                 float* mag, int num_samples, int num_taps, cudaStream_t stream)
+{
+    RFX_CHECK(rfx_channelize_magnitude_launch(plan, x, taps, mag, num_samples, num_taps, stream));
+}
+
+void magnitude_device(const cf32* x, float* mag, int num_samples)
+{
+    RFX_CHECK(rfx_magnitude_launch(x, mag, num_samples, nullptr));
+}
+
+std::vector<float> magnitude_cuda(const std::vector<cf32>& x, Bench& bench)
+{
+    const int num_samples = static_cast<int>(x.size());
+    std::vector<float> mag(x.size());
+    DeviceBuffer<cf32> d_x(x.size());
+    DeviceBuffer<float> d_mag(mag.size());
+    bench.run([&] { d_x.upload(x.data(), x.size()); },
+              [&] { magnitude_device(d_x.get(), d_mag.get(), num_samples); },
+              [&] { d_mag.download(mag.data(), mag.size()); });
+    return mag;
+}
+
+std::vector<float> channelize_magnitude(const char* impl_name, const std::vector<cf32>& x,
+                                        const std::vector<float>& taps, int channels,
+                                        Bench& bench)
+{
+    int impl = 0;
+    RFX_CHECK(rfx_parse_chan_impl(impl_name, &impl));
+    if (channels < 1) {
+        throw std::runtime_error("channelize: need at least one channel");
+    }
+    const int num_samples = static_cast<int>(x.size());
+    const int num_taps = static_cast<int>(taps.size());
+    const int frames = channelize_frames(num_samples, channels);
+    std::vector<float> mag(static_cast<std::size_t>(frames) * static_cast<std::size_t>(channels));
+    if (frames == 0) {
+        return mag;
+    }
+    rfx_chan_plan* plan = nullptr;
+    RFX_CHECK(rfx_chan_plan_create(impl, channels, num_samples, &plan));
+    struct PlanGuard {
+        rfx_chan_plan* p;
+        ~PlanGuard() { rfx_chan_plan_destroy(p); }
+    } guard{plan};
+    DeviceBuffer<cf32> d_x(x.size());
+    DeviceBuffer<float> d_h(taps.size());
+    DeviceBuffer<float> d_mag(mag.size());
+    bench.run(
+        [&] {
+            d_x.upload(x.data(), x.size());
+            d_h.upload(taps.data(), taps.size());
+        },
+        [&] {
+            channelize_magnitude_device(plan, d_x.get(), d_h.get(), d_mag.get(), num_samples,
+                                        num_taps);
+        },
+        [&] { d_mag.download(mag.data(), mag.size()); });
+    return mag;
+}
+
 // ---- host-vector operations ----------------------------------------------------------------
 
 namespace {

@@ -35,6 +35,15 @@ std::vector<cf32> fir_stored(const char* impl, const StoredSamples& x,
 std::vector<cf32> channelize_cuda(const std::vector<cf32>& x, const std::vector<float>& taps,
                                   int channels, Bench& bench);
 
+// mag[n] = |x[n]| (src/ops.hpp:27-29): one float per complex sample.
+std::vector<float> magnitude_cuda(const std::vector<cf32>& x, Bench& bench);
+
+// |channelize(x)| in one pass: frames x channels floats. `impl` is a channelize_impls() name;
+// the tensor-core form takes the magnitude in its epilogue (rfx_channelize_magnitude_launch).
+std::vector<float> channelize_magnitude(const char* impl, const std::vector<cf32>& x,
+                                        const std::vector<float>& taps, int channels,
+                                        Bench& bench);
+
 // The channelizer's implementations, selectable with --impl (the project has one).
 using ChanFn = std::vector<cf32> (*)(const std::vector<cf32>& x, const std::vector<float>& taps,
                                      int channels, Bench& bench);

@@ -70,11 +70,16 @@ SIGNATURES = {
     "rfx_channelize_launch": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _VP]),
     "rfx_channelize_branches": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
     "rfx_channelize_tc_static": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
+    "rfx_channelize_magnitude_launch": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _VP]),
+    "rfx_magnitude_launch": (_I, [_VP, _VP, _I64, _VP]),
     "rfx_fir_stream": (_I, [_VP, _I64, _VP, _I, ctypes.POINTER(StreamConfig), _VP,
                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
     "rfx_fir_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_fir_host_format": (_I, [_I, _I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_channelize_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
+    "rfx_channelize_magnitude_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP,
+                                           ctypes.POINTER(Bench)]),
+    "rfx_magnitude_host": (_I, [_VP, _I64, _VP, ctypes.POINTER(Bench)]),
     "rfx_autotune_fir": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),
     "rfx_autotune_save": (_I, [ctypes.c_char_p]),
     "rfx_autotune_load": (_I, [ctypes.c_char_p]),
@@ -235,6 +240,13 @@ class ChanPlan:
                                             out.data_ptr(), n, taps.numel(),
                                             _stream_ptr(stream)))
 
+    def launch_magnitude(self, x, taps, mag, stream=None, num_samples: int | None = None) -> None:
+        """mag[t][k] = |z[t][k]|: float32 (frames, channels)."""
+        n = x.numel() if num_samples is None else int(num_samples)
+        _check(load().rfx_channelize_magnitude_launch(self.handle, x.data_ptr(), taps.data_ptr(),
+                                                      mag.data_ptr(), n, taps.numel(),
+                                                      _stream_ptr(stream)))
+
     def close(self) -> None:
         if self.handle:
             _check(load().rfx_chan_plan_destroy(self.handle))
@@ -267,6 +279,33 @@ def channelize(x, taps, channels: int, impl="plain", stream=None):
         plan.launch(x, taps, out, stream)
         torch.cuda.current_stream().synchronize()
     return out
+
+
+def channelize_magnitude(x, taps, channels: int, impl="plain", stream=None):
+    """Returns the (frames, channels) float32 CUDA tensor |channelize(x)|."""
+    import torch
+
+    f = frames(x.numel(), channels)
+    mag = torch.empty((f, channels), dtype=torch.float32, device=x.device)
+    with ChanPlan(channels, x.numel(), impl) as plan:
+        plan.launch_magnitude(x, taps, mag, stream)
+        torch.cuda.current_stream().synchronize()
+    return mag
+
+
+def magnitude_launch(x, mag, stream=None, num_samples: int | None = None) -> None:
+    """mag[:n] = |x[:n]| on the GPU: x complex64, mag float32 CUDA tensors."""
+    n = x.numel() if num_samples is None else int(num_samples)
+    _check(load().rfx_magnitude_launch(x.data_ptr(), mag.data_ptr(), n, _stream_ptr(stream)))
+
+
+def magnitude(x, stream=None):
+    """Returns a new float32 CUDA tensor |x| of x's shape."""
+    import torch
+
+    mag = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+    magnitude_launch(x, mag, stream)
+    return mag
 
 
 def channelize_branches(x, taps, channels: int, stream=None):
@@ -313,6 +352,33 @@ def channelize_host(impl, x, taps, channels: int, warmup: int = 0, runs: int = 1
     _check(load().rfx_channelize_host(impl_v, x.ctypes.data, x.size, taps.ctypes.data,
                                       taps.size, channels, z.ctypes.data, ctypes.byref(b)))
     return z.reshape(f, channels), b
+
+
+def channelize_magnitude_host(impl, x, taps, channels: int, warmup: int = 0, runs: int = 1):
+    """|channelize| on host NumPy arrays. Returns ((frames, channels) float32, Bench)."""
+    import numpy as np
+
+    x = np.ascontiguousarray(x, dtype=np.complex64)
+    taps = np.ascontiguousarray(taps, dtype=np.float32)
+    f = frames(x.size, channels)
+    mag = np.empty(f * channels, dtype=np.float32)
+    impl_v = parse_chan_impl(impl) if isinstance(impl, str) else int(impl)
+    b = Bench(warmup=warmup, runs=runs)
+    _check(load().rfx_channelize_magnitude_host(impl_v, x.ctypes.data, x.size, taps.ctypes.data,
+                                                taps.size, channels, mag.ctypes.data,
+                                                ctypes.byref(b)))
+    return mag.reshape(f, channels), b
+
+
+def magnitude_host(x, warmup: int = 0, runs: int = 1):
+    """|x| on a host NumPy array (complex64). Returns (float32 array, Bench)."""
+    import numpy as np
+
+    x = np.ascontiguousarray(x, dtype=np.complex64)
+    mag = np.empty(x.shape, dtype=np.float32)
+    b = Bench(warmup=warmup, runs=runs)
+    _check(load().rfx_magnitude_host(x.ctypes.data, x.size, mag.ctypes.data, ctypes.byref(b)))
+    return mag, b
 
 
 def fir_stream(x, taps, impl="plain", chunk: int = 1 << 20, depth: int = 3,

@@ -175,6 +175,23 @@ int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps,
 int rfx_channelize_branches(const void* x, const float* taps, void* u, int64_t num_samples,
                             int channels, int num_taps, cudaStream_t stream);
 
+/* The channelizer followed by the magnitude of every channel output, mag[t][k] = |z[t][k]|
+ * (frames x channels float32). Tensor-core plans compute it in the DFT-GEMM epilogue, so the
+ * complex channel outputs never reach HBM; plain plans run the magnitude kernel over the
+ * channel outputs in a plan-owned buffer (allocated by the first such call). mag 16-byte
+ * aligned. Fuses channelize |> magnitude (compiler/examples/channelizer.sf,
+ * src/magnitude.cu:17-25); no single-call counterpart in the project. */
+int rfx_channelize_magnitude_launch(rfx_chan_plan* plan, const void* x, const float* taps,
+                                    float* mag, int64_t num_samples, int num_taps,
+                                    cudaStream_t stream);
+
+/* ---- magnitude ------------------------------------------------------------------------- */
+
+/* mag[i] = |x[i]| = sqrt(re^2 + im^2) for i < num_samples (x cf32, mag float32, both 16-byte
+ * aligned), enqueued on `stream`. Replaces magnitude_device (src/device_ops.hpp:57,
+ * src/magnitude.cu:27-37). */
+int rfx_magnitude_launch(const void* x, float* mag, int64_t num_samples, cudaStream_t stream);
+
 /* The 64-channel tensor-core channelizer (what rfx_channelize_launch computes with an
  * RFX_CHAN_TC plan, same kernel and results) without a plan and without allocating anything:
  * its twiddle operand (66,048 bytes) lives in a fixed array of the library's device memory,
@@ -247,6 +264,14 @@ int rfx_fir_host_format(int impl, int format, const void* x, int64_t num_samples
  * Replaces channelize_cuda (src/ops.hpp:40-41). */
 int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
                         int num_taps, int channels, void* z_iq, rfx_bench* bench);
+
+/* rfx_channelize_magnitude_launch on host buffers: `mag` receives frames * channels float32. */
+int rfx_channelize_magnitude_host(int impl, const void* x_iq, int64_t num_samples,
+                                  const float* taps, int num_taps, int channels, float* mag,
+                                  rfx_bench* bench);
+
+/* The magnitude on host buffers. Replaces magnitude_cuda (src/ops.hpp:27-29). */
+int rfx_magnitude_host(const void* x_iq, int64_t num_samples, float* mag, rfx_bench* bench);
 
 /* ---- tuning --------------------------------------------------------------------------- */
 

@@ -14,6 +14,7 @@ Restated from the gpu-rf-pipeline project (file:line inside that project):
 * ``fir_f32_seq``  src/fir.cu:30-40 — the reference GPU kernels' float32 arithmetic (one fused
                    multiply-add per tap, taps in ascending order), for bit-exact comparisons.
 * ``channelize_branch_f32_seq``  src/channelize.cu:25-49 — the reference's float32 branch sums.
+* ``magnitude``    tools/reference.py:98-100 — |z| of each value, float64.
 * ``decode``       src/io.cpp:110-148 — SigMF integer samples to cf32: each ci16_le component
                    v * (1 / 32768), each ci8 component v * (1 / 128), in float32.
 
@@ -87,6 +88,11 @@ def _taps32(taps: np.ndarray) -> np.ndarray:
 
 
 # --- NumPy restatements -------------------------------------------------------------------
+
+def magnitude(z: np.ndarray) -> np.ndarray:
+    """|z| of each value, float64, same shape."""
+    return np.abs(np.asarray(z, dtype=np.complex128))
+
 
 SAMPLE_FORMATS = {"cf32": 0, "ci16": 1, "ci8": 2}  # rfx_sample_format
 

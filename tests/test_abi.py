@@ -127,3 +127,15 @@ def test_fir_format_argument_errors(lib) -> None:
     assert lib.rfx_fir_launch_format(5, 1, p, p, p, 10, 3, None) == 1
     assert lib.rfx_fir_launch_format(0, 1, None, None, None, 0, 3, None) == 0
     assert lib.rfx_fir_host_format(0, 9, None, 0, None, 1, 256, None, None) == 1
+
+
+def test_magnitude_argument_errors(lib) -> None:
+    buf = ctypes.create_string_buffer(64)
+    p = (ctypes.addressof(buf) + 15) & ~15
+    assert lib.rfx_magnitude_launch(None, None, 0, None) == 0
+    assert lib.rfx_magnitude_launch(None, p, 4, None) == 1
+    assert lib.rfx_magnitude_launch(p + 8, p, 4, None) == 3
+    assert lib.rfx_magnitude_launch(p, p, -1, None) == 1
+    assert lib.rfx_channelize_magnitude_launch(None, p, p, p, 10, 5, None) == 1
+    assert lib.rfx_magnitude_host(None, 3, None, None) == 1
+    assert lib.rfx_channelize_magnitude_host(0, None, 10, None, 5, 0, None, None) == 1

@@ -396,3 +396,58 @@ def test_sigmf_sample_rate_comes_from_the_recording(fixtures: Path, tmp_path: Pa
     proc = rfgpu("stream", "--in", fixtures / "tone_ci16.sigmf-data", "--taps",
                  fixtures / "lowpass.f32", "--out", tmp_path / "y.cf32", "--bench", 3)
     assert json.loads(proc.stdout)["sample_rate"] == signals.SAMPLE_RATE
+
+
+# --- magnitude (tests/test_pipeline.py:88-110) and channelize --output magnitude -------------
+
+def test_bad_channelize_output_is_a_usage_error(fixtures: Path, tmp_path: Path) -> None:
+    proc = rfgpu("channelize", "--in", fixtures / "tone.cf32", "--taps",
+                 fixtures / "channelizer_proto.f32", "--channels", 16, "--out",
+                 tmp_path / "z.f32", "--output", "power", check=False)
+    assert proc.returncode == 2
+    assert "--output" in proc.stderr
+
+
+def test_magnitude_usage_errors(tmp_path: Path) -> None:
+    proc = rfgpu("magnitude", "--in", tmp_path / "x.cf32", check=False)
+    assert proc.returncode == 2
+    proc = rfgpu("magnitude", "--in", tmp_path / "x.cf32", "--out", tmp_path / "m.f32",
+                 "--taps", tmp_path / "h.f32", check=False)
+    assert proc.returncode == 2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tone.cf32", "tone_odd.cf32", "short.cf32",
+                                  "tone_ci16.sigmf-meta"])
+def test_magnitude_matches_reference(fixtures: Path, tmp_path: Path, name: str) -> None:
+    out = tmp_path / "magnitude.f32"
+    rfgpu("magnitude", "--in", fixtures / name, "--out", out)
+    stem = name.split(".")[0]
+    expected = orc.magnitude(signals.fixture_signal(stem))
+    actual = np.fromfile(out, dtype="<f4")
+    assert actual.shape == expected.shape
+    np.testing.assert_allclose(actual, expected, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_magnitude_of_zeros_is_exactly_zero(fixtures: Path, tmp_path: Path) -> None:
+    out = tmp_path / "magnitude.f32"
+    rfgpu("magnitude", "--in", fixtures / "zeros.cf32", "--out", out)
+    actual = np.fromfile(out, dtype="<f4")
+    assert actual.shape == (4096,) and not np.any(actual)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl,channels,taps", [("plain", 16, "channelizer_proto"),
+                                                ("auto", 64, "lowpass_long"),
+                                                ("tc_split", 64, "lowpass_long")])
+def test_channelize_magnitude_output_is_the_magnitude_of_channelize(
+        fixtures: Path, tmp_path: Path, impl: str, channels: int, taps: str) -> None:
+    args = ["--in", fixtures / "tone.cf32", "--taps", fixtures / f"{taps}.f32",
+            "--channels", channels, "--impl", impl]
+    rfgpu("channelize", *args, "--out", tmp_path / "z.cf32")
+    rfgpu("magnitude", "--in", tmp_path / "z.cf32", "--out", tmp_path / "mz.f32")
+    proc = rfgpu("channelize", *args, "--out", tmp_path / "m.f32", "--output", "magnitude",
+                 "--bench", 3)
+    assert json.loads(proc.stdout)["num_out"] == 65536
+    assert (tmp_path / "m.f32").read_bytes() == (tmp_path / "mz.f32").read_bytes()
