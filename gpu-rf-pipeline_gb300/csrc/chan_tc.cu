@@ -359,10 +359,11 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             for (int i = 0; i < kR; ++i) {
                 const float2 a = unpack2(u0[i]);
                 const float2 b = unpack2(u1[i]);
-                const uint32_t mx = max(max(absbits(a.x), absbits(a.y)),
-                                        max(absbits(b.x), absbits(b.y)));
+                // Non-negative floats order like their bit patterns.
+                const float m = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(b.x), fabsf(b.y)));
                 // Clamped to 127 (only |u| < 2^-113 would want more): the stored exponent.
-                ef[i] = min(scale_exponent(__reduce_max_sync(0xFFFFFFFFu, mx)), 127);
+                ef[i] = min(scale_exponent(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(m))),
+                            127);
             }
             if (lane == 0) {
                 signed char* fe = ctl.fexp[k % kExpBufs];
@@ -382,13 +383,14 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             const uint32_t off_im = static_cast<uint32_t>(kim >> 3) * kPlane + (kim & 7) * 2u;
 #pragma unroll
             for (int i = 0; i < kR; ++i) {
-                const float2 a = unpack2(u0[i]);
-                const float2 b = unpack2(u1[i]);
-                const float fa = exp2i(ef[i] / 2);
-                const float fb = exp2i(ef[i] - ef[i] / 2);
+                // ef <= 127 and >= -113: 2^ef is one normal float; the scaling is exact.
+                const float f = exp2_exact(ef[i]);
+                const f32x2 ff = pack2(f, f);
+                const float2 a = unpack2(mul2(u0[i], ff));
+                const float2 b = unpack2(mul2(u1[i], ff));
                 uint32_t re_hi, re_lo, im_hi, im_lo;
-                split2(a.x * fa * fb, b.x * fa * fb, re_hi, re_lo);
-                split2(a.y * fa * fb, b.y * fa * fb, im_hi, im_lo);
+                split2(a.x, b.x, re_hi, re_lo);
+                split2(a.y, b.y, im_hi, im_lo);
                 const uint32_t row = static_cast<uint32_t>(frow0 + i) * 16u;
                 sts32(sbase + lay.a_hi + off_re + row, re_hi);
                 sts32(sbase + lay.a_lo + off_re + row, re_lo);
@@ -459,19 +461,23 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
 #pragma unroll
                 for (int s = 0; s < 2; ++s) {
                     const long long t = t_base + 16 * r + 8 * s;
-                    const int shift = -(fe[quarter * 32 + (lane >> 2) + 16 * r + 8 * s] + kWExp);
-                    const float fa = exp2i(shift / 2);
-                    const float fb = exp2i(shift - shift / 2);
+                    // shift in [-141, 99]: 2^shift is one float (subnormal below -126), and the
+                    // scaling is exact unless the result itself is subnormal.
+                    const float f =
+                        exp2_exact(-(fe[quarter * 32 + (lane >> 2) + 16 * r + 8 * s] + kWExp));
+                    const f32x2 ff = pack2(f, f);
                     if (t < frames) {
 #pragma unroll
                         for (int jj = 0; jj < 2; ++jj) {
                             const float* a = &v[r][4 * (2 * jj) + 2 * s];
                             const float* b = &v[r][4 * (2 * jj + 1) + 2 * s];
                             const long long o = t * kM + 16 * slice + 8 * jj + 2 * (lane & 3);
-                            const float re0 = a[0] * fa * fb;
-                            const float im0 = a[1] * fa * fb;
-                            const float re1 = b[0] * fa * fb;
-                            const float im1 = b[1] * fa * fb;
+                            const float2 za = unpack2(mul2(pack2(a[0], a[1]), ff));
+                            const float2 zb = unpack2(mul2(pack2(b[0], b[1]), ff));
+                            const float re0 = za.x;
+                            const float im0 = za.y;
+                            const float re1 = zb.x;
+                            const float im1 = zb.y;
                             if constexpr (kMag) {
                                 // Channels c, c + 1 of the frame: 8 bytes, four lanes 32.
                                 *reinterpret_cast<float2*>(static_cast<float*>(out) + o) =

@@ -128,6 +128,12 @@ __device__ __forceinline__ float exp2i(int e)
     return __int_as_float((e + 127) << 23);
 }
 
+// 2^e as a float for e in [-149, 127] (subnormal below -126), exact.
+__device__ __forceinline__ float exp2_exact(int e)
+{
+    return e >= -126 ? __int_as_float((e + 127) << 23) : __int_as_float(1 << (e + 149));
+}
+
 // Exponent that brings a magnitude with these float bits into [2^14, 2^15): 141 - biased
 // exponent; 0 for zero.
 __device__ __forceinline__ int scale_exponent(uint32_t abs_bits)
