@@ -264,7 +264,9 @@ __device__ __forceinline__ float2 ldg_one(const void* x, int fmt, long long s)
 // samples of a tile window). smap: the same rows, boxes of 256 components x `srows` (a scan
 // slice). fmt: x's sample format (0 cf32, 1 ci16, 2 ci8); the copies move the components as
 // stored and the producers decode them.
-template <int S>
+// kInt: x holds integer components (fmt 1 or 2, a runtime argument); without it x is cf32
+// and the format branches compile away (they cost the cf32 kernel 7 %).
+template <int S, bool kInt>
 __global__ void __launch_bounds__(kThreads, 1)
 fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap smap,
               const void* __restrict__ x, const float* __restrict__ taps,
@@ -272,6 +274,9 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
+    if (!kInt) {
+        fmt = 0;
+    }
     const int es = component_bytes(fmt);
     const Layout lay = tc_layout(num_taps, S, sbufs, es);
     const int C = lay.C;
@@ -793,7 +798,7 @@ bool fir_tc_supported(int num_taps)
     return num_taps > 1 && l.bytes <= 227u * 1024u && l.rows <= 256;
 }
 
-template <int S>
+template <int S, bool kInt>
 static cudaError_t launch_stages(int fmt, const void* x, const float* taps, void* y, long long n,
                                  int num_taps, int sbufs, cudaStream_t stream)
 {
@@ -819,13 +824,13 @@ static cudaError_t launch_stages(int fmt, const void* x, const float* taps, void
     }
     // The block's warps must fit the register file at this register count.
     cudaFuncAttributes attr{};
-    if ((err = cudaFuncGetAttributes(&attr, fir_tc_kernel<S>)) != cudaSuccess) {
+    if ((err = cudaFuncGetAttributes(&attr, fir_tc_kernel<S, kInt>)) != cudaSuccess) {
         return err;
     }
     if (attr.maxThreadsPerBlock < kThreads) {
         return cudaErrorLaunchOutOfResources;
     }
-    err = cudaFuncSetAttribute(fir_tc_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    err = cudaFuncSetAttribute(fir_tc_kernel<S, kInt>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(bytes));
     if (err != cudaSuccess) {
         return err;
@@ -844,7 +849,7 @@ static cudaError_t launch_stages(int fmt, const void* x, const float* taps, void
     const long long blocks = (n + kB - 1) / kB;
     const int tiles = static_cast<int>((blocks + kNB - 1) / kNB);
     const int grid = tiles < sms ? tiles : sms;
-    fir_tc_kernel<S><<<grid, kThreads, bytes, stream>>>(
+    fir_tc_kernel<S, kInt><<<grid, kThreads, bytes, stream>>>(
         map, smap, x, taps, static_cast<float2*>(y), n, num_taps, tiles, sbufs, fmt);
     return cudaGetLastError();
 }
@@ -857,13 +862,16 @@ static cudaError_t launch_single(int fmt, const void* x, const float* taps, void
     // The deep scan ring first (it hides the scan copies' latency), then the most stages.
     for (int sbufs = kScanBufsMax; sbufs >= 2; sbufs -= 2) {
         if (max_stages >= 6 && tc_layout(num_taps, 6, sbufs, es).bytes <= 227u * 1024u) {
-            return launch_stages<6>(fmt, x, taps, y, n, num_taps, sbufs, stream);
+            return fmt == 0 ? launch_stages<6, false>(fmt, x, taps, y, n, num_taps, sbufs, stream)
+                            : launch_stages<6, true>(fmt, x, taps, y, n, num_taps, sbufs, stream);
         }
         if (max_stages >= 4 && tc_layout(num_taps, 4, sbufs, es).bytes <= 227u * 1024u) {
-            return launch_stages<4>(fmt, x, taps, y, n, num_taps, sbufs, stream);
+            return fmt == 0 ? launch_stages<4, false>(fmt, x, taps, y, n, num_taps, sbufs, stream)
+                            : launch_stages<4, true>(fmt, x, taps, y, n, num_taps, sbufs, stream);
         }
         if (tc_layout(num_taps, 2, sbufs, es).bytes <= 227u * 1024u) {
-            return launch_stages<2>(fmt, x, taps, y, n, num_taps, sbufs, stream);
+            return fmt == 0 ? launch_stages<2, false>(fmt, x, taps, y, n, num_taps, sbufs, stream)
+                            : launch_stages<2, true>(fmt, x, taps, y, n, num_taps, sbufs, stream);
         }
     }
     return cudaErrorInvalidValue;
