@@ -490,7 +490,9 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             for (int w = 0; w < kProducerWarps; ++w) {
                 tmax = max(tmax, ctl.pmax[rb][w]);
             }
-            const int ex = scale_exponent(tmax);
+            // Clamped to 127 (only a window with max |x| < 2^-113 would want more), so that 2^ex
+            // is one float and the producers scale with a single exact multiply.
+            const int ex = min(scale_exponent(tmax), 127);
             if (k & 1) {
                 ex_odd = ex;
             } else {
@@ -547,8 +549,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             const int st = v % kStagesPerTile;
             const long long j0 = static_cast<long long>(tile_of(k)) * kNB;
             const int ex = (k & 1) ? ex_odd : ex_even;
-            const float fa = exp2i(ex / 2);
-            const float fb = exp2i(ex - ex / 2);
+            const float fs = exp2_exact(ex);   // ex in [-113, 127]: exact scaling
+            const f32x2 fs2 = pack2(fs, fs);
             const int slot = v % S;
             const int rslot = v % kRaw;
             if (!mbar_wait_bounded(smem_u32(&ctl.empty[slot]), ((v / S) & 1) ^ 1, fault,
@@ -559,15 +561,19 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
             }
             const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
             const uint32_t raw = sbase + lay.raw0 + static_cast<uint32_t>(rslot) * lay.raw;
-            const int items = lay.rows * 8;  // sample pairs: 8 per window row
             const uint32_t pair_bytes = 4u * static_cast<uint32_t>(es);
             // Window row of the input's last, partial block (outside the tensor maps), if any.
             const long long tail_rel = full_blocks - (j0 - C);
             const int b_tail = tail_rel >= 0 && tail_rel < lay.rows ? static_cast<int>(tail_rel) : -1;
+            // Item f = 8 b + q (sample pair q of window row b): kProducers is a multiple of 8, so
+            // a thread keeps its q and steps b by kProducers / 8.
+            static_assert(kProducers % 8 == 0, "producer stride");
+            const int q = ptid & 7;
+            const uint32_t elem_off = static_cast<uint32_t>(q >> 2) * lay.pitch +
+                                      static_cast<uint32_t>(q & 3) * 4u;
 #pragma unroll 2
-            for (int f = ptid; f < items; f += kProducers) {
-                const int b = f >> 3;
-                const int q = f & 7;
+            for (int b = ptid >> 3; b < lay.rows; b += kProducers / 8) {
+                const int f = 8 * b + q;
                 float4 v4;
                 if (b != b_tail) {
                     // zero outside [0, n)
@@ -584,12 +590,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ 
                         v4.y = w2.y;
                     }
                 }
+                const float2 s0 = unpack2(mul2(pack2(v4.x, v4.y), fs2));
+                const float2 s1 = unpack2(mul2(pack2(v4.z, v4.w), fs2));
                 uint32_t re_hi, re_lo, im_hi, im_lo;
-                split2(v4.x * fa * fb, v4.z * fa * fb, re_hi, re_lo);
-                split2(v4.y * fa * fb, v4.w * fa * fb, im_hi, im_lo);
-                const uint32_t plane = static_cast<uint32_t>(q >> 2) * lay.pitch;
-                const uint32_t elem = static_cast<uint32_t>(q & 3) * 4u;
-                const uint32_t row_re = plane + static_cast<uint32_t>(2 * b) * 16u + elem;
+                split2(s0.x, s1.x, re_hi, re_lo);
+                split2(s0.y, s1.y, im_hi, im_lo);
+                const uint32_t row_re = elem_off + static_cast<uint32_t>(2 * b) * 16u;
                 sts32(stage + row_re, re_hi);
                 sts32(stage + row_re + 16u, im_hi);
                 sts32(stage + lay.split + row_re, re_lo);

@@ -107,7 +107,13 @@ def test_bad_channel_count_is_an_error() -> None:
 @pytest.mark.parametrize("n,k,m", [(100, 37, 4), (64, 16, 16), (7, 63, 4), (33, 1, 1),
                                    (50, 24, 8), (70001, 1024, 64), (1 << 16, 4096, 1024),
                                    (5 * 1024 + 3, 32768, 1024), (12345, 100, 12),
-                                   (3000, 640, 160), (1 << 18, 1024, 64), (999, 2000, 3)])
+                                   (3000, 640, 160), (1 << 18, 1024, 64), (999, 2000, 3),
+                                   # the shared-memory form (64 channels and up): partial branch
+                                   # blocks, partial frame blocks, inputs shorter than the taps,
+                                   # taps not a multiple of the channels, one tap per branch
+                                   (5000, 333, 100), (20011, 6400, 200), (130, 4096, 64),
+                                   (64 * 65 + 1, 64 * 40 + 7, 64), (70000, 128, 128),
+                                   (4097, 65, 65), (1 << 16, 32768, 1024), (200, 64, 64)])
 def test_branch_sums_are_bit_exact(n: int, k: int, m: int) -> None:
     # rfx_channelize_branches against the reference's float32 branch arithmetic, bit for bit.
     rng = np.random.default_rng(7 * n + k + m)
