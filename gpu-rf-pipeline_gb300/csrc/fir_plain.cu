@@ -246,7 +246,7 @@ __device__ __forceinline__ void fir_plain_tile(const void* __restrict__ xv,
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 fir_plain_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
                  float2* __restrict__ y, long long n, int num_taps)
 {
@@ -256,7 +256,7 @@ fir_plain_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
 
 // Several captures sharing one tap set: blockIdx.y picks the capture; blocks past a shorter
 // capture's end return at once (as the project's batched kernels, src/fused.cu:141-162).
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 fir_plain_batched_kernel(PlainBatch batch, const float* __restrict__ taps, int num_taps)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -271,7 +271,7 @@ fir_plain_batched_kernel(PlainBatch batch, const float* __restrict__ taps, int n
 
 // Captures with their own taps: block b takes tile b - tile0[c] of the capture c whose tiles
 // contain it (same arithmetic per capture as fir_plain_kernel, so the same bits).
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 fir_plain_caps_kernel(const __grid_constant__ PlainCaps caps)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -293,7 +293,7 @@ fir_plain_caps_kernel(const __grid_constant__ PlainCaps caps)
 
 // Integer I/Q input (ci16, ci8), decoded in the load stage.
 template <int kFmt>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 fir_plain_fmt_kernel(const void* __restrict__ x, const float* __restrict__ taps,
                      float2* __restrict__ y, long long n, int num_taps)
 {
