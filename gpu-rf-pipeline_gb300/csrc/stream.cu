@@ -19,6 +19,11 @@
 //  * the implementation (auto resolved once for the whole capture) and the tensor-core tile
 //    shape and ring depth are fixed before the first chunk.
 //
+// Input formats: cf32, or integer I/Q as stored (ci16, ci8: rfx_sample_format) — then only the
+// stored bytes cross the host link and the kernels convert them in their load stage, with the
+// bits of streaming the converted samples (integer input runs the single-CTA tensor-core form,
+// whose tile the chunking follows).
+//
 // Memory modes (src/stream.hpp:34-38): copy (host copies into and out of the pinned ring);
 // registered (x and y page-locked in place; memory that is already page-locked is used as is);
 // zero-copy (the chunk is written into mapped pinned memory, a gather kernel reads it across the
@@ -43,7 +48,8 @@
 namespace rfx {
 namespace {
 
-__global__ void copy_samples(const float2* __restrict__ src, float2* __restrict__ dst, long long n)
+template <typename T>
+__global__ void copy_elements(const T* __restrict__ src, T* __restrict__ dst, long long n)
 {
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
     for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
@@ -52,14 +58,24 @@ __global__ void copy_samples(const float2* __restrict__ src, float2* __restrict_
     }
 }
 
-cudaError_t launch_copy(const void* src, void* dst, long long n, cudaStream_t stream)
+// Copies n samples of `sample_bytes` bytes (8, 4 or 2) with one element per sample.
+cudaError_t launch_copy(const void* src, void* dst, long long n, int sample_bytes,
+                        cudaStream_t stream)
 {
     if (n <= 0) {
         return cudaSuccess;
     }
-    const long long blocks = std::min<long long>((n + 255) / 256, 4096);
-    copy_samples<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(
-        static_cast<const float2*>(src), static_cast<float2*>(dst), n);
+    const unsigned blocks = static_cast<unsigned>(std::min<long long>((n + 255) / 256, 4096));
+    if (sample_bytes == 8) {
+        copy_elements<<<blocks, 256, 0, stream>>>(static_cast<const float2*>(src),
+                                                  static_cast<float2*>(dst), n);
+    } else if (sample_bytes == 4) {
+        copy_elements<<<blocks, 256, 0, stream>>>(static_cast<const unsigned int*>(src),
+                                                  static_cast<unsigned int*>(dst), n);
+    } else {
+        copy_elements<<<blocks, 256, 0, stream>>>(static_cast<const unsigned short*>(src),
+                                                  static_cast<unsigned short*>(dst), n);
+    }
     return cudaGetLastError();
 }
 
@@ -140,8 +156,23 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
                               int num_taps, const rfx_stream_config* config, void* y_iq,
                               double* total_ms, int* chunks_out)
 {
+    return rfx_fir_stream_format(RFX_FORMAT_CF32, x_iq, num_samples, taps, num_taps, config,
+                                 y_iq, total_ms, chunks_out);
+}
+
+extern "C" int rfx_fir_stream_format(int format, const void* x_in, int64_t num_samples,
+                                     const float* taps, int num_taps,
+                                     const rfx_stream_config* config, void* y_iq,
+                                     double* total_ms, int* chunks_out)
+{
     using namespace rfx;
     char msg[256];
+    if (format < RFX_FORMAT_CF32 || format > RFX_FORMAT_CI8) {
+        std::snprintf(msg, sizeof(msg), "stream: unknown sample format %d", format);
+        return set_last_error(RFX_ERR_INVALID, msg);
+    }
+    // Bytes per input sample as stored: cf32 8, ci16 4, ci8 2 (outputs are cf32).
+    const int ib = format == RFX_FORMAT_CF32 ? 8 : format == RFX_FORMAT_CI16 ? 4 : 2;
     if (config == nullptr) {
         return set_last_error(RFX_ERR_INVALID, "stream: null config");
     }
@@ -173,7 +204,7 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
     if (num_samples == 0) {
         return RFX_OK;
     }
-    if (x_iq == nullptr || y_iq == nullptr || taps == nullptr) {
+    if (x_in == nullptr || y_iq == nullptr || taps == nullptr) {
         return set_last_error(RFX_ERR_INVALID, "stream: null host pointer");
     }
 
@@ -187,7 +218,8 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
         impl = RFX_FIR_PLAIN;  // as rfx_fir_launch: one tap, or beyond the tensor-core form
     }
     const TcConfig tc = tuned_fir_tc_config(num_taps, n);
-    const long long tile = impl == RFX_FIR_TC ? fir_tc_tile_outputs(num_taps, n, tc) : 1;
+    const long long tile =
+        impl == RFX_FIR_TC ? fir_tc_tile_outputs_format(format, num_taps, n, tc) : 1;
     const long long history = tile > 1 ? tile : num_taps - 1;
     const long long chunk = config->chunk;
     const long long slot_len = chunk + 2 * (tile - 1) + history;
@@ -200,15 +232,16 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
     cudaError_t err;
     res.slots.resize(static_cast<size_t>(config->depth));
     const size_t slot_bytes = static_cast<size_t>(slot_len) * 8;
+    const size_t slot_in_bytes = static_cast<size_t>(slot_len) * ib;
     for (Slot& s : res.slots) {
         if (!registered) {
             const unsigned flags = zero_copy ? cudaHostAllocMapped : cudaHostAllocDefault;
-            if ((err = cudaHostAlloc(&s.host_in, slot_bytes, flags)) != cudaSuccess ||
+            if ((err = cudaHostAlloc(&s.host_in, slot_in_bytes, flags)) != cudaSuccess ||
                 (err = cudaHostAlloc(&s.host_out, slot_bytes, flags)) != cudaSuccess) {
                 return cuda_error(err, "stream: cudaHostAlloc");
             }
         }
-        if ((err = cudaMalloc(&s.dev_in, slot_bytes)) != cudaSuccess ||
+        if ((err = cudaMalloc(&s.dev_in, slot_in_bytes)) != cudaSuccess ||
             (err = cudaMalloc(&s.dev_out, slot_bytes)) != cudaSuccess ||
             (err = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)) != cudaSuccess ||
             (err = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming)) != cudaSuccess) {
@@ -217,7 +250,8 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
     }
     const size_t bytes = static_cast<size_t>(n) * 8;
     if (registered) {
-        if ((err = lock_in_place(x_iq, bytes, &res.registered[0])) != cudaSuccess ||
+        if ((err = lock_in_place(x_in, static_cast<size_t>(n) * ib, &res.registered[0])) !=
+                cudaSuccess ||
             (err = lock_in_place(y_iq, bytes, &res.registered[1])) != cudaSuccess) {
             return cuda_error(err, "stream: cudaHostRegister");
         }
@@ -229,7 +263,7 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
         return cuda_error(err, "stream: tap upload");
     }
 
-    const auto* x = static_cast<const float2*>(x_iq);
+    const auto* x = static_cast<const unsigned char*>(x_in);   // samples of ib bytes
     auto* y = static_cast<float2*>(y_iq);
     // Waits for the chunk in `s`, then moves its outputs into y (copy and zero-copy modes).
     auto retire = [&](Slot& s) -> cudaError_t {
@@ -265,29 +299,31 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
         s.count = end - start;
         s.offset = start - in_start;
         const cudaStream_t st = s.stream;
+        const unsigned char* src_in = x + static_cast<size_t>(in_start) * ib;
+        const size_t in_bytes = static_cast<size_t>(in_len) * ib;
         if (registered) {
-            err = cudaMemcpyAsync(s.dev_in, x + in_start, static_cast<size_t>(in_len) * 8,
-                                  cudaMemcpyHostToDevice, st);
+            err = cudaMemcpyAsync(s.dev_in, src_in, in_bytes, cudaMemcpyHostToDevice, st);
         } else {
             // Where a receiver would write the samples.
-            std::memcpy(s.host_in, x + in_start, static_cast<size_t>(in_len) * 8);
+            std::memcpy(s.host_in, src_in, in_bytes);
             if (zero_copy) {
                 void* mapped = nullptr;
                 err = cudaHostGetDevicePointer(&mapped, s.host_in, 0);
                 if (err == cudaSuccess) {
-                    err = launch_copy(mapped, s.dev_in, in_len, st);
+                    err = launch_copy(mapped, s.dev_in, in_len, ib, st);
                 }
             } else {
-                err = cudaMemcpyAsync(s.dev_in, s.host_in, static_cast<size_t>(in_len) * 8,
-                                      cudaMemcpyHostToDevice, st);
+                err = cudaMemcpyAsync(s.dev_in, s.host_in, in_bytes, cudaMemcpyHostToDevice, st);
             }
         }
         if (err != cudaSuccess) {
             return cuda_error(err, "stream: upload");
         }
         err = impl == RFX_FIR_TC
-                  ? fir_tc_launch(s.dev_in, res.taps, s.dev_out, in_len, num_taps, tc, st)
-                  : fir_plain_launch(s.dev_in, res.taps, s.dev_out, in_len, num_taps, st);
+                  ? fir_tc_launch_format(format, s.dev_in, res.taps, s.dev_out, in_len, num_taps,
+                                         tc, st)
+                  : fir_plain_launch_format(format, s.dev_in, res.taps, s.dev_out, in_len,
+                                            num_taps, st);
         if (err != cudaSuccess) {
             return cuda_error(err, "stream: FIR launch");
         }
@@ -300,7 +336,7 @@ extern "C" int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float
             void* mapped = nullptr;
             err = cudaHostGetDevicePointer(&mapped, s.host_out, 0);
             if (err == cudaSuccess) {
-                err = launch_copy(src, static_cast<float2*>(mapped) + s.offset, s.count, st);
+                err = launch_copy(src, static_cast<float2*>(mapped) + s.offset, s.count, 8, st);
             }
         } else {
             err = cudaMemcpyAsync(static_cast<float2*>(s.host_out) + s.offset, src, out_bytes,

@@ -322,12 +322,14 @@ int run_stream(int argc, char** argv)
     config.chunk = args.integer("--chunk", config.chunk, 1);
     config.depth = args.integer("--depth", config.depth, 1);
     const BenchConfig bench = bench_config(args);
-    const std::vector<cf32> x = read_cf32(args.required("--in"));
+    // Integer recordings stream as stored (half or a quarter of the bytes over the host link)
+    // and are converted on the GPU, with the bits of streaming the converted samples.
+    const StoredSamples x = read_stored(args.required("--in"));
     const std::vector<float> taps = read_f32(args.required("--taps"));
     if (taps.empty()) {
         throw std::runtime_error(args.required("--taps") + ": no taps");
     }
-    require_int_range(x.size(), "stream input");
+    require_int_range(x.count, "stream input");
     require_int_range(static_cast<std::size_t>(config.chunk) + taps.size(), "chunk with history");
     double rate = sample_rate(args.required("--in"));
     if (args.has("--rate")) {
@@ -346,7 +348,7 @@ int run_stream(int argc, char** argv)
     write_cf32(args.required("--out"), y);
     if (!args.has("--bench")) {
         std::printf("stream[%s]: %zu samples in %d chunks of %d, depth %d -> %s\n", impl.c_str(),
-                    x.size(), timing.chunks, config.chunk, config.depth,
+                    x.count, timing.chunks, config.chunk, config.depth,
                     args.required("--out").c_str());
         return 0;
     }
@@ -360,12 +362,12 @@ int run_stream(int argc, char** argv)
     }
     const double std_ms =
         times.size() > 1 ? std::sqrt(var / static_cast<double>(times.size() - 1)) : 0.0;
-    const double msps = mean > 0 ? static_cast<double>(x.size()) / (mean * 1e3) : 0.0;
+    const double msps = mean > 0 ? static_cast<double>(x.count) / (mean * 1e3) : 0.0;
     std::printf("{\"op\": \"stream\", \"impl\": \"%s\", \"memory\": \"%s\", \"gpu\": \"%s\", "
                 "\"num_in\": %zu, \"chunk\": %d, \"depth\": %d, \"chunks\": %d, \"runs\": %d, "
                 "\"warmup\": %d, \"total_ms\": {\"mean\": %.6f, \"std\": %.6f}, \"msps\": %.3f, "
                 "\"sample_rate\": %.1f, \"realtime_factor\": %.3f}\n",
-                impl.c_str(), memory.c_str(), gpu_name().c_str(), x.size(), config.chunk,
+                impl.c_str(), memory.c_str(), gpu_name().c_str(), x.count, config.chunk,
                 config.depth, timing.chunks, bench.runs, bench.warmup, mean, std_ms, msps, rate,
                 rate > 0 ? msps * 1e6 / rate : 0.0);
     return 0;

@@ -19,13 +19,16 @@ bool parse_stream_memory(const std::string& name, StreamMemory& memory)
     return true;
 }
 
-std::vector<cf32> fir_stream(const std::vector<cf32>& x, const std::vector<float>& taps,
-                             const StreamConfig& config, StreamTiming& timing)
+namespace {
+
+std::vector<cf32> stream_samples(int format, const void* x, std::size_t count,
+                                 const std::vector<float>& taps, const StreamConfig& config,
+                                 StreamTiming& timing)
 {
     if (config.chunk < 1 || config.depth < 1) {
         throw std::runtime_error("stream: chunk and depth must be at least 1");
     }
-    std::vector<cf32> y(x.size());
+    std::vector<cf32> y(count);
     rfx_stream_config c{};
     c.impl = to_rfx_impl(config.impl);
     c.memory = config.memory == StreamMemory::Copy         ? RFX_STREAM_COPY
@@ -35,9 +38,25 @@ std::vector<cf32> fir_stream(const std::vector<cf32>& x, const std::vector<float
     c.depth = config.depth;
     double total_ms = 0.0;
     int chunks = 0;
-    RFX_CHECK(rfx_fir_stream(x.data(), static_cast<int64_t>(x.size()), taps.data(),
-                             static_cast<int>(taps.size()), &c, y.data(), &total_ms, &chunks));
+    RFX_CHECK(rfx_fir_stream_format(format, x, static_cast<int64_t>(count), taps.data(),
+                                    static_cast<int>(taps.size()), &c, y.data(), &total_ms,
+                                    &chunks));
     timing.total_ms = total_ms;
     timing.chunks = chunks;
     return y;
+}
+
+}  // namespace
+
+std::vector<cf32> fir_stream(const std::vector<cf32>& x, const std::vector<float>& taps,
+                             const StreamConfig& config, StreamTiming& timing)
+{
+    return stream_samples(RFX_FORMAT_CF32, x.data(), x.size(), taps, config, timing);
+}
+
+std::vector<cf32> fir_stream(const StoredSamples& x, const std::vector<float>& taps,
+                             const StreamConfig& config, StreamTiming& timing)
+{
+    return stream_samples(static_cast<int>(x.format), x.bytes.data(), x.count, taps, config,
+                          timing);
 }

@@ -6,6 +6,7 @@
 // bits as filtering the whole capture at once with the same implementation.
 
 #include "device_ops.hpp"
+#include "io.hpp"
 #include "types.hpp"
 
 #include <string>
@@ -34,4 +35,10 @@ struct StreamTiming {
 
 // Output length x.size(). Allocation and the tap upload happen before the clock starts.
 std::vector<cf32> fir_stream(const std::vector<cf32>& x, const std::vector<float>& taps,
+                             const StreamConfig& config, StreamTiming& timing);
+
+// The same over samples as stored (an integer SigMF recording): the stored bytes stream to the
+// device and the kernels convert them (rfx_fir_stream_format); the bits of fir_stream over the
+// converted samples.
+std::vector<cf32> fir_stream(const StoredSamples& x, const std::vector<float>& taps,
                              const StreamConfig& config, StreamTiming& timing);

@@ -74,6 +74,8 @@ SIGNATURES = {
     "rfx_magnitude_launch": (_I, [_VP, _VP, _I64, _VP]),
     "rfx_fir_stream": (_I, [_VP, _I64, _VP, _I, ctypes.POINTER(StreamConfig), _VP,
                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
+    "rfx_fir_stream_format": (_I, [_I, _VP, _I64, _VP, _I, ctypes.POINTER(StreamConfig), _VP,
+                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
     "rfx_fir_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_fir_host_format": (_I, [_I, _I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
     "rfx_channelize_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP, ctypes.POINTER(Bench)]),
@@ -382,26 +384,38 @@ def magnitude_host(x, warmup: int = 0, runs: int = 1):
 
 
 def fir_stream(x, taps, impl="plain", chunk: int = 1 << 20, depth: int = 3,
-               memory: str = "copy", out=None):
-    """The streamed FIR of a host capture (numpy complex64 or a CPU tensor; pinned tensors are
-    used in place in "registered" mode). Returns (y, total_ms, chunks)."""
+               memory: str = "copy", out=None, fmt: str = "cf32"):
+    """The streamed FIR of a host capture (numpy array or CPU tensor; pinned tensors are used
+    in place in "registered" mode). cf32: complex64 samples; ci16 / ci8: the interleaved integer
+    components as stored (int16 / int8), converted on the GPU. Returns (y complex64, total_ms,
+    chunks)."""
     import numpy as np
 
+    comp = _COMPONENT_BYTES[fmt]
     if hasattr(x, "data_ptr"):
-        x_ptr, n = x.data_ptr(), x.numel()
-        y = out if out is not None else x.new_empty(x.shape)
+        x_ptr = x.data_ptr()
+        n = x.numel() * x.element_size() // (2 * comp)
+        if out is not None:
+            y = out
+        else:
+            import torch
+
+            y = torch.empty(n, dtype=torch.complex64, pin_memory=x.is_pinned())
         y_ptr = y.data_ptr()
     else:
-        x = np.ascontiguousarray(x, dtype=np.complex64)
-        x_ptr, n = x.ctypes.data, x.size
-        y = out if out is not None else np.empty_like(x)
+        dtype = {"cf32": np.complex64, "ci16": np.dtype("<i2"), "ci8": np.int8}[fmt]
+        x = np.ascontiguousarray(x, dtype=dtype)
+        x_ptr = x.ctypes.data
+        n = x.nbytes // (2 * comp)
+        y = out if out is not None else np.empty(n, dtype=np.complex64)
         y_ptr = y.ctypes.data if not hasattr(y, "data_ptr") else y.data_ptr()
     taps = np.ascontiguousarray(taps, dtype=np.float32)
     cfg = StreamConfig(_impl(impl), STREAM_MEMORY[memory], chunk, depth)
     ms = ctypes.c_double()
     chunks = ctypes.c_int()
-    _check(load().rfx_fir_stream(x_ptr, n, taps.ctypes.data, taps.size, ctypes.byref(cfg), y_ptr,
-                                 ctypes.byref(ms), ctypes.byref(chunks)))
+    _check(load().rfx_fir_stream_format(_format(fmt), x_ptr, n, taps.ctypes.data, taps.size,
+                                        ctypes.byref(cfg), y_ptr, ctypes.byref(ms),
+                                        ctypes.byref(chunks)))
     return y, ms.value, chunks.value
 
 

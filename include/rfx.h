@@ -236,6 +236,13 @@ typedef struct rfx_stream_config {
 int rfx_fir_stream(const void* x_iq, int64_t num_samples, const float* taps, int num_taps,
                    const rfx_stream_config* config, void* y_iq, double* total_ms, int* chunks);
 
+/* rfx_fir_stream over host samples stored in `format` (rfx_sample_format): each chunk's stored
+ * bytes are uploaded (a half or a quarter of cf32's for ci16 / ci8) and converted by the
+ * kernels, with the bits of streaming the host-converted samples. y_iq is cf32. */
+int rfx_fir_stream_format(int format, const void* x, int64_t num_samples, const float* taps,
+                          int num_taps, const rfx_stream_config* config, void* y_iq,
+                          double* total_ms, int* chunks);
+
 /* ---- host-buffer operations (timed like the project's Bench) --------------------------- */
 
 /* Phase timings of a host-buffer call, as the project's BenchResult (src/bench.hpp:17-32). */

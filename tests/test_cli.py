@@ -379,6 +379,20 @@ def test_sigmf_fir_is_the_fir_of_the_converted_samples(fixtures: Path, tmp_path:
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("rec", ["tone_ci16", "tone_ci8"])
+@pytest.mark.parametrize("impl", ["tiled", "tc_split"])
+@pytest.mark.parametrize("memory", ["copy", "zero-copy"])
+def test_sigmf_stream_is_bit_identical_to_fir(fixtures: Path, tmp_path: Path, rec: str, impl: str,
+                                              memory: str) -> None:
+    rfgpu("fir", "--in", fixtures / f"{rec}.sigmf-meta", "--taps", fixtures / "lowpass_long.f32",
+          "--out", tmp_path / "fir.cf32", "--impl", impl)
+    rfgpu("stream", "--in", fixtures / f"{rec}.sigmf-data", "--taps",
+          fixtures / "lowpass_long.f32", "--out", tmp_path / "stream.cf32", "--impl", impl,
+          "--chunk", 3000, "--depth", 3, "--memory", memory)
+    assert (tmp_path / "fir.cf32").read_bytes() == (tmp_path / "stream.cf32").read_bytes()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("impl", ["plain", "auto"])
 def test_sigmf_channelize_and_stream_read_the_recording(fixtures: Path, tmp_path: Path,
                                                         impl: str) -> None:
