@@ -51,8 +51,27 @@ __device__ __forceinline__ void taps_block(f32x2 (&acc)[kR], const f32x2 (&cur)[
     }
 }
 
-template <bool kGuard>
-__device__ __forceinline__ void load_block(f32x2 (&blk)[kR], const float2* __restrict__ x,
+// Sample s of x in format kFmt (0 cf32; 1 ci16, 2 ci8: components converted as the project's
+// SigMF reader converts them, src/io.cpp:110-148, so the sums are those of the converted input).
+template <int kFmt>
+__device__ __forceinline__ f32x2 load_sample(const void* __restrict__ x, long long s)
+{
+    if constexpr (kFmt == 0) {
+        const float2 w = __ldg(static_cast<const float2*>(x) + s);
+        return pack2(w.x, w.y);
+    } else if constexpr (kFmt == 1) {
+        const short2 w = __ldg(static_cast<const short2*>(x) + s);
+        return pack2(static_cast<float>(w.x) * (1.0f / 32768.0f),
+                     static_cast<float>(w.y) * (1.0f / 32768.0f));
+    } else {
+        const char2 w = __ldg(static_cast<const char2*>(x) + s);
+        return pack2(static_cast<float>(w.x) * (1.0f / 128.0f),
+                     static_cast<float>(w.y) * (1.0f / 128.0f));
+    }
+}
+
+template <bool kGuard, int kFmt>
+__device__ __forceinline__ void load_block(f32x2 (&blk)[kR], const void* __restrict__ x,
                                            long long n, int channels, int m, long long d0)
 {
 #pragma unroll
@@ -60,15 +79,14 @@ __device__ __forceinline__ void load_block(f32x2 (&blk)[kR], const float2* __res
         const long long s = (d0 + i) * channels - m;
         f32x2 v = 0ull;
         if (!kGuard || (s >= 0 && s < n)) {
-            const float2 w = __ldg(x + s);
-            v = pack2(w.x, w.y);
+            v = load_sample<kFmt>(x, s);
         }
         blk[i] = v;
     }
 }
 
-template <bool kGuard>
-__device__ __forceinline__ void branch_frames(f32x2 (&acc)[kR], const float2* __restrict__ x,
+template <bool kGuard, int kFmt>
+__device__ __forceinline__ void branch_frames(f32x2 (&acc)[kR], const void* __restrict__ x,
                                               const float* __restrict__ taps, long long n,
                                               int channels, int m, int P, long long t0)
 {
@@ -77,24 +95,24 @@ __device__ __forceinline__ void branch_frames(f32x2 (&acc)[kR], const float2* __
     const int rem = P - groups * kR;
     f32x2 a[kR];
     f32x2 b[kR];
-    load_block<kGuard>(a, x, n, channels, m, t0);
+    load_block<kGuard, kFmt>(a, x, n, channels, m, t0);
     int g = 0;
     for (; g + 2 <= groups; g += 2) {
-        load_block<kGuard>(b, x, n, channels, m, t0 - kR * (g + 1));
+        load_block<kGuard, kFmt>(b, x, n, channels, m, t0 - kR * (g + 1));
         taps_block<kGuard>(acc, a, b, taps, channels, m, kR * g, kR, t0, first_valid_d);
-        load_block<kGuard>(a, x, n, channels, m, t0 - kR * (g + 2));
+        load_block<kGuard, kFmt>(a, x, n, channels, m, t0 - kR * (g + 2));
         taps_block<kGuard>(acc, b, a, taps, channels, m, kR * (g + 1), kR, t0, first_valid_d);
     }
     if (g < groups) {
-        load_block<kGuard>(b, x, n, channels, m, t0 - kR * (g + 1));
+        load_block<kGuard, kFmt>(b, x, n, channels, m, t0 - kR * (g + 1));
         taps_block<kGuard>(acc, a, b, taps, channels, m, kR * g, kR, t0, first_valid_d);
         if (rem > 0) {
-            load_block<kGuard>(a, x, n, channels, m, t0 - kR * (g + 2));
+            load_block<kGuard, kFmt>(a, x, n, channels, m, t0 - kR * (g + 2));
             taps_block<kGuard>(acc, b, a, taps, channels, m, kR * (g + 1), rem, t0,
                                first_valid_d);
         }
     } else if (rem > 0) {
-        load_block<kGuard>(b, x, n, channels, m, t0 - kR * (g + 1));
+        load_block<kGuard, kFmt>(b, x, n, channels, m, t0 - kR * (g + 1));
         taps_block<kGuard>(acc, a, b, taps, channels, m, kR * g, rem, t0, first_valid_d);
     }
 }
@@ -102,8 +120,9 @@ __device__ __forceinline__ void branch_frames(f32x2 (&acc)[kR], const float2* __
 
 // Block: `width` consecutive branches x (256 / width) frame groups of kR frames. Groups with
 // t0 < guard_frames or reaching past the last frame test every load and term.
+template <int kFmt>
 __global__ void __launch_bounds__(kBranchThreads)
-chan_branch_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
+chan_branch_kernel(const void* __restrict__ x, const float* __restrict__ taps,
                    float2* __restrict__ u, long long n, long long frames, int channels,
                    int num_taps, int width, int guard_frames)
 {
@@ -122,9 +141,9 @@ chan_branch_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
         acc[i] = 0ull;
     }
     if (t0 < guard_frames || t0 + kR > frames) {
-        branch_frames<true>(acc, x, taps, n, channels, m, P, t0);
+        branch_frames<true, kFmt>(acc, x, taps, n, channels, m, P, t0);
     } else {
-        branch_frames<false>(acc, x, taps, n, channels, m, P, t0);
+        branch_frames<false, kFmt>(acc, x, taps, n, channels, m, P, t0);
     }
 #pragma unroll
     for (int i = 0; i < kR; ++i) {
@@ -135,7 +154,7 @@ chan_branch_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
 }
 
 cudaError_t chan_branch_launch(const void* x, const float* taps, void* u, long long frames,
-                               int channels, int num_taps, cudaStream_t stream)
+                               int channels, int num_taps, cudaStream_t stream, int format)
 {
     if (frames == 0 || channels < 1) {
         return cudaSuccess;
@@ -159,10 +178,24 @@ cudaError_t chan_branch_launch(const void* x, const float* taps, void* u, long l
     // group loads starts kR * ceil(P / kR) frames back): they take the tested path.
     const int max_p = (num_taps + channels - 1) / channels;
     const int guard_frames = kR * ((max_p + kR - 1) / kR + 1);
-    chan_branch_kernel<<<dim3(static_cast<unsigned>(gx), static_cast<unsigned>(gy)),
-                         kBranchThreads, 0, stream>>>(
-        static_cast<const float2*>(x), taps, static_cast<float2*>(u), n, frames, channels,
-        num_taps, w, guard_frames);
+    const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
+    float2* uo = static_cast<float2*>(u);
+    switch (format) {
+    case 0:
+        chan_branch_kernel<0><<<grid, kBranchThreads, 0, stream>>>(x, taps, uo, n, frames, channels,
+                                                                   num_taps, w, guard_frames);
+        break;
+    case 1:
+        chan_branch_kernel<1><<<grid, kBranchThreads, 0, stream>>>(x, taps, uo, n, frames, channels,
+                                                                   num_taps, w, guard_frames);
+        break;
+    case 2:
+        chan_branch_kernel<2><<<grid, kBranchThreads, 0, stream>>>(x, taps, uo, n, frames, channels,
+                                                                   num_taps, w, guard_frames);
+        break;
+    default:
+        return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -107,12 +107,13 @@ struct Layout {
     uint32_t w_hi, w_lo, a_hi, a_lo, win0, taps, bytes;
 };
 
-__host__ __device__ inline Layout chan_layout(int num_taps)
+// sb: bytes per input sample as stored (8 cf32, 4 ci16, 2 ci8).
+__host__ __device__ inline Layout chan_layout(int num_taps, int sb = 8)
 {
     Layout l;
     l.P = (num_taps + kM - 1) / kM;
     l.wrows = kHalf + l.P;
-    l.win = static_cast<uint32_t>(l.wrows) * kM * 8u;
+    l.win = static_cast<uint32_t>(l.wrows) * kM * static_cast<uint32_t>(sb);
     l.w_hi = 1024;
     l.w_lo = l.w_hi + kSplit;
     l.a_hi = l.w_lo + kSplit;
@@ -167,20 +168,47 @@ __device__ __forceinline__ void branch_group(f32x2 (&acc)[kR], const f32x2 (&cur
     }
 }
 
+// Sample formats of x (rfx_sample_format): 0 cf32; 1 ci16 and 2 ci8, whose components are
+// converted as the project's SigMF reader converts them (src/io.cpp:110-148: v / 32768, v / 128,
+// exact in float32) where the window is read, so the results are those of the converted input.
+__host__ __device__ constexpr int sample_bytes(int fmt) { return fmt == 0 ? 8 : fmt == 1 ? 4 : 2; }
+
+template <int kFmt>
+__device__ __forceinline__ f32x2 lds_sample(uint32_t addr)
+{
+    if constexpr (kFmt == 0) {
+        return lds64(addr);
+    } else if constexpr (kFmt == 1) {
+        uint32_t w;
+        asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(addr));
+        return pack2(static_cast<float>(static_cast<int>(w << 16) >> 16) * (1.0f / 32768.0f),
+                     static_cast<float>(static_cast<int>(w) >> 16) * (1.0f / 32768.0f));
+    } else {
+        unsigned short w;
+        asm volatile("ld.shared.u16 %0, [%1];" : "=h"(w) : "r"(addr));
+        const int v = w;
+        return pack2(static_cast<float>(static_cast<int>(static_cast<uint32_t>(v) << 24) >> 24) *
+                         (1.0f / 128.0f),
+                     static_cast<float>(static_cast<int>(static_cast<uint32_t>(v) << 16) >> 24) *
+                         (1.0f / 128.0f));
+    }
+}
+
 }  // namespace
 
 // kMag: the output is |z| (float per channel, frames x 64) instead of z (cf32), computed from
 // the same floats z would hold.
-template <bool kTapsSmem, bool kMag>
+template <bool kTapsSmem, bool kMag, int kFmt>
 __global__ void __launch_bounds__(kThreads, 1)
-chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restrict__ x,
+chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const void* __restrict__ x,
                const float* __restrict__ taps, const uint16_t* __restrict__ w_img,
                void* __restrict__ out, long long n, long long frames, int num_taps,
                int num_tiles)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
-    const Layout lay = chan_layout(num_taps);
+    constexpr int kSb = sample_bytes(kFmt);
+    const Layout lay = chan_layout(num_taps, kSb);
     const int P = lay.P;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -273,10 +301,10 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
         // (The block of the last tap group may start up to 8 rows before the window; those
         // samples are never used and lie in the operand area before it.)
         auto load_block = [&](f32x2 (&blk)[kR], uint32_t base, int d0) {
-            const uint32_t a = base + static_cast<uint32_t>(d0 * kM * 8);
+            const uint32_t a = base + static_cast<uint32_t>(d0 * kM * kSb);
 #pragma unroll
             for (int i = 0; i < kR; ++i) {
-                blk[i] = lds64(a + static_cast<uint32_t>(i * kM * 8));
+                blk[i] = lds_sample<kFmt>(a + static_cast<uint32_t>(i * kM * kSb));
             }
         };
         // u[t + i][m] for the thread's 8 frames of one branch m from the warp's half-window.
@@ -288,7 +316,7 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
             // Frame t = first row + P + 8 fgroup; d = 0 is row 8 fgroup + P - (m > 0).
             const uint32_t base =
                 buf + static_cast<uint32_t>(((kR * fgroup + P - (m > 0 ? 1 : 0)) * kM +
-                                             ((kM - m) & (kM - 1))) * 8);
+                                             ((kM - m) & (kM - 1))) * kSb);
             const int groups = P / kR;
             const int rem = P - groups * kR;
             f32x2 a[kR];
@@ -323,8 +351,19 @@ chan_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float2* __restric
                 return;   // uniform across the half's warps
             }
             if (htid < tail) {
-                const float2 v = __ldg(x + full_rows * kM + htid);
-                sts64(buf + static_cast<uint32_t>(rel * kM + htid) * 8u, pack2(v.x, v.y));
+                // The stored sample, as the copy would have placed it.
+                const uint32_t dst = buf + static_cast<uint32_t>(rel * kM + htid) * kSb;
+                const long long s = full_rows * kM + htid;
+                if constexpr (kFmt == 0) {
+                    const float2 v = __ldg(static_cast<const float2*>(x) + s);
+                    sts64(dst, pack2(v.x, v.y));
+                } else if constexpr (kFmt == 1) {
+                    const uint32_t v = __ldg(static_cast<const unsigned int*>(x) + s);
+                    sts32(dst, v);
+                } else {
+                    const unsigned short v = __ldg(static_cast<const unsigned short*>(x) + s);
+                    asm volatile("st.shared.u16 [%0], %1;" ::"r"(dst), "h"(v) : "memory");
+                }
             }
             fence_proxy_async_smem();
             asm volatile("bar.sync %0, %1;" ::"r"(1 + hw), "n"(kHalfWarps * 32) : "memory");
@@ -603,11 +642,11 @@ cudaError_t chan_tc_build_twiddles(void* img, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-template <bool kTapsSmem, bool kMag>
+template <bool kTapsSmem, bool kMag, int kFmt>
 static cudaError_t launch_chan(const void* x, const float* taps, const void* twiddles, void* z,
                                long long n, long long frames, int num_taps, cudaStream_t stream)
 {
-    const Layout lay = chan_layout(num_taps);
+    const Layout lay = chan_layout(num_taps, sample_bytes(kFmt));
     int device = 0;
     int sms = 0;
     cudaError_t err = cudaGetDevice(&device);
@@ -618,35 +657,55 @@ static cudaError_t launch_chan(const void* x, const float* taps, const void* twi
     }
     const uint32_t bytes = lay.bytes > 120u * 1024u ? lay.bytes : 120u * 1024u;
     cudaFuncAttributes attr{};
-    if ((err = cudaFuncGetAttributes(&attr, chan_tc_kernel<kTapsSmem, kMag>)) != cudaSuccess) {
+    if ((err = cudaFuncGetAttributes(&attr, chan_tc_kernel<kTapsSmem, kMag, kFmt>)) != cudaSuccess) {
         return err;
     }
     if (attr.maxThreadsPerBlock < kThreads) {
         return cudaErrorLaunchOutOfResources;
     }
-    err = cudaFuncSetAttribute(chan_tc_kernel<kTapsSmem, kMag>,
+    err = cudaFuncSetAttribute(chan_tc_kernel<kTapsSmem, kMag, kFmt>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(bytes));
     if (err != cudaSuccess) {
         return err;
     }
-    // x viewed as rows of 128 floats (one frame of 64 samples), full frames only; boxes of one
-    // half-window.
+    // x viewed as rows of 128 components (one frame of 64 samples), full frames only; boxes of
+    // one half-window. The copy moves the components as stored.
     CUtensorMap map;
-    err = encode_rows_f32(&map, x, n / kM, 2 * kM, 2 * kM, static_cast<uint32_t>(lay.wrows));
+    err = encode_rows(&map, x, sample_bytes(kFmt) / 2, n / kM, 2 * kM, 2 * kM,
+                      static_cast<uint32_t>(lay.wrows));
     if (err != cudaSuccess) {
         return err;
     }
     const int tiles = static_cast<int>((frames + kFrames - 1) / kFrames);
     const int grid = tiles < sms ? tiles : sms;
-    chan_tc_kernel<kTapsSmem, kMag><<<grid, kThreads, bytes, stream>>>(
-        map, static_cast<const float2*>(x), taps, static_cast<const uint16_t*>(twiddles),
+    chan_tc_kernel<kTapsSmem, kMag, kFmt><<<grid, kThreads, bytes, stream>>>(
+        map, x, taps, static_cast<const uint16_t*>(twiddles),
         z, n, frames, num_taps, tiles);
     return cudaGetLastError();
 }
 
+template <int kFmt>
+static cudaError_t launch_format(const void* x, const float* taps, const void* twiddles, void* z,
+                                 long long n, long long frames, int num_taps, bool magnitude,
+                                 cudaStream_t stream)
+{
+    const bool smem_taps = chan_layout(num_taps).P <= kSmemTapsMax;
+    if (magnitude) {
+        return smem_taps ? launch_chan<true, true, kFmt>(x, taps, twiddles, z, n, frames,
+                                                         num_taps, stream)
+                         : launch_chan<false, true, kFmt>(x, taps, twiddles, z, n, frames,
+                                                          num_taps, stream);
+    }
+    return smem_taps
+               ? launch_chan<true, false, kFmt>(x, taps, twiddles, z, n, frames, num_taps, stream)
+               : launch_chan<false, false, kFmt>(x, taps, twiddles, z, n, frames, num_taps,
+                                                 stream);
+}
+
 cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddles, void* z,
-                           long long n, int num_taps, cudaStream_t stream, bool magnitude)
+                           long long n, int num_taps, cudaStream_t stream, bool magnitude,
+                           int format)
 {
     const long long frames = (n + kM - 1) / kM;
     if (frames == 0) {
@@ -655,15 +714,16 @@ cudaError_t chan_tc_launch(const void* x, const float* taps, const void* twiddle
     if (n < kM) {
         return cudaErrorInvalidValue;  // the caller routes inputs shorter than a frame elsewhere
     }
-    const bool smem_taps = chan_layout(num_taps).P <= kSmemTapsMax;
-    if (magnitude) {
-        return smem_taps
-                   ? launch_chan<true, true>(x, taps, twiddles, z, n, frames, num_taps, stream)
-                   : launch_chan<false, true>(x, taps, twiddles, z, n, frames, num_taps, stream);
+    switch (format) {
+    case 0:
+        return launch_format<0>(x, taps, twiddles, z, n, frames, num_taps, magnitude, stream);
+    case 1:
+        return launch_format<1>(x, taps, twiddles, z, n, frames, num_taps, magnitude, stream);
+    case 2:
+        return launch_format<2>(x, taps, twiddles, z, n, frames, num_taps, magnitude, stream);
+    default:
+        return cudaErrorInvalidValue;
     }
-    return smem_taps
-               ? launch_chan<true, false>(x, taps, twiddles, z, n, frames, num_taps, stream)
-               : launch_chan<false, false>(x, taps, twiddles, z, n, frames, num_taps, stream);
 }
 
 cudaError_t chan_tc_take_fault(unsigned int* code)

@@ -163,7 +163,8 @@ int set_last_error(int status, const char* message) { return fail(status, "%s", 
 struct rfx_chan_plan;
 namespace {
 int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
-                    int64_t num_samples, int num_taps, cudaStream_t stream, bool magnitude);
+                    int64_t num_samples, int num_taps, cudaStream_t stream, bool magnitude,
+                    int format);
 }  // namespace
 
 struct rfx_chan_plan {
@@ -483,14 +484,30 @@ int rfx_chan_plan_destroy(rfx_chan_plan* plan)
 int rfx_channelize_launch(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
                           int64_t num_samples, int num_taps, cudaStream_t stream)
 {
-    return channelize_plan(plan, x, taps, out, num_samples, num_taps, stream, false);
+    return channelize_plan(plan, x, taps, out, num_samples, num_taps, stream, false,
+                           RFX_FORMAT_CF32);
+}
+
+int rfx_channelize_launch_format(rfx_chan_plan* plan, int format, int output, const void* x,
+                                 const float* taps, void* out, int64_t num_samples, int num_taps,
+                                 cudaStream_t stream)
+{
+    if (check_format(format) != RFX_OK) {
+        return RFX_ERR_INVALID;
+    }
+    if (output != RFX_CHAN_OUT_COMPLEX && output != RFX_CHAN_OUT_MAGNITUDE) {
+        return fail(RFX_ERR_INVALID, "channelize: unknown output %d", output);
+    }
+    return channelize_plan(plan, x, taps, out, num_samples, num_taps, stream,
+                           output == RFX_CHAN_OUT_MAGNITUDE, format);
 }
 
 int rfx_channelize_magnitude_launch(rfx_chan_plan* plan, const void* x, const float* taps,
                                     float* mag, int64_t num_samples, int num_taps,
                                     cudaStream_t stream)
 {
-    return channelize_plan(plan, x, taps, mag, num_samples, num_taps, stream, true);
+    return channelize_plan(plan, x, taps, mag, num_samples, num_taps, stream, true,
+                           RFX_FORMAT_CF32);
 }
 
 int rfx_magnitude_launch(const void* x, float* mag, int64_t num_samples, cudaStream_t stream)
@@ -520,7 +537,8 @@ namespace {
 // the tensor-core form computes it in its epilogue, the plain form runs the magnitude kernel
 // over the channel outputs in the plan's scratch buffer (allocated by the first such call).
 int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void* out,
-                    int64_t num_samples, int num_taps, cudaStream_t stream, bool magnitude)
+                    int64_t num_samples, int num_taps, cudaStream_t stream, bool magnitude,
+                    int format)
 {
     if (plan == nullptr) {
         return fail(RFX_ERR_INVALID, "channelize: null plan");
@@ -554,7 +572,7 @@ int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void*
                         num_taps);
         }
         const cudaError_t err = rfx::chan_tc_launch(x, taps, plan->twiddles, out, num_samples,
-                                                    num_taps, stream, magnitude);
+                                                    num_taps, stream, magnitude, format);
         return err == cudaSuccess ? RFX_OK : cuda_fail(err, "chan_tc_launch");
     }
     if (frames != plan->frames) {
@@ -574,7 +592,7 @@ int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void*
         z = plan->scratch;
     }
     cudaError_t err = rfx::chan_branch_launch(x, taps, z, frames, plan->channels, num_taps,
-                                              stream);
+                                              stream, format);
     if (err != cudaSuccess) {
         return cuda_fail(err, "chan_branch_launch");
     }
@@ -794,6 +812,20 @@ int rfx_fir_host_format(int impl, int format, const void* x_iq, int64_t num_samp
 int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const float* taps,
                         int num_taps, int channels, void* z_iq, rfx_bench* bench)
 {
+    return rfx_channelize_host_format(impl, RFX_FORMAT_CF32, RFX_CHAN_OUT_COMPLEX, x_iq,
+                                      num_samples, taps, num_taps, channels, z_iq, bench);
+}
+
+int rfx_channelize_host_format(int impl, int format, int output, const void* x,
+                               int64_t num_samples, const float* taps, int num_taps,
+                               int channels, void* out, rfx_bench* bench)
+{
+    if (check_format(format) != RFX_OK) {
+        return RFX_ERR_INVALID;
+    }
+    if (output != RFX_CHAN_OUT_COMPLEX && output != RFX_CHAN_OUT_MAGNITUDE) {
+        return fail(RFX_ERR_INVALID, "channelize: unknown output %d", output);
+    }
     if (channels < 1) {
         return fail(RFX_ERR_INVALID, "channelize: need at least one channel");
     }
@@ -804,7 +836,7 @@ int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const f
     if (frames == 0) {
         return RFX_OK;
     }
-    if (x_iq == nullptr || z_iq == nullptr || taps == nullptr) {
+    if (x == nullptr || out == nullptr || taps == nullptr) {
         return fail(RFX_ERR_INVALID, "channelize: null host pointer");
     }
     rfx_chan_plan* plan = nullptr;
@@ -817,8 +849,9 @@ int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const f
         ~PlanGuard() { rfx_chan_plan_destroy(p); }
     } guard{plan};
     DeviceMem dx, dz, dh;
-    const size_t xbytes = static_cast<size_t>(num_samples) * 8;
-    const size_t zbytes = static_cast<size_t>(frames) * channels * 8;
+    const size_t xbytes = static_cast<size_t>(num_samples) * format_sample_bytes(format);
+    const size_t zbytes = static_cast<size_t>(frames) * channels *
+                          (output == RFX_CHAN_OUT_MAGNITUDE ? 4u : 8u);
     cudaError_t err;
     if ((err = cudaMalloc(&dx.p, xbytes)) != cudaSuccess ||
         (err = cudaMalloc(&dz.p, zbytes)) != cudaSuccess ||
@@ -828,16 +861,17 @@ int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const f
     return timed_passes(
         bench,
         [&] {
-            int r = copy(dx.p, x_iq, xbytes, cudaMemcpyHostToDevice);
+            int r = copy(dx.p, x, xbytes, cudaMemcpyHostToDevice);
             return r != RFX_OK ? r
                                : copy(dh.p, taps, sizeof(float) * num_taps,
                                       cudaMemcpyHostToDevice);
         },
         [&] {
-            return rfx_channelize_launch(plan, dx.p, static_cast<const float*>(dh.p), dz.p,
-                                         num_samples, num_taps, nullptr);
+            return rfx_channelize_launch_format(plan, format, output, dx.p,
+                                                static_cast<const float*>(dh.p), dz.p,
+                                                num_samples, num_taps, nullptr);
         },
-        [&] { return copy(z_iq, dz.p, zbytes, cudaMemcpyDeviceToHost); });
+        [&] { return copy(out, dz.p, zbytes, cudaMemcpyDeviceToHost); });
 }
 
 int rfx_magnitude_host(const void* x_iq, int64_t num_samples, float* mag, rfx_bench* bench)
@@ -870,51 +904,8 @@ int rfx_channelize_magnitude_host(int impl, const void* x_iq, int64_t num_sample
                                   const float* taps, int num_taps, int channels, float* mag,
                                   rfx_bench* bench)
 {
-    if (channels < 1) {
-        return fail(RFX_ERR_INVALID, "channelize: need at least one channel");
-    }
-    if (num_taps < 1) {
-        return fail(RFX_ERR_INVALID, "channelize: need at least one tap");
-    }
-    const int64_t frames = rfx_channelize_frames(num_samples, channels);
-    if (frames == 0) {
-        return RFX_OK;
-    }
-    if (x_iq == nullptr || mag == nullptr || taps == nullptr) {
-        return fail(RFX_ERR_INVALID, "channelize: null host pointer");
-    }
-    rfx_chan_plan* plan = nullptr;
-    int rc = rfx_chan_plan_create(impl, channels, num_samples, &plan);
-    if (rc != RFX_OK) {
-        return rc;
-    }
-    struct PlanGuard {
-        rfx_chan_plan* p;
-        ~PlanGuard() { rfx_chan_plan_destroy(p); }
-    } guard{plan};
-    DeviceMem dx, dm, dh;
-    const size_t xbytes = static_cast<size_t>(num_samples) * 8;
-    const size_t mbytes = static_cast<size_t>(frames) * channels * 4;
-    cudaError_t err;
-    if ((err = cudaMalloc(&dx.p, xbytes)) != cudaSuccess ||
-        (err = cudaMalloc(&dm.p, mbytes)) != cudaSuccess ||
-        (err = cudaMalloc(&dh.p, sizeof(float) * num_taps)) != cudaSuccess) {
-        return cuda_fail(err, "cudaMalloc");
-    }
-    return timed_passes(
-        bench,
-        [&] {
-            int r = copy(dx.p, x_iq, xbytes, cudaMemcpyHostToDevice);
-            return r != RFX_OK ? r
-                               : copy(dh.p, taps, sizeof(float) * num_taps,
-                                      cudaMemcpyHostToDevice);
-        },
-        [&] {
-            return rfx_channelize_magnitude_launch(plan, dx.p, static_cast<const float*>(dh.p),
-                                                   static_cast<float*>(dm.p), num_samples,
-                                                   num_taps, nullptr);
-        },
-        [&] { return copy(mag, dm.p, mbytes, cudaMemcpyDeviceToHost); });
+    return rfx_channelize_host_format(impl, RFX_FORMAT_CF32, RFX_CHAN_OUT_MAGNITUDE, x_iq,
+                                      num_samples, taps, num_taps, channels, mag, bench);
 }
 
 }  // extern "C"

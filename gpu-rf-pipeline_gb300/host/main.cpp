@@ -271,13 +271,28 @@ int run_channelize(int argc, char** argv)
         throw UsageError("unknown --output '" + output + "' (available: complex, magnitude)");
     }
     Bench bench(bench_config(args));
-    const std::vector<cf32> x = read_cf32(args.required("--in"));
+    StoredSamples stored = read_stored(args.required("--in"));
     const std::vector<float> taps = read_f32(args.required("--taps"));
     if (taps.empty()) {
         throw std::runtime_error(args.required("--taps") + ": no taps");
     }
-    require_int_range(x.size() + static_cast<std::size_t>(channels), "padded channelizer input");
+    require_int_range(stored.count + static_cast<std::size_t>(channels),
+                      "padded channelizer input");
     require_int_range(taps.size(), "tap array");
+    if (stored.format != SampleFormat::Cf32) {
+        // Integer recordings go to the device as stored and are converted there.
+        std::vector<cf32> z;
+        std::vector<float> mag;
+        channelize_stored(impl.name, stored, taps, channels, output == "magnitude", z, mag, bench);
+        if (output == "magnitude") {
+            finish_f32(args, "channelize", impl.name, stored.count, mag, bench);
+        } else {
+            finish(args, "channelize", impl.name, stored.count, z, bench);
+        }
+        return 0;
+    }
+    const std::vector<cf32> x = to_cf32(stored);
+    stored.bytes = std::vector<std::uint8_t>();
     if (output == "magnitude") {
         finish_f32(args, "channelize", impl.name, x.size(),
                    channelize_magnitude(impl.name, x, taps, channels, bench), bench);

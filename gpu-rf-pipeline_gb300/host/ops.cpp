@@ -113,6 +113,54 @@ void channelize_magnitude_device(rfx_chan_plan* plan, const cf32* x, const float
     RFX_CHECK(rfx_channelize_magnitude_launch(plan, x, taps, mag, num_samples, num_taps, stream));
 }
 
+void channelize_stored(const char* impl_name, const StoredSamples& x,
+                       const std::vector<float>& taps, int channels, bool magnitude,
+                       std::vector<cf32>& z, std::vector<float>& mag, Bench& bench)
+{
+    int impl = 0;
+    RFX_CHECK(rfx_parse_chan_impl(impl_name, &impl));
+    if (channels < 1) {
+        throw std::runtime_error("channelize: need at least one channel");
+    }
+    const int num_samples = static_cast<int>(x.count);
+    const int num_taps = static_cast<int>(taps.size());
+    const int frames = channelize_frames(num_samples, channels);
+    const std::size_t outputs = static_cast<std::size_t>(frames) * static_cast<std::size_t>(channels);
+    z.assign(magnitude ? 0 : outputs, cf32{});
+    mag.assign(magnitude ? outputs : 0, 0.0f);
+    if (frames == 0) {
+        return;
+    }
+    rfx_chan_plan* plan = nullptr;
+    RFX_CHECK(rfx_chan_plan_create(impl, channels, num_samples, &plan));
+    struct PlanGuard {
+        rfx_chan_plan* p;
+        ~PlanGuard() { rfx_chan_plan_destroy(p); }
+    } guard{plan};
+    DeviceBuffer<std::uint8_t> d_x(x.bytes.size());
+    DeviceBuffer<float> d_h(taps.size());
+    DeviceBuffer<cf32> d_out(outputs);   // |z| uses the first half of it
+    bench.run(
+        [&] {
+            d_x.upload(x.bytes.data(), x.bytes.size());
+            d_h.upload(taps.data(), taps.size());
+        },
+        [&] {
+            RFX_CHECK(rfx_channelize_launch_format(
+                plan, static_cast<int>(x.format),
+                magnitude ? RFX_CHAN_OUT_MAGNITUDE : RFX_CHAN_OUT_COMPLEX, d_x.get(), d_h.get(),
+                d_out.get(), num_samples, num_taps, nullptr));
+        },
+        [&] {
+            if (magnitude) {
+                CUDA_CHECK(cudaMemcpy(mag.data(), d_out.get(), outputs * sizeof(float),
+                                      cudaMemcpyDeviceToHost));
+            } else {
+                d_out.download(z.data(), outputs);
+            }
+        });
+}
+
 void magnitude_device(const cf32* x, float* mag, int num_samples)
 {
     RFX_CHECK(rfx_magnitude_launch(x, mag, num_samples, nullptr));

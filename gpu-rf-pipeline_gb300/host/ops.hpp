@@ -44,6 +44,13 @@ std::vector<float> channelize_magnitude(const char* impl, const std::vector<cf32
                                         const std::vector<float>& taps, int channels,
                                         Bench& bench);
 
+// The channelizer of samples as stored (an integer SigMF recording), converted on the device:
+// the results of channelizing the host-converted samples. `magnitude`: |z| per channel
+// (frames x channels floats, returned as floats in `mag`), else z in `z`.
+void channelize_stored(const char* impl, const StoredSamples& x, const std::vector<float>& taps,
+                       int channels, bool magnitude, std::vector<cf32>& z, std::vector<float>& mag,
+                       Bench& bench);
+
 // The channelizer's implementations, selectable with --impl (the project has one).
 using ChanFn = std::vector<cf32> (*)(const std::vector<cf32>& x, const std::vector<float>& taps,
                                      int channels, Bench& bench);

@@ -71,6 +71,7 @@ SIGNATURES = {
     "rfx_channelize_branches": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
     "rfx_channelize_tc_static": (_I, [_VP, _VP, _VP, _I64, _I, _I, _VP]),
     "rfx_channelize_magnitude_launch": (_I, [_VP, _VP, _VP, _VP, _I64, _I, _VP]),
+    "rfx_channelize_launch_format": (_I, [_VP, _I, _I, _VP, _VP, _VP, _I64, _I, _VP]),
     "rfx_magnitude_launch": (_I, [_VP, _VP, _I64, _VP]),
     "rfx_fir_stream": (_I, [_VP, _I64, _VP, _I, ctypes.POINTER(StreamConfig), _VP,
                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
@@ -82,6 +83,8 @@ SIGNATURES = {
     "rfx_channelize_magnitude_host": (_I, [_I, _VP, _I64, _VP, _I, _I, _VP,
                                            ctypes.POINTER(Bench)]),
     "rfx_magnitude_host": (_I, [_VP, _I64, _VP, ctypes.POINTER(Bench)]),
+    "rfx_channelize_host_format": (_I, [_I, _I, _I, _VP, _I64, _VP, _I, _I, _VP,
+                                        ctypes.POINTER(Bench)]),
     "rfx_autotune_fir": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),
     "rfx_autotune_save": (_I, [ctypes.c_char_p]),
     "rfx_autotune_load": (_I, [ctypes.c_char_p]),
@@ -249,6 +252,16 @@ class ChanPlan:
                                                       mag.data_ptr(), n, taps.numel(),
                                                       _stream_ptr(stream)))
 
+    def launch_format(self, fmt, x, taps, out, magnitude: bool = False, stream=None,
+                      num_samples: int | None = None) -> None:
+        """The channelizer over x stored in `fmt` (cf32 / ci16 / ci8 components), converted
+        where the kernels read it; out: complex64 z, or float32 |z| with `magnitude`."""
+        n = (x.numel() * x.element_size() // (2 * _COMPONENT_BYTES[fmt]) if num_samples is None
+             else int(num_samples))
+        _check(load().rfx_channelize_launch_format(self.handle, _format(fmt), 1 if magnitude else 0,
+                                                   x.data_ptr(), taps.data_ptr(), out.data_ptr(),
+                                                   n, taps.numel(), _stream_ptr(stream)))
+
     def close(self) -> None:
         if self.handle:
             _check(load().rfx_chan_plan_destroy(self.handle))
@@ -293,6 +306,22 @@ def channelize_magnitude(x, taps, channels: int, impl="plain", stream=None):
         plan.launch_magnitude(x, taps, mag, stream)
         torch.cuda.current_stream().synchronize()
     return mag
+
+
+def channelize_format(x, taps, channels: int, fmt: str, impl="plain", magnitude: bool = False,
+                      stream=None):
+    """The channelizer of stored samples x (CUDA tensor of cf32 / int16 / int8 components):
+    a (frames, channels) complex64 tensor, or float32 |z| with `magnitude`."""
+    import torch
+
+    n = x.numel() * x.element_size() // (2 * _COMPONENT_BYTES[fmt])
+    f = frames(n, channels)
+    out = torch.empty((f, channels), dtype=torch.float32 if magnitude else torch.complex64,
+                      device=x.device)
+    with ChanPlan(channels, n, impl) as plan:
+        plan.launch_format(fmt, x, taps, out, magnitude, stream, n)
+        torch.cuda.current_stream().synchronize()
+    return out
 
 
 def magnitude_launch(x, mag, stream=None, num_samples: int | None = None) -> None:

@@ -185,6 +185,19 @@ int rfx_channelize_magnitude_launch(rfx_chan_plan* plan, const void* x, const fl
                                     float* mag, int64_t num_samples, int num_taps,
                                     cudaStream_t stream);
 
+/* Outputs of the channelizer entry points that take one. */
+typedef enum rfx_chan_output {
+    RFX_CHAN_OUT_COMPLEX = 0,    /* z: frames x channels cf32 */
+    RFX_CHAN_OUT_MAGNITUDE = 1   /* |z|: frames x channels float32 */
+} rfx_chan_output;
+
+/* rfx_channelize_launch / rfx_channelize_magnitude_launch (`output`) over x stored in `format`
+ * (rfx_sample_format): integer components are converted where the kernels read the samples,
+ * with the results of converting them first as the project does (src/io.cpp:110-148). */
+int rfx_channelize_launch_format(rfx_chan_plan* plan, int format, int output, const void* x,
+                                 const float* taps, void* out, int64_t num_samples, int num_taps,
+                                 cudaStream_t stream);
+
 /* ---- magnitude ------------------------------------------------------------------------- */
 
 /* mag[i] = |x[i]| = sqrt(re^2 + im^2) for i < num_samples (x cf32, mag float32, both 16-byte
@@ -276,6 +289,12 @@ int rfx_channelize_host(int impl, const void* x_iq, int64_t num_samples, const f
 int rfx_channelize_magnitude_host(int impl, const void* x_iq, int64_t num_samples,
                                   const float* taps, int num_taps, int channels, float* mag,
                                   rfx_bench* bench);
+
+/* The channelizer on host samples stored in `format`, with either output (rfx_chan_output):
+ * the stored bytes are uploaded; `out` receives frames * channels cf32 or float32. */
+int rfx_channelize_host_format(int impl, int format, int output, const void* x,
+                               int64_t num_samples, const float* taps, int num_taps,
+                               int channels, void* out, rfx_bench* bench);
 
 /* The magnitude on host buffers. Replaces magnitude_cuda (src/ops.hpp:27-29). */
 int rfx_magnitude_host(const void* x_iq, int64_t num_samples, float* mag, rfx_bench* bench);

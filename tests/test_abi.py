@@ -139,3 +139,12 @@ def test_magnitude_argument_errors(lib) -> None:
     assert lib.rfx_channelize_magnitude_launch(None, p, p, p, 10, 5, None) == 1
     assert lib.rfx_magnitude_host(None, 3, None, None) == 1
     assert lib.rfx_channelize_magnitude_host(0, None, 10, None, 5, 0, None, None) == 1
+
+
+def test_channelize_format_argument_errors(lib) -> None:
+    assert lib.rfx_channelize_launch_format(None, 7, 0, None, None, None, 10, 5, None) == 1
+    assert lib.rfx_channelize_launch_format(None, 1, 5, None, None, None, 10, 5, None) == 1
+    assert lib.rfx_channelize_launch_format(None, 1, 0, None, None, None, 10, 5, None) == 1
+    assert lib.rfx_channelize_host_format(0, 4, 0, None, 10, None, 5, 4, None, None) == 1
+    assert lib.rfx_channelize_host_format(0, 1, 0, None, 10, None, 5, 0, None, None) == 1
+    assert lib.rfx_fir_stream_format(9, None, 10, None, 5, None, None, None, None) == 1
