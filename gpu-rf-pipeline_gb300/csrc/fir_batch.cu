@@ -4,20 +4,31 @@
 // Work list: every capture is cut into tiles of 96 blocks of 128 outputs (as fir_tc.cu); the
 // (capture, tile) items are numbered capture by capture, and each block of the grid takes one
 // contiguous range of items, the ranges chosen on the host so that every block gets about the
-// same work (measured: about the same per tile whatever the filter). The capture table travels in the kernel parameters (48 bytes per
-// capture), so a launch allocates nothing and can be captured in a CUDA graph.
+// same work (measured: about the same per tile whatever the filter). The capture table,
+// including each capture's two TMA tensor maps, travels in the kernel parameters (304 bytes per
+// capture, 96 captures per launch), so a launch allocates nothing and can be captured in a CUDA
+// graph.
 //
-// The per-tile pipeline is the one of fir_tc.cu (worker warps convert scaled FP16 hi/lo sample
-// planes; h_hi x_hi goes to accumulator H in groups of at most 18 MMAs, each drained into FP32
-// running sums in registers, the cross products to accumulator X, drained once per tile; one
-// thread issues the MMAs from a lean loop), with two differences: samples are loaded from global
-// memory by the workers (one tensor map per capture would not fit the parameter space), and when
-// a block's range moves on to the next capture its tap strip is rebuilt — after every MMA of the
-// previous capture has completed, which the drain of its last tile's X accumulator guarantees.
+// The per-tile pipeline is the one of fir_tc.cu, roles included: 16 drain warps hold the FP32
+// running sums and write the outputs; 7 producer warps compute each tile's scale from TMA scan
+// slices of its window, convert each K-step's samples (arriving by 2-D TMA copies, zero fill
+// outside the capture) into scaled FP16 hi/lo planes, and keep the copies flowing; one thread
+// issues the MMAs (h_hi x_hi into accumulator H in groups of at most 18, the cross products
+// into X once per tile). What the batch adds:
+//  * every quantity of a tile (window rows, tensor maps, partial last block, outputs) comes from
+//    its capture;
+//  * the shared-memory buffers are sized for the largest filter of the launch; the operand
+//    planes keep that pitch for every capture, so the sample descriptors do not change;
+//  * when a block's range moves on to the next capture, the producers rebuild the tap strip —
+//    after the MMA thread has committed the last MMA of the previous capture (`strip_free`),
+//    before the first stage of the new capture is marked full;
+//  * the drain's scale is per tile: 2^-(ex + eh), eh the tile's capture's tap scale.
 #include "fir_tc.cuh"
 #include "fir_plain.cuh"
 #include "tc_common.cuh"
+#include "tmap.hpp"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,17 +46,21 @@ constexpr int kB = 128;
 constexpr int kNB = 96;
 constexpr int kN = 2 * kNB;
 constexpr int kStagesPerTile = kB / 16;
-constexpr int kWorkerWarps = 16;
-constexpr int kWorkers = kWorkerWarps * 32;
-constexpr int kMmaWarp = 16;
-constexpr int kThreads = 17 * 32;
+constexpr int kDrainWarps = 16;
+constexpr int kProducerWarps = 7;
+constexpr int kProducers = kProducerWarps * 32;
+constexpr int kFirstProducerWarp = kDrainWarps;
+constexpr int kMmaWarp = kDrainWarps + kProducerWarps;
+constexpr int kThreads = (kMmaWarp + 1) * 32;
 constexpr int kCols = kN / 4;
 constexpr int kHGroup = 18;       // MMAs per H accumulation, at most
+constexpr int kRaw = 3;           // TMA raw-sample ring depth
+constexpr int kScanBufsMax = 4;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kXCol = kN;
 constexpr uint32_t kIdesc = idesc_f16(kB, kN);
-constexpr int kBatchCaps = 192;   // captures per launch
-constexpr int kBatchCtas = 192;   // blocks per launch (one per SM)
+constexpr int kBatchCaps = 96;    // captures per launch (the parameter space holds their maps)
+constexpr int kBatchCtas = 160;   // blocks per launch at most (one per SM)
 
 struct BatchCap {
     const float2* x;
@@ -53,36 +68,70 @@ struct BatchCap {
     const float* taps;
     long long n;
     int num_taps;
-    int C;
+    int C;                // previous blocks a block reaches back to
     int tiles;
-    int item0;   // first item of this capture in the work list
+    int item0;            // first item of this capture in the work list
 };
 
 struct BatchParams {
+    CUtensorMap xmap[kBatchCaps];  // x as rows of 256 floats (full blocks), boxes 32 x rows
+    CUtensorMap smap[kBatchCaps];  // the same rows, boxes 256 floats x srows (scan slices)
     BatchCap cap[kBatchCaps];
     int count;
     int cmax;
+    int sbufs;
     int cta_item[kBatchCtas + 1];
 };
+static_assert(sizeof(BatchParams) <= 32000, "kernel parameter space");
 
-struct Layout {
-    int rows_max;
-    uint32_t pitch, split, stage;
-    int tcount_max;
-    uint32_t taps_hi, taps_lo, stages0, bytes;
+// Per-capture window geometry.
+struct Geo {
+    int C;
+    int rows;              // window blocks per tile: kNB + C
+    int srows;             // window rows per scan slice
+    uint32_t raw_tx;       // bytes of one raw copy: rows * 32 floats
+    uint32_t scan_tx;      // bytes of one scan copy: srows * 256 floats
+    long long full_blocks; // rows the tensor maps cover
 };
 
-__host__ __device__ inline Layout batch_layout(int cmax, int stages)
+__host__ __device__ inline Geo geo_of(int C, long long n)
 {
+    Geo g;
+    g.C = C;
+    g.rows = kNB + C;
+    g.srows = (g.rows + kStagesPerTile - 1) / kStagesPerTile;
+    g.raw_tx = static_cast<uint32_t>(g.rows) * 128u;
+    g.scan_tx = static_cast<uint32_t>(g.srows) * 1024u;
+    g.full_blocks = n / kB;
+    return g;
+}
+
+// Shared memory, sized for the largest filter of the launch (cmax).
+struct Layout {
+    uint32_t pitch;       // bytes per plane: 2 rows * 16 B per window block (+16)
+    uint32_t split;
+    uint32_t stage;
+    uint32_t raw;         // raw stage pitch
+    uint32_t scan;        // scan slice pitch
+    int tcount;           // core matrices of the largest tap strip
+    uint32_t taps_hi, taps_lo, raw0, scan0, stages0, bytes;
+};
+
+__host__ __device__ inline Layout batch_layout(int cmax, int stages, int sbufs)
+{
+    const Geo g = geo_of(cmax, 0);
     Layout l;
-    l.rows_max = kNB + cmax;
-    l.pitch = static_cast<uint32_t>(2 * l.rows_max) * 16u + 16u;
+    l.pitch = static_cast<uint32_t>(2 * g.rows) * 16u + 16u;
     l.split = 2u * l.pitch;
     l.stage = 2u * l.split;
-    l.tcount_max = 16 * cmax + 31;
+    l.raw = (g.raw_tx + 127u) & ~127u;
+    l.scan = (g.scan_tx + 127u) & ~127u;
+    l.tcount = 16 * cmax + 31;
     l.taps_hi = 1024;
-    l.taps_lo = l.taps_hi + 128u * static_cast<uint32_t>(l.tcount_max);
-    l.stages0 = (l.taps_lo + 128u * static_cast<uint32_t>(l.tcount_max) + 127u) & ~127u;
+    l.taps_lo = l.taps_hi + 128u * static_cast<uint32_t>(l.tcount);
+    l.raw0 = (l.taps_lo + 128u * static_cast<uint32_t>(l.tcount) + 127u) & ~127u;
+    l.scan0 = l.raw0 + kRaw * l.raw;
+    l.stages0 = l.scan0 + static_cast<uint32_t>(sbufs) * l.scan;
     l.bytes = l.stages0 + l.stage * static_cast<uint32_t>(stages);
     return l;
 }
@@ -90,17 +139,22 @@ __host__ __device__ inline Layout batch_layout(int cmax, int stages)
 struct Ctrl {
     unsigned long long full[8];
     unsigned long long empty[8];
+    unsigned long long raw_full[kRaw];
+    unsigned long long raw_empty[kRaw];
+    unsigned long long scan_full[kScanBufsMax];
+    unsigned long long scan_empty[kScanBufsMax];
     unsigned long long pfull;
     unsigned long long pempty;
     unsigned long long xfull;
     unsigned long long xempty;
-    unsigned long long reduce[2];
-    unsigned long long tap_reduce[2];
+    unsigned long long sready[4];   // the output scale of item k is in shift[k % 4]
+    unsigned long long strip_free;  // every MMA of the previous capture has completed
     unsigned long long teardown;
     uint32_t tmem_base;
     int abort;
-    uint32_t warp_max[2][kWorkerWarps];
-    uint32_t tap_max[2][kWorkerWarps];
+    uint32_t pmax[2][kProducerWarps];
+    uint32_t tmaxw[2][kProducerWarps];
+    int shift[4];                   // ex + eh of item k
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
@@ -113,8 +167,7 @@ __device__ __forceinline__ int capture_of(const BatchParams& p, int item, int cu
     return cursor;
 }
 
-// H groups of a tile of a capture with P chunks: `ksg` whole K-steps (P <= 18), or `gpk`
-// groups of at most `cpg` chunks per K-step (P > 18); see fir_tc.cu.
+// H groups of a tile with P chunks (see fir_tc.cu).
 struct HGroups {
     int ksg;
     int gpk;
@@ -156,20 +209,16 @@ __device__ __forceinline__ void h_group_range(const HGroups& g, int P, int gi, i
     }
 }
 
-// Last K-step of group gi.
-__device__ __forceinline__ int h_group_last_step(const HGroups& g, int gi)
-{
-    return g.gpk == 1 ? min(kStagesPerTile, (gi + 1) * g.ksg) - 1 : gi / g.gpk;
-}
-
 }  // namespace
 
 template <int S>
-__global__ void __launch_bounds__(kThreads, 1) fir_batch_kernel(const __grid_constant__ BatchParams p)
+__global__ void __launch_bounds__(kThreads, 1)
+fir_batch_kernel(const __grid_constant__ BatchParams p)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
-    const Layout lay = batch_layout(p.cmax, S);
+    const int sbufs = p.sbufs;
+    const Layout lay = batch_layout(p.cmax, S, sbufs);
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const uint32_t sbase = smem_u32(smem);
@@ -177,24 +226,35 @@ __global__ void __launch_bounds__(kThreads, 1) fir_batch_kernel(const __grid_con
     unsigned int* fault = &g_fault_fir_batch;
     const int first_item = p.cta_item[blockIdx.x];
     const int my_items = p.cta_item[blockIdx.x + 1] - first_item;
-    const int my_steps = my_items * kStagesPerTile;
     if (my_items <= 0) {
         return;  // uniform for the whole block: nothing allocated yet
     }
+    const int my_steps = my_items * kStagesPerTile;
+    const int scan_slices = (my_items - 1) * kStagesPerTile;
+    // Tile index of item k within its capture.
+    auto tile_in = [&](const BatchCap& c, int k) { return first_item + k - c.item0; };
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < S; ++i) {
-            mbar_init(smem_u32(&ctl.full[i]), kWorkerWarps);
+            mbar_init(smem_u32(&ctl.full[i]), kProducerWarps);
             mbar_init(smem_u32(&ctl.empty[i]), 1);
         }
-        for (int i = 0; i < 2; ++i) {
-            mbar_init(smem_u32(&ctl.reduce[i]), kWorkerWarps);
-            mbar_init(smem_u32(&ctl.tap_reduce[i]), kWorkerWarps);
+        for (int i = 0; i < kRaw; ++i) {
+            mbar_init(smem_u32(&ctl.raw_full[i]), 1);
+            mbar_init(smem_u32(&ctl.raw_empty[i]), kProducerWarps);
+        }
+        for (int i = 0; i < sbufs; ++i) {
+            mbar_init(smem_u32(&ctl.scan_full[i]), 1);
+            mbar_init(smem_u32(&ctl.scan_empty[i]), kProducerWarps);
+        }
+        for (int i = 0; i < 4; ++i) {
+            mbar_init(smem_u32(&ctl.sready[i]), 1);
         }
         mbar_init(smem_u32(&ctl.pfull), 1);
-        mbar_init(smem_u32(&ctl.pempty), kWorkerWarps);
+        mbar_init(smem_u32(&ctl.pempty), kDrainWarps);
         mbar_init(smem_u32(&ctl.xfull), 1);
-        mbar_init(smem_u32(&ctl.xempty), kWorkerWarps);
+        mbar_init(smem_u32(&ctl.xempty), kDrainWarps);
+        mbar_init(smem_u32(&ctl.strip_free), 1);
         mbar_init(smem_u32(&ctl.teardown), 1);
         ctl.abort = 0;
         fence_mbar_init();
@@ -202,230 +262,52 @@ __global__ void __launch_bounds__(kThreads, 1) fir_batch_kernel(const __grid_con
     if (warp == kMmaWarp) {
         tmem_alloc(smem_u32(&ctl.tmem_base), kTmemCols);
     }
+    __syncthreads();
+    // Raw copy of K-step u into raw slot `slot`: item u / 8, floats 32 (u % 8) .. of its window.
+    auto issue_raw = [&](int u, int cursor, uint32_t dst, uint32_t bar) -> int {
+        const int k = u / kStagesPerTile;
+        cursor = capture_of(p, first_item + k, cursor);
+        const BatchCap& c = p.cap[cursor];
+        const Geo g = geo_of(c.C, c.n);
+        mbar_arrive_expect_tx(bar, g.raw_tx);
+        tma_load_2d(dst, &p.xmap[cursor], 32 * (u % kStagesPerTile), tile_in(c, k) * kNB - c.C,
+                    bar);
+        return cursor;
+    };
+    // Scan slice q: item q / 8 + 1's window rows (q % 8) srows .. + srows.
+    auto issue_scan = [&](int q, int cursor) -> int {
+        const int kn = q / kStagesPerTile + 1;
+        cursor = capture_of(p, first_item + kn, cursor);
+        const BatchCap& c = p.cap[cursor];
+        const Geo g = geo_of(c.C, c.n);
+        const uint32_t bar = smem_u32(&ctl.scan_full[q % sbufs]);
+        mbar_arrive_expect_tx(bar, g.scan_tx);
+        tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(q % sbufs) * lay.scan, &p.smap[cursor], 0,
+                    tile_in(c, kn) * kNB - c.C + (q % kStagesPerTile) * g.srows, bar);
+        return cursor;
+    };
+    if (threadIdx.x == 0) {
+        int cur = capture_of(p, first_item, 0);
+        for (int u = 0; u < kRaw && u < my_steps; ++u) {
+            cur = issue_raw(u, cur, sbase + lay.raw0 + u * lay.raw, smem_u32(&ctl.raw_full[u]));
+        }
+        cur = capture_of(p, first_item, 0);
+        for (int q = 0; q < sbufs - 2 && q < scan_slices; ++q) {
+            cur = issue_scan(q, cur);
+        }
+    }
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    if (warp < kWorkerWarps) {
+    if (warp < kDrainWarps) {
+        // ---- drain warps: running sums, outputs ----------------------------------------------
         const int quarter = warp & 3;
         const int slice = warp >> 2;
         const int r = kB - 1 - (quarter * 32 + lane);
         const uint32_t lane_addr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
                                    static_cast<uint32_t>(slice * kCols);
-        const int wtid = threadIdx.x;
-        int ex_even = 0;     // scale exponents of even and odd items
-        int ex_odd = 0;
-        int eh = 0;          // tap scale of the strip currently in shared memory
-        int switches = 0;    // tap-strip rebuilds so far (phase of tap_reduce)
-        int cur_prod = capture_of(p, first_item, 0);
-        int cur_drain = cur_prod;
-        int cur_scan = cur_prod;
-
-        auto item_capture = [&](int local_item, int& cursor) -> int {
-            cursor = capture_of(p, first_item + local_item, cursor);
-            return cursor;
-        };
-        auto window = [&](const BatchCap& c, int tile, long long& lo_s, long long& hi_s) {
-            const long long j0 = static_cast<long long>(tile) * kNB;
-            const long long win0 = (j0 - c.C) * kB;
-            lo_s = win0 > 0 ? win0 : 0;
-            hi_s = (j0 + kNB) * kB < c.n ? (j0 + kNB) * kB : c.n;
-        };
-        auto load_pair = [&](const float2* x, long long s, long long hi_s) -> uint32_t {
-            if (s + 1 < hi_s) {
-                return absmax4(__ldg(reinterpret_cast<const float4*>(x + s)));
-            }
-            if (s < hi_s) {
-                const float2 w2 = __ldg(x + s);
-                return max(absbits(w2.x), absbits(w2.y));
-            }
-            return 0u;
-        };
-        auto reduce_scale = [&](int k, uint32_t m) -> bool {
-            m = __reduce_max_sync(0xFFFFFFFFu, m);
-            const int rb = k & 1;
-            if (lane == 0) {
-                ctl.warp_max[rb][warp] = m;
-                mbar_arrive(smem_u32(&ctl.reduce[rb]));
-            }
-            if (!mbar_wait_bounded(smem_u32(&ctl.reduce[rb]), (k >> 1) & 1, fault,
-                                   kFaultStageEmpty, abort)) {
-                return false;
-            }
-            uint32_t tmax = 0;
-#pragma unroll
-            for (int w = 0; w < kWorkerWarps; ++w) {
-                tmax = max(tmax, ctl.warp_max[rb][w]);
-            }
-            if (k & 1) {
-                ex_odd = scale_exponent(tmax);
-            } else {
-                ex_even = scale_exponent(tmax);
-            }
-            return true;
-        };
-        // The tap strip of capture c (every worker writes its share after its own drain of the
-        // last partial sum that used the old strip).
-        auto build_strip = [&](const BatchCap& c) -> bool {
-            uint32_t m = 0;
-            for (int k = wtid; k < c.num_taps; k += kWorkers) {
-                m = max(m, absbits(__ldg(c.taps + k)));
-            }
-            m = __reduce_max_sync(0xFFFFFFFFu, m);
-            const int rb = switches & 1;
-            if (lane == 0) {
-                ctl.tap_max[rb][warp] = m;
-                mbar_arrive(smem_u32(&ctl.tap_reduce[rb]));
-            }
-            if (!mbar_wait_bounded(smem_u32(&ctl.tap_reduce[rb]), (switches >> 1) & 1, fault,
-                                   kFaultStageEmpty, abort)) {
-                return false;
-            }
-            uint32_t tmax = 0;
-#pragma unroll
-            for (int w = 0; w < kWorkerWarps; ++w) {
-                tmax = max(tmax, ctl.tap_max[rb][w]);
-            }
-            ++switches;
-            eh = scale_exponent(tmax);
-            const float fa = exp2i(eh / 2);
-            const float fb = exp2i(eh - eh / 2);
-            const int dmax = (c.C + 1) * kB - 1;
-            const int pairs = (16 * c.C + 31) * 32;
-            for (int i = wtid; i < pairs; i += kWorkers) {
-                const int t = i >> 5;
-                const int q = (i >> 2) & 7;
-                const int e = (i & 3) * 2;
-                const int i0 = dmax - 8 * t - q - e;
-                const int i1 = i0 - 1;
-                const float v0 = (i0 >= 0 && i0 < c.num_taps) ? __ldg(c.taps + i0) * fa * fb : 0.0f;
-                const float v1 = (i1 >= 0 && i1 < c.num_taps) ? __ldg(c.taps + i1) * fa * fb : 0.0f;
-                uint32_t hi, lo;
-                split2(v0, v1, hi, lo);
-                const uint32_t off = static_cast<uint32_t>(t) * 128u + q * 16u + e * 2u;
-                sts32(sbase + lay.taps_hi + off, hi);
-                sts32(sbase + lay.taps_lo + off, lo);
-            }
-            return true;  // made visible to the MMAs by the fence before the next full arrive
-        };
-        uint32_t next_max = 0;
-        auto produce = [&](int v) -> bool {
-            const int k = v / kStagesPerTile;
-            const int st = v % kStagesPerTile;
-            const int ci = item_capture(k, cur_prod);
-            const BatchCap& c = p.cap[ci];
-            const int tile = first_item + k - c.item0;
-            const long long j0 = static_cast<long long>(tile) * kNB;
-            uint32_t pre[3] = {0u, 0u, 0u};
-            const bool has_next = k + 1 < my_items;
-            if (has_next) {
-                const int cn = item_capture(k + 1, cur_scan);
-                const BatchCap& c2 = p.cap[cn];
-                long long lo_n, hi_n;
-                window(c2, first_item + k + 1 - c2.item0, lo_n, hi_n);
-                const long long pairs = (hi_n - lo_n + 1) / 2;
-                const long long per = (pairs + kStagesPerTile - 1) / kStagesPerTile;
-                const long long end = (st + 1) * per < pairs ? (st + 1) * per : pairs;
-                long long idx = st * per + wtid;
-#pragma unroll
-                for (int i = 0; i < 3; ++i, idx += kWorkers) {
-                    if (idx < end) {
-                        pre[i] = load_pair(c2.x, lo_n + 2 * idx, hi_n);
-                    }
-                }
-                for (; idx < end; idx += kWorkers) {
-                    pre[0] = max(pre[0], load_pair(c2.x, lo_n + 2 * idx, hi_n));
-                }
-            }
-            const int ex = (k & 1) ? ex_odd : ex_even;
-            const float fa = exp2i(ex / 2);
-            const float fb = exp2i(ex - ex / 2);
-            const int slot = v % S;
-            if (!mbar_wait_bounded(smem_u32(&ctl.empty[slot]), ((v / S) & 1) ^ 1, fault,
-                                   kFaultStageEmpty, abort)) {
-                return false;
-            }
-            const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
-            const int items = (kNB + c.C) * 8;
-            for (int f = wtid; f < items; f += kWorkers) {
-                const int b = f >> 3;
-                const int q = f & 7;
-                const long long sidx = (j0 - c.C + b) * kB + 16 * st + 2 * q;
-                float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (sidx >= 0 && sidx + 1 < c.n) {
-                    v4 = __ldg(reinterpret_cast<const float4*>(c.x + sidx));
-                } else if (sidx >= 0 && sidx < c.n) {
-                    const float2 w2 = __ldg(c.x + sidx);
-                    v4.x = w2.x;
-                    v4.y = w2.y;
-                }
-                uint32_t re_hi, re_lo, im_hi, im_lo;
-                split2(v4.x * fa * fb, v4.z * fa * fb, re_hi, re_lo);
-                split2(v4.y * fa * fb, v4.w * fa * fb, im_hi, im_lo);
-                const uint32_t plane = static_cast<uint32_t>(q >> 2) * lay.pitch;
-                const uint32_t elem = static_cast<uint32_t>(q & 3) * 4u;
-                const uint32_t row_re = plane + static_cast<uint32_t>(2 * b) * 16u + elem;
-                sts32(stage + row_re, re_hi);
-                sts32(stage + row_re + 16u, im_hi);
-                sts32(stage + lay.split + row_re, re_lo);
-                sts32(stage + lay.split + row_re + 16u, im_lo);
-            }
-            fence_proxy_async_smem();
-            __syncwarp();
-            if (lane == 0) {
-                mbar_arrive(smem_u32(&ctl.full[slot]));
-            }
-            if (has_next) {
-                next_max = max(next_max, max(pre[0], max(pre[1], pre[2])));
-                if (st == kStagesPerTile - 1) {
-                    if (!reduce_scale(k + 1, next_max)) {
-                        return false;
-                    }
-                    next_max = 0;
-                }
-            }
-            return true;
-        };
-        // A K-step that starts a new capture (not the block's first) needs a new tap strip.
-        int sw_cursor = cur_prod;
-        auto starts_capture = [&](int v) -> bool {
-            if (v % kStagesPerTile != 0 || v == 0) {
-                return false;
-            }
-            const int k = v / kStagesPerTile;
-            const int a = item_capture(k - 1, sw_cursor);
-            const int b = capture_of(p, first_item + k, a);
-            return a != b;
-        };
-
-        bool ok = true;
-        {
-            // Prologue: tap strip and scale of the first item, then the first stages.
-            const BatchCap& c0 = p.cap[cur_prod];
-            ok = build_strip(c0);
-            long long lo0, hi0;
-            window(c0, first_item - c0.item0, lo0, hi0);
-            uint32_t m = 0;
-            const long long pairs = (hi0 - lo0 + 1) / 2;
-            for (long long base = 0; base < pairs && ok; base += 8 * kWorkers) {
-                uint32_t part[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const long long idx = base + wtid + i * kWorkers;
-                    part[i] = idx < pairs ? load_pair(c0.x, lo0 + 2 * idx, hi0) : 0u;
-                }
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    m = max(m, part[i]);
-                }
-            }
-            ok = ok && reduce_scale(0, m);
-        }
-        int produced = 0;
-        while (ok && produced < S && produced < my_steps && !starts_capture(produced)) {
-            ok = produce(produced++);
-        }
         float acc[kCols];
 #pragma unroll
         for (int i = 0; i < kCols; ++i) {
@@ -446,15 +328,14 @@ __global__ void __launch_bounds__(kThreads, 1) fir_batch_kernel(const __grid_con
             fence_before();
             __syncwarp();
         };
-        int g = 0;   // H groups drained so far (the pfull / pempty phase)
-        int gi = 0;  // next group of the current item
-        for (int u = 0; u < my_steps && ok && !*abort; ++u) {
-            const int k = u / kStagesPerTile;
-            const int st = u % kStagesPerTile;
-            const int ci = item_capture(k, cur_drain);
-            const BatchCap& c = p.cap[ci];
+        bool ok = true;
+        int g = 0;   // H groups drained so far
+        int cursor = capture_of(p, first_item, 0);
+        for (int k = 0; k < my_items && ok && !*abort; ++k) {
+            cursor = capture_of(p, first_item + k, cursor);
+            const BatchCap& c = p.cap[cursor];
             const HGroups grp = h_groups(c.C + 1, S);
-            while (gi < grp.per_tile && h_group_last_step(grp, gi) <= st) {
+            for (int gi = 0; gi < grp.per_tile; ++gi, ++g) {
                 if (!mbar_wait_bounded(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
                                        abort)) {
                     ok = false;
@@ -464,74 +345,307 @@ __global__ void __launch_bounds__(kThreads, 1) fir_batch_kernel(const __grid_con
                 if (lane == 0) {
                     mbar_arrive(smem_u32(&ctl.pempty));
                 }
-                ++g;
-                ++gi;
             }
-            if (!ok) {
+            if (!ok ||
+                !mbar_wait_bounded(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull, abort)) {
                 break;
             }
-            if (st == kStagesPerTile - 1) {
-                if (!mbar_wait_bounded(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull,
-                                       abort)) {
-                    break;
-                }
-                drain(kXCol);
-                if (lane == 0) {
-                    mbar_arrive(smem_u32(&ctl.xempty));
-                }
-                const int shift = -(((k & 1) ? ex_odd : ex_even) + eh);
-                const float fa = exp2i(shift / 2);
-                const float fb = exp2i(shift - shift / 2);
-                const long long jb0 =
-                    static_cast<long long>(first_item + k - c.item0) * kNB + slice * (kCols / 2);
-#pragma unroll
-                for (int b = 0; b < kCols / 2; ++b) {
-                    const long long o = (jb0 + b) * kB + r;
-                    if (o < c.n) {
-                        c.y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
-                    }
-                    acc[2 * b] = 0.0f;
-                    acc[2 * b + 1] = 0.0f;
-                }
-                gi = 0;
+            drain(kXCol);
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&ctl.xempty));
             }
-            while (ok && produced < my_steps && produced <= u + S) {
-                if (starts_capture(produced)) {
-                    if (produced != u + 1) {
-                        break;  // wait until every MMA of the old capture has been drained
-                    }
-                    ok = build_strip(p.cap[capture_of(p, first_item + produced / kStagesPerTile,
-                                                      cur_prod)]);
-                    if (!ok) {
-                        break;
-                    }
+            if (!mbar_wait_bounded(smem_u32(&ctl.sready[k & 3]), (k >> 2) & 1, fault,
+                                   kFaultScale, abort)) {
+                break;
+            }
+            const int shift = -*reinterpret_cast<volatile int*>(&ctl.shift[k & 3]);
+            const float fa = exp2i(shift / 2);
+            const float fb = exp2i(shift - shift / 2);
+            const long long jb0 =
+                static_cast<long long>(tile_in(c, k)) * kNB + slice * (kCols / 2);
+#pragma unroll
+            for (int b = 0; b < kCols / 2; ++b) {
+                const long long o = (jb0 + b) * kB + r;
+                if (o < c.n) {
+                    c.y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
                 }
-                ok = produce(produced++);
+                acc[2 * b] = 0.0f;
+                acc[2 * b + 1] = 0.0f;
             }
         }
-    } else if (lane == 0) {
-        // MMA issuer: lean loop, per MMA one descriptor step and the MMA (see fir_tc.cu).
-        const uint32_t taps_hi = sbase + lay.taps_hi;
-        const uint32_t taps_lo = sbase + lay.taps_lo;
+    } else if (warp < kFirstProducerWarp + kProducerWarps) {
+        // ---- producers: tap strips, scales, operand stages, copies ---------------------------
+        const int pw = warp - kFirstProducerWarp;
+        const int ptid = static_cast<int>(threadIdx.x) - kFirstProducerWarp * 32;
+        int ex_even = 0;            // sample scale exponents of even and odd items
+        int ex_odd = 0;
+        int eh = 0;                 // tap scale exponent of capture eh_cap
+        int eh_cap = -1;
+        int switches = 0;           // tap strips rebuilt after the first (strip_free phases)
+        int tmax_uses = 0;
+        uint32_t next_max = 0;
+        int cur_prod = capture_of(p, first_item, 0);
+        int cur_scan = cur_prod;
+        int cur_raw = cur_prod;
+        int cur_issue = cur_prod;
+
+        // Max of |samples| of capture c in [s, s + 2) clipped to hi_s.
+        auto load_pair = [&](const BatchCap& c, long long s, long long hi_s) -> uint32_t {
+            if (s + 1 < hi_s) {
+                return absmax4(__ldg(reinterpret_cast<const float4*>(c.x + s)));
+            }
+            if (s < hi_s) {
+                const float2 w2 = __ldg(c.x + s);
+                return max(absbits(w2.x), absbits(w2.y));
+            }
+            return 0u;
+        };
+        // Max over the producers of a per-thread value (all producers call it together).
+        auto producers_max = [&](uint32_t m, uint32_t (&slots)[2][kProducerWarps], int use) {
+            m = __reduce_max_sync(0xFFFFFFFFu, m);
+            if (lane == 0) {
+                slots[use & 1][pw] = m;
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory");
+            uint32_t t = 0;
+#pragma unroll
+            for (int w = 0; w < kProducerWarps; ++w) {
+                t = max(t, slots[use & 1][w]);
+            }
+            return t;
+        };
+        // Tap scale exponent of capture ci (once per capture, when its first tile's scale is
+        // published).
+        auto tap_exponent = [&](int ci) {
+            const BatchCap& c = p.cap[ci];
+            uint32_t m = 0;
+            for (int i = ptid; i < c.num_taps; i += kProducers) {
+                m = max(m, absbits(__ldg(c.taps + i)));
+            }
+            eh = scale_exponent(producers_max(m, ctl.tmaxw, tmax_uses++));
+            eh_cap = ci;
+        };
+        // Item k's sample scale from its window maximum m, and its output shift ex + eh.
+        auto reduce_scale = [&](int k, uint32_t m, int ci) {
+            const uint32_t tmax = producers_max(m, ctl.pmax, k);
+            if (ci != eh_cap) {
+                tap_exponent(ci);
+            }
+            const int ex = min(scale_exponent(tmax), 127);
+            if (k & 1) {
+                ex_odd = ex;
+            } else {
+                ex_even = ex;
+            }
+            if (ptid == 0) {
+                ctl.shift[k & 3] = ex + eh;
+                mbar_arrive(smem_u32(&ctl.sready[k & 3]));
+            }
+        };
+        // The tap strip of capture ci, scaled by 2^eh (eh of ci).
+        auto build_strip = [&](int ci) {
+            const BatchCap& c = p.cap[ci];
+            const float fa = exp2i(eh / 2);
+            const float fb = exp2i(eh - eh / 2);
+            const int dmax = (c.C + 1) * kB - 1;
+            const int pairs = (16 * c.C + 31) * 32;
+            for (int i = ptid; i < pairs; i += kProducers) {
+                const int t = i >> 5;
+                const int q = (i >> 2) & 7;
+                const int e = (i & 3) * 2;
+                const int i0 = dmax - 8 * t - q - e;
+                const int i1 = i0 - 1;
+                const float v0 = (i0 >= 0 && i0 < c.num_taps) ? __ldg(c.taps + i0) * fa * fb : 0.0f;
+                const float v1 = (i1 >= 0 && i1 < c.num_taps) ? __ldg(c.taps + i1) * fa * fb : 0.0f;
+                uint32_t hi, lo;
+                split2(v0, v1, hi, lo);
+                const uint32_t off = static_cast<uint32_t>(t) * 128u + q * 16u + e * 2u;
+                sts32(sbase + lay.taps_hi + off, hi);
+                sts32(sbase + lay.taps_lo + off, lo);
+            }
+            // Made visible to the MMAs by the fence before this K-step's full arrival.
+        };
+        // Scan slice q (item q / 8 + 1), copied by TMA sbufs - 1 K-steps earlier.
+        auto consume_slice = [&](int q) -> bool {
+            const int qb = q % sbufs;
+            if (!mbar_wait_bounded(smem_u32(&ctl.scan_full[qb]), (q / sbufs) & 1, fault,
+                                   kFaultTileLoad, abort)) {
+                return false;
+            }
+            const int k = q / kStagesPerTile + 1;
+            cur_scan = capture_of(p, first_item + k, cur_scan);
+            const BatchCap& c = p.cap[cur_scan];
+            const Geo g = geo_of(c.C, c.n);
+            const long long j0 = static_cast<long long>(tile_in(c, k)) * kNB;
+            const int r0 = (q % kStagesPerTile) * g.srows;
+            const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
+            const int quads = min(g.srows, g.rows - r0) * 64;   // sample pairs in the window
+            uint32_t m = next_max;
+#pragma unroll 4
+            for (int f = ptid; f < quads; f += kProducers) {
+                m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
+            }
+            // The capture's partial last block lies outside its tensor map.
+            const long long tail_row = g.full_blocks - (j0 - c.C) - r0;
+            if (tail_row >= 0 && tail_row * 64 < quads && ptid < 64) {
+                m = max(m, load_pair(c, g.full_blocks * kB + 2 * ptid, c.n));
+            }
+            next_max = m;
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&ctl.scan_empty[qb]));
+            }
+            if (q % kStagesPerTile == kStagesPerTile - 1) {
+                reduce_scale(k, next_max, cur_scan);
+                next_max = 0;
+            }
+            return true;
+        };
+        // Producing K-step v: finish scan slice v - 1; at a new capture's first K-step, rebuild
+        // the tap strip; convert the raw samples; queue step v + kRaw's raw copy and scan slice
+        // v + sbufs - 2.
+        auto produce = [&](int v) -> bool {
+            if (v >= 1 && v - 1 < scan_slices && !consume_slice(v - 1)) {
+                return false;
+            }
+            const int k = v / kStagesPerTile;
+            const int st = v % kStagesPerTile;
+            const int prev = cur_prod;
+            cur_prod = capture_of(p, first_item + k, cur_prod);
+            const BatchCap& c = p.cap[cur_prod];
+            if (st == 0 && k > 0 && cur_prod != prev) {
+                // Every MMA that reads the old strip has completed before it is overwritten.
+                if (!mbar_wait_bounded(smem_u32(&ctl.strip_free), switches & 1, fault,
+                                       kFaultStageEmpty, abort)) {
+                    return false;
+                }
+                ++switches;
+                build_strip(cur_prod);
+            }
+            const Geo g = geo_of(c.C, c.n);
+            const long long j0 = static_cast<long long>(tile_in(c, k)) * kNB;
+            const int ex = (k & 1) ? ex_odd : ex_even;
+            const float fs = exp2_exact(ex);   // ex in [-113, 127]: exact scaling
+            const f32x2 fs2 = pack2(fs, fs);
+            const int slot = v % S;
+            const int rslot = v % kRaw;
+            if (!mbar_wait_bounded(smem_u32(&ctl.empty[slot]), ((v / S) & 1) ^ 1, fault,
+                                   kFaultStageEmpty, abort) ||
+                !mbar_wait_bounded(smem_u32(&ctl.raw_full[rslot]), (v / kRaw) & 1, fault,
+                                   kFaultTileLoad, abort)) {
+                return false;
+            }
+            const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
+            const uint32_t raw = sbase + lay.raw0 + static_cast<uint32_t>(rslot) * lay.raw;
+            const long long tail_rel = g.full_blocks - (j0 - c.C);
+            const int b_tail = tail_rel >= 0 && tail_rel < g.rows ? static_cast<int>(tail_rel) : -1;
+            static_assert(kProducers % 8 == 0, "producer stride");
+            const int q = ptid & 7;
+            const uint32_t elem_off = static_cast<uint32_t>(q >> 2) * lay.pitch +
+                                      static_cast<uint32_t>(q & 3) * 4u;
+#pragma unroll 2
+            for (int b = ptid >> 3; b < g.rows; b += kProducers / 8) {
+                const int f = 8 * b + q;
+                float4 v4;
+                if (b != b_tail) {
+                    v4 = lds128(raw + static_cast<uint32_t>(f) * 16u);  // zero outside [0, n)
+                } else {
+                    const long long sidx = g.full_blocks * kB + 16 * st + 2 * q;
+                    v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (sidx + 1 < c.n) {
+                        v4 = __ldg(reinterpret_cast<const float4*>(c.x + sidx));
+                    } else if (sidx < c.n) {
+                        const float2 w2 = __ldg(c.x + sidx);
+                        v4.x = w2.x;
+                        v4.y = w2.y;
+                    }
+                }
+                const float2 s0 = unpack2(mul2(pack2(v4.x, v4.y), fs2));
+                const float2 s1 = unpack2(mul2(pack2(v4.z, v4.w), fs2));
+                uint32_t re_hi, re_lo, im_hi, im_lo;
+                split2(s0.x, s1.x, re_hi, re_lo);
+                split2(s0.y, s1.y, im_hi, im_lo);
+                const uint32_t row_re = elem_off + static_cast<uint32_t>(2 * b) * 16u;
+                sts32(stage + row_re, re_hi);
+                sts32(stage + row_re + 16u, im_hi);
+                sts32(stage + lay.split + row_re, re_lo);
+                sts32(stage + lay.split + row_re + 16u, im_lo);
+            }
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(smem_u32(&ctl.full[slot]));
+                mbar_arrive(smem_u32(&ctl.raw_empty[rslot]));
+            }
+            if (ptid == 0) {
+                if (v + kRaw < my_steps) {
+                    if (!mbar_wait_bounded(smem_u32(&ctl.raw_empty[rslot]), (v / kRaw) & 1,
+                                           fault, kFaultStageEmpty, abort)) {
+                        return false;
+                    }
+                    cur_raw = issue_raw(v + kRaw, cur_raw, raw, smem_u32(&ctl.raw_full[rslot]));
+                }
+                const int qn = v + sbufs - 2;
+                if (qn < scan_slices) {
+                    if (!mbar_wait_bounded(smem_u32(&ctl.scan_empty[qn % sbufs]),
+                                           ((qn / sbufs) & 1) ^ 1, fault, kFaultStageEmpty,
+                                           abort)) {
+                        return false;
+                    }
+                    cur_issue = issue_scan(qn, cur_issue);
+                }
+            }
+            return true;
+        };
+
+        // Item 0: its capture's tap scale and strip, its scale from its whole window.
+        {
+            const BatchCap& c = p.cap[cur_prod];
+            const long long j0 = static_cast<long long>(tile_in(c, 0)) * kNB;
+            const long long win0 = (j0 - c.C) * kB;
+            const long long lo0 = win0 > 0 ? win0 : 0;
+            const long long hi0 = (j0 + kNB) * kB < c.n ? (j0 + kNB) * kB : c.n;
+            const long long pairs = (hi0 - lo0 + 1) / 2;
+            uint32_t m = 0;
+            for (long long base = 0; base < pairs; base += 8 * kProducers) {
+                uint32_t part[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const long long idx = base + ptid + i * kProducers;
+                    part[i] = idx < pairs ? load_pair(c, lo0 + 2 * idx, hi0) : 0u;
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    m = max(m, part[i]);
+                }
+            }
+            reduce_scale(0, m, cur_prod);
+            build_strip(cur_prod);
+        }
+        bool ok = true;
+        for (int v = 0; v < my_steps && ok && !*abort; ++v) {
+            ok = produce(v);
+        }
+    } else if (warp == kMmaWarp && lane == 0) {
+        // ---- MMA issuer (one thread), as in fir_tc.cu, per item's capture -------------------
         const unsigned long long a_desc = smem_desc(0, 128, 128);
         const unsigned long long b_desc = smem_desc(0, lay.pitch, 128);
         const uint32_t stage_units = lay.stage >> 4;
         const uint32_t split_units = lay.split >> 4;
-        const uint32_t stages_units = (sbase + lay.stages0) >> 4;
         const uint32_t h_acc = tmem;
         const uint32_t x_acc = tmem + kXCol;
         int cursor = capture_of(p, first_item, 0);
-        int g = 0;
         int ready = 0;
+        int g = 0;
         bool stop = false;
         for (int k = 0; k < my_items && !stop && !*abort; ++k) {
             cursor = capture_of(p, first_item + k, cursor);
             const int C = p.cap[cursor].C;
             const int P = C + 1;
             const HGroups grp = h_groups(P, S);
-            const uint32_t a_hi0 = (taps_hi >> 4) + static_cast<uint32_t>(16 * C) * 8u;
-            const uint32_t a_lo0 = (taps_lo >> 4) + static_cast<uint32_t>(16 * C) * 8u;
-            const uint32_t b_base = stages_units + static_cast<uint32_t>(2 * C);
+            const uint32_t a_hi0 = ((sbase + lay.taps_hi) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+            const uint32_t a_lo0 = ((sbase + lay.taps_lo) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+            const uint32_t b_base = ((sbase + lay.stages0) >> 4) + static_cast<uint32_t>(2 * C);
             for (int gi = 0; gi < grp.per_tile && !stop; ++gi, ++g) {
                 int st0, st1, c0, c1;
                 h_group_range(grp, P, gi, st0, st1, c0, c1);
@@ -554,14 +668,23 @@ __global__ void __launch_bounds__(kThreads, 1) fir_batch_kernel(const __grid_con
                         fence_after();
                         ready = u + 1;
                     }
-                    uint32_t a = a_hi0 + static_cast<uint32_t>(2 * st - 16 * c0) * 8u;
-                    uint32_t b = b_base + static_cast<uint32_t>(slot) * stage_units -
-                                 static_cast<uint32_t>(2 * c0);
-                    for (int c = c0; c < c1; ++c) {
-                        mma_f16<kIdesc>(h_acc, a_desc | a, b_desc | b, acc);
+                    unsigned long long da =
+                        a_desc | (a_hi0 + static_cast<uint32_t>(2 * st - 16 * c0) * 8u);
+                    unsigned long long db =
+                        b_desc | (b_base + static_cast<uint32_t>(slot) * stage_units -
+                                  static_cast<uint32_t>(2 * c0));
+                    int c = c0;
+                    if (acc == 0) {
+                        mma_f16<kIdesc>(h_acc, da, db, 0u);
                         acc = 1;
-                        a -= 128;
-                        b -= 2;
+                        da -= 128;
+                        db -= 2;
+                        ++c;
+                    }
+                    for (; c < c1; ++c) {
+                        mma_f16_acc<kIdesc>(h_acc, da, db);
+                        da -= 128;
+                        db -= 2;
                     }
                 }
                 if (stop) {
@@ -580,31 +703,55 @@ __global__ void __launch_bounds__(kThreads, 1) fir_batch_kernel(const __grid_con
                 for (int st = st0; st < st1; ++st) {
                     const int slot = (k * kStagesPerTile + st) % S;
                     const uint32_t off = static_cast<uint32_t>(2 * st - 16 * c0) * 8u;
-                    uint32_t ah = a_hi0 + off;
-                    uint32_t al = a_lo0 + off;
-                    uint32_t b = b_base + static_cast<uint32_t>(slot) * stage_units -
-                                 static_cast<uint32_t>(2 * c0);
-                    for (int c = c0; c < c1; ++c) {
-                        mma_f16<kIdesc>(x_acc, a_desc | ah, b_desc | (b + split_units), acc);
-                        mma_f16<kIdesc>(x_acc, a_desc | al, b_desc | b, 1u);
+                    unsigned long long dah = a_desc | (a_hi0 + off);
+                    unsigned long long dal = a_desc | (a_lo0 + off);
+                    unsigned long long dbh =
+                        b_desc | (b_base + static_cast<uint32_t>(slot) * stage_units -
+                                  static_cast<uint32_t>(2 * c0));
+                    unsigned long long dbl = dbh + split_units;
+                    int c = c0;
+                    if (acc == 0) {
+                        mma_f16<kIdesc>(x_acc, dah, dbl, 0u);
+                        mma_f16_acc<kIdesc>(x_acc, dal, dbh);
                         acc = 1;
-                        ah -= 128;
-                        al -= 128;
-                        b -= 2;
+                        dah -= 128;
+                        dal -= 128;
+                        dbh -= 2;
+                        dbl -= 2;
+                        ++c;
+                    }
+                    for (; c < c1; ++c) {
+                        mma_f16_acc<kIdesc>(x_acc, dah, dbl);
+                        mma_f16_acc<kIdesc>(x_acc, dal, dbh);
+                        dah -= 128;
+                        dal -= 128;
+                        dbh -= 2;
+                        dbl -= 2;
                     }
                     if (c1 == P) {
                         mma_commit(smem_u32(&ctl.empty[slot]));
                     }
                 }
             }
-            if (!stop) {
-                mma_commit(smem_u32(&ctl.xfull));
+            if (stop) {
+                break;
+            }
+            mma_commit(smem_u32(&ctl.xfull));
+            // The strip of this capture is free once these MMAs complete.
+            if (k + 1 < my_items && capture_of(p, first_item + k + 1, cursor) != cursor) {
+                mma_commit(smem_u32(&ctl.strip_free));
             }
         }
         mma_commit(smem_u32(&ctl.teardown));
         mbar_wait_bounded(smem_u32(&ctl.teardown), 0, fault, kFaultTeardown, nullptr);
     }
 
+    // After a give-up, TMA copies may still be in flight: give them time to land (bounded).
+    if (threadIdx.x == 0 && *abort) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (globaltimer_ns() - t0 < 2000000ull) {
+        }
+    }
     fence_before();
     __syncthreads();
     fence_after();
@@ -621,8 +768,8 @@ void partition(const std::vector<BatchCap>& caps, int total_items, int parts, in
 {
     std::vector<double> prefix(total_items + 1, 0.0);
     for (const BatchCap& c : caps) {
-        // Measured on GB300: a tile costs about the same whatever its filter (the workers'
-        // conversion of its window bounds it), 5 % more at 9 chunks than at 2.
+        // Measured on GB300 (the single-capture kernel, same pipeline): a tile costs about the
+        // same whatever its filter from 63 to 1025 taps (15.2 and 15.7 us per tile and SM).
         const double per_tile = 1.0 + 0.007 * static_cast<double>(c.C + 1);
         for (int t = 0; t < c.tiles; ++t) {
             prefix[c.item0 + t + 1] = per_tile;
@@ -644,9 +791,9 @@ void partition(const std::vector<BatchCap>& caps, int total_items, int parts, in
 }
 
 template <int S>
-cudaError_t launch_batch(const BatchParams& params, int grid, int cmax, cudaStream_t stream)
+cudaError_t launch_batch(const BatchParams& params, int grid, const Layout& lay,
+                         cudaStream_t stream)
 {
-    const Layout lay = batch_layout(cmax, S);
     const uint32_t bytes = lay.bytes > 120u * 1024u ? lay.bytes : 120u * 1024u;
     cudaError_t err = cudaFuncSetAttribute(fir_batch_kernel<S>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -662,7 +809,8 @@ cudaError_t launch_batch(const BatchParams& params, int grid, int cmax, cudaStre
 
 bool fir_batch_supported(int num_taps)
 {
-    return fir_tc_supported(num_taps) && batch_layout((num_taps + kB - 2) / kB, 2).bytes <= 227u * 1024u;
+    return fir_tc_supported(num_taps) &&
+           batch_layout((num_taps + kB - 2) / kB, 2, 2).bytes <= 227u * 1024u;
 }
 
 cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cudaStream_t stream)
@@ -679,6 +827,8 @@ cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cuda
     // Captures the tensor-core kernel takes go into the work list; the rest (one tap, shorter
     // than a block, or taps beyond the shared-memory budget) run the plain kernel, in order.
     std::vector<BatchCap> caps;
+    std::vector<CUtensorMap> xmaps;
+    std::vector<CUtensorMap> smaps;
     for (int i = 0; i < count; ++i) {
         const rfx_fir_capture& c = captures[i];
         if (c.num_samples == 0) {
@@ -700,7 +850,22 @@ cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cuda
         b.C = (c.num_taps + kB - 2) / kB;
         const long long blocks = (c.num_samples + kB - 1) / kB;
         b.tiles = static_cast<int>((blocks + kNB - 1) / kNB);
+        // x as rows of 256 floats (full 128-sample blocks only); boxes of one K-step's 32
+        // floats by the window's rows, and of whole rows by a scan slice's rows.
+        const Geo g = geo_of(b.C, b.n);
+        CUtensorMap xm;
+        CUtensorMap sm;
+        err = encode_rows(&xm, c.x, 4, b.n / kB, 2 * kB, 32, static_cast<uint32_t>(g.rows));
+        if (err == cudaSuccess) {
+            err = encode_rows(&sm, c.x, 4, b.n / kB, 2 * kB, 2 * kB,
+                              static_cast<uint32_t>(g.srows));
+        }
+        if (err != cudaSuccess) {
+            return err;
+        }
         caps.push_back(b);
+        xmaps.push_back(xm);
+        smaps.push_back(sm);
     }
     for (std::size_t first = 0; first < caps.size(); first += kBatchCaps) {
         const std::size_t chunk = std::min<std::size_t>(kBatchCaps, caps.size() - first);
@@ -716,14 +881,28 @@ cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cuda
         BatchParams* params = new BatchParams{};
         for (std::size_t i = 0; i < chunk; ++i) {
             params->cap[i] = part[i];
+            params->xmap[i] = xmaps[first + i];
+            params->smap[i] = smaps[first + i];
         }
         params->count = static_cast<int>(chunk);
         params->cmax = cmax;
         partition(part, items, grid, params->cta_item);
-        if (batch_layout(cmax, 4).bytes <= 227u * 1024u) {
-            err = launch_batch<4>(*params, grid, cmax, stream);
-        } else {
-            err = launch_batch<2>(*params, grid, cmax, stream);
+        // The deep scan ring first, then the most operand stages that fit.
+        err = cudaErrorInvalidValue;
+        bool launched = false;
+        for (int sbufs = kScanBufsMax; sbufs >= 2 && !launched; sbufs -= 2) {
+            params->sbufs = sbufs;
+            for (int stages : {6, 4, 2}) {
+                const Layout lay = batch_layout(cmax, stages, sbufs);
+                if (lay.bytes > 227u * 1024u) {
+                    continue;
+                }
+                err = stages == 6   ? launch_batch<6>(*params, grid, lay, stream)
+                      : stages == 4 ? launch_batch<4>(*params, grid, lay, stream)
+                                    : launch_batch<2>(*params, grid, lay, stream);
+                launched = true;
+                break;
+            }
         }
         delete params;
         if (err != cudaSuccess) {
