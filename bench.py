@@ -227,7 +227,7 @@ def load_workload(name: str):
 # workload (dram__bytes_read.sum + dram__bytes_write.sum); writes still in L2 at the kernel's end
 # are not counted by that capture.
 NCU_TRAFFIC_BYTES = {
-    ("fir1025_tones", "tc_split"): 134.4e6 + 81.7e6,   # profiles/fir_tc_fir1025_full.md
+    ("fir1025_tones", "tc_split"): 134.5e6 + 80.1e6,   # profiles/fir_tc_fir1025_full.md
     ("fir63_white", "plain"): 134.2e6 + 89.1e6,        # profiles/fir_plain_fir63_full.md
     ("pfb64", "tc_split"): 134.4e6 + 83.2e6,           # profiles/chan_tc_pfb64_full.md
 }
