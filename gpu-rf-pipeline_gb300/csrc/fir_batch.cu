@@ -154,7 +154,13 @@ struct Ctrl {
     int abort;
     uint32_t pmax[2][kProducerWarps];
     uint32_t tmaxw[2][kProducerWarps];
-    int shift[4];                   // ex + eh of item k
+    // Item k's output description for the drain warps (slot k % 4, published with sready):
+    // its capture's output and length, its first output block, its H groups, ex + eh.
+    float2* item_y[4];
+    long long item_n[4];
+    long long item_block0[4];
+    int item_groups[4];
+    int shift[4];
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
@@ -330,12 +336,16 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
         };
         bool ok = true;
         int g = 0;   // H groups drained so far
-        int cursor = capture_of(p, first_item, 0);
         for (int k = 0; k < my_items && ok && !*abort; ++k) {
-            cursor = capture_of(p, first_item + k, cursor);
-            const BatchCap& c = p.cap[cursor];
-            const HGroups grp = h_groups(c.C + 1, S);
-            for (int gi = 0; gi < grp.per_tile; ++gi, ++g) {
+            // Item k's description (published with its scale before its first stage, so
+            // before any of its MMAs: no wait in practice). Read from shared memory rather
+            // than looked up in the capture table, which kept too many registers live.
+            if (!mbar_wait_bounded(smem_u32(&ctl.sready[k & 3]), (k >> 2) & 1, fault,
+                                   kFaultScale, abort)) {
+                break;
+            }
+            const int per_tile = *reinterpret_cast<volatile int*>(&ctl.item_groups[k & 3]);
+            for (int gi = 0; gi < per_tile; ++gi, ++g) {
                 if (!mbar_wait_bounded(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
                                        abort)) {
                     ok = false;
@@ -354,20 +364,19 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
             if (lane == 0) {
                 mbar_arrive(smem_u32(&ctl.xempty));
             }
-            if (!mbar_wait_bounded(smem_u32(&ctl.sready[k & 3]), (k >> 2) & 1, fault,
-                                   kFaultScale, abort)) {
-                break;
-            }
+            // Slot k % 4 is rewritten only for item k + 4, which needs this drain finished.
             const int shift = -*reinterpret_cast<volatile int*>(&ctl.shift[k & 3]);
             const float fa = exp2i(shift / 2);
             const float fb = exp2i(shift - shift / 2);
-            const long long jb0 =
-                static_cast<long long>(tile_in(c, k)) * kNB + slice * (kCols / 2);
+            float2* const y = *reinterpret_cast<float2* volatile*>(&ctl.item_y[k & 3]);
+            const long long n_out = *reinterpret_cast<volatile long long*>(&ctl.item_n[k & 3]);
+            const long long jb0 = *reinterpret_cast<volatile long long*>(&ctl.item_block0[k & 3]) +
+                                  slice * (kCols / 2);
 #pragma unroll
             for (int b = 0; b < kCols / 2; ++b) {
                 const long long o = (jb0 + b) * kB + r;
-                if (o < c.n) {
-                    c.y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
+                if (o < n_out) {
+                    y[o] = make_float2(acc[2 * b] * fa * fb, acc[2 * b + 1] * fa * fb);
                 }
                 acc[2 * b] = 0.0f;
                 acc[2 * b + 1] = 0.0f;
@@ -438,7 +447,12 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
                 ex_even = ex;
             }
             if (ptid == 0) {
+                const BatchCap& c = p.cap[ci];
                 ctl.shift[k & 3] = ex + eh;
+                ctl.item_y[k & 3] = c.y;
+                ctl.item_n[k & 3] = c.n;
+                ctl.item_block0[k & 3] = static_cast<long long>(tile_in(c, k)) * kNB;
+                ctl.item_groups[k & 3] = h_groups(c.C + 1, S).per_tile;
                 mbar_arrive(smem_u32(&ctl.sready[k & 3]));
             }
         };
