@@ -181,4 +181,25 @@ __device__ __forceinline__ void sts64(uint32_t addr, f32x2 v)
     asm volatile("st.shared.b64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
 }
 
+// ---- per-thread asynchronous copies (global -> shared) ----------------------------------
+
+// kBytes (4, 8 or 16) bytes from src to shared address dst; src_bytes = 0 reads nothing and
+// writes zeros.
+template <int kBytes>
+__device__ __forceinline__ void cp_async(uint32_t dst, const void* src, uint32_t src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(dst), "l"(src),
+                 "n"(kBytes), "r"(src_bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// Waits until at most kPending of this thread's committed copy groups are still in flight.
+template <int kPending>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory");
+}
+
 }  // namespace rfx

@@ -66,7 +66,8 @@ def test_64_channels_match_the_converted_input(fmt: str, impl: str, n: int, k: i
 
 @pytest.mark.parametrize("fmt", ["ci16", "ci8"])
 @pytest.mark.parametrize("n,k,m", [(100, 37, 4), (7, 63, 4), (12345, 100, 12), (5000, 333, 100),
-                                   (1 << 16, 32768, 1024), (999, 2000, 3)])
+                                   (1 << 16, 32768, 1024), (999, 2000, 3),
+                                   (1 << 18, 1024, 64), (1 << 20, 32768, 1024)])
 def test_plain_branch_sums_of_any_channel_count(fmt: str, n: int, k: int, m: int) -> None:
     c = stored(fmt, n, seed=3 * n + m)
     h = (np.random.default_rng(m).standard_normal(k) / np.sqrt(k)).astype(np.float32)

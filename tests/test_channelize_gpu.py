@@ -113,7 +113,18 @@ def test_bad_channel_count_is_an_error() -> None:
                                    # taps not a multiple of the channels, one tap per branch
                                    (5000, 333, 100), (20011, 6400, 200), (130, 4096, 64),
                                    (64 * 65 + 1, 64 * 40 + 7, 64), (70000, 128, 128),
-                                   (4097, 65, 65), (1 << 16, 32768, 1024), (200, 64, 64)])
+                                   (4097, 65, 65), (1 << 16, 32768, 1024), (200, 64, 64),
+                                   # the register-ring form (8, 16, 24 or 32 taps in every
+                                   # branch): many segments per branch at each ring depth,
+                                   # several segments per block (fewer than 128 channels),
+                                   # partial branch blocks, partial last steps, inputs within
+                                   # the tested first steps
+                                   (1 << 20, 24 * 64, 64), (300007, 8 * 48, 48),
+                                   (1 << 21, 1600, 100), (1 << 22, 32768, 1024),
+                                   (1 << 20, 32 * 256, 256), (777777, 24 * 33, 33),
+                                   (130, 8 * 16, 16), (5003, 16 * 64, 64),
+                                   # tap counts just off the ring form take the other kernel
+                                   (1 << 20, 16 * 256 - 3, 256), (777777, 20 * 33, 33)])
 def test_branch_sums_are_bit_exact(n: int, k: int, m: int) -> None:
     # rfx_channelize_branches against the reference's float32 branch arithmetic, bit for bit.
     rng = np.random.default_rng(7 * n + k + m)
