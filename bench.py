@@ -261,12 +261,18 @@ class Arm:
             self.outs = [torch.empty((f, m), dtype=torch.complex64, device=device)
                          for _ in range(2)]
             self.plan = rfx.ChanPlan(m, n, impl)
-            # plain: the branch kernel and cuFFT's inverse transform (counted as one of ours)
-            self.launches_per_step = 2 if impl == "plain" else 1
+            # plain: the branch kernel and cuFFT's inverse transform (counted as one of ours);
+            # tensor core: one fused kernel at 64 channels, branch kernel + DFT kernel at 1024.
+            # auto picks the tensor-core form at 64 channels, plain otherwise.
+            chan_tc = impl == "tc_split" or (impl == "auto" and m == 64)
+            self.launches_per_step = 1 if chan_tc and m == 64 else 2
         else:
             self.outs = [torch.empty_like(self.xs[0]) for _ in range(2)]
             self.launches_per_step = 1
-        uses_tc = impl == "tc_split" or (impl == "auto" and auto_picks_tc(w.taps.size, n))
+        if w.channels:
+            uses_tc = impl == "tc_split" or (impl == "auto" and w.channels == 64)
+        else:
+            uses_tc = impl == "tc_split" or (impl == "auto" and auto_picks_tc(w.taps.size, n))
         self.dtype = "f16x3->f32" if uses_tc else "f32"
 
     def launch(self, i: int) -> None:
@@ -728,9 +734,11 @@ def run_ours(args) -> None:
             useful = 4.0 * n * (-(-w.taps.size // w.channels))  # branch FIR flops
         else:
             useful = 4.0 * n * w.taps.size                       # FIR flops
-    # auto first where it is not simply the tensor-core form: it is the arm a user runs.
-    order = (["auto", "tc_split", "plain"] if w.captures or (not w.channels and w.taps.size < 160)
-             else ["tc_split", "plain"])
+    # auto first where it is not simply the tensor-core form: it is the arm a user runs (the
+    # short FIR, the batch, and the 1024-channel channelizer, whose plain form is faster).
+    auto_first = (w.captures or (not w.channels and w.taps.size < 160)
+                  or (w.channels and w.channels != 64))
+    order = ["auto", "tc_split", "plain"] if auto_first else ["tc_split", "plain"]
     arms, clocks = measure_arms(rfx, w, order, args, dist, device, sample_clocks=True)
     impl = next(iter(arms))
     prim = arms[impl]
@@ -765,6 +773,8 @@ def run_ours(args) -> None:
     kernel_impl = impl
     if impl == "auto" and not w.captures and not w.channels:
         kernel_impl = "tc_split" if auto_picks_tc(w.taps.size, n) else "plain"
+    if impl == "auto" and w.channels:
+        kernel_impl = "tc_split" if w.channels == 64 else "plain"
     traffic = NCU_TRAFFIC_BYTES.get((w.name, kernel_impl))
     if traffic is not None:
         roofline["traffic"] = traffic

@@ -195,7 +195,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
     const HGroups grp = h_groups(P, S);
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const uint32_t rank = cluster_rank();      // 0: issues the MMAs
+    const uint32_t rank = cluster_ctarank();      // 0: issues the MMAs
     const uint32_t sbase = smem_u32(smem);
     volatile int* abort = &ctl.abort;
     unsigned int* fault = &g_fault_fir_tc2;
@@ -302,7 +302,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
     fence_proxy_async_smem();
     fence_before();
     __syncthreads();
-    cluster_sync();   // both CTAs' barriers are initialized before any remote arrival
+    cluster_sync_all();   // both CTAs' barriers are initialized before any remote arrival
     fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
@@ -344,7 +344,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
         int g = 0;
         for (int k = 0; k < my_tiles && ok && !*abort; ++k) {
             for (int gi = 0; gi < grp.per_tile; ++gi, ++g) {
-                if (!mbar_wait_cluster(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
+                if (!mbar_wait_cluster_bounded(smem_u32(&ctl.pfull), g & 1, fault, kFaultAccumFull,
                                        abort)) {
                     ok = false;
                     break;
@@ -353,7 +353,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 arrive_lead(&ctl.pempty);
             }
             if (!ok ||
-                !mbar_wait_cluster(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull, abort)) {
+                !mbar_wait_cluster_bounded(smem_u32(&ctl.xfull), k & 1, fault, kFaultAccumFull, abort)) {
                 break;
             }
             drain(kXCol);
@@ -412,10 +412,10 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 tmax = max(tmax, ctl.pmax[rb][w]);
             }
             if (ptid == 0) {
-                st_cluster_u32(map_to(smem_u32(&ctl.peer_max[rb]), rank ^ 1u), tmax);
-                mbar_arrive_cluster(map_to(smem_u32(&ctl.xchg[rb]), rank ^ 1u));
+                st_cluster_u32(cluster_map(smem_u32(&ctl.peer_max[rb]), rank ^ 1u), tmax);
+                mbar_arrive_cluster(cluster_map(smem_u32(&ctl.xchg[rb]), rank ^ 1u));
             }
-            if (!mbar_wait_cluster(smem_u32(&ctl.xchg[rb]), (k >> 1) & 1, fault, kFaultScale,
+            if (!mbar_wait_cluster_bounded(smem_u32(&ctl.xchg[rb]), (k >> 1) & 1, fault, kFaultScale,
                                    abort)) {
                 return false;
             }
@@ -479,7 +479,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
             const float fb = exp2i(ex - ex / 2);
             const int slot = v % S;
             const int rslot = v % kRaw;
-            if (!mbar_wait_cluster(smem_u32(&ctl.empty[slot]), ((v / S) & 1) ^ 1, fault,
+            if (!mbar_wait_cluster_bounded(smem_u32(&ctl.empty[slot]), ((v / S) & 1) ^ 1, fault,
                                    kFaultStageEmpty, abort) ||
                 !mbar_wait_bounded(smem_u32(&ctl.raw_full[rslot]), (v / kRaw) & 1, fault,
                                    kFaultTileLoad, abort)) {
@@ -596,7 +596,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
         // completed phase into ONE release-arrive on the even CTA's barrier, instead of one
         // cross-CTA arrive per warp. Independent lanes, so no sequence waits behind another.
         if (lane == 0) {
-            const uint32_t lead = map_to(smem_u32(&ctl.full[0]), 0);
+            const uint32_t lead = cluster_map(smem_u32(&ctl.full[0]), 0);
             for (int v = 0; v < my_steps && !*abort; ++v) {
                 const int slot = v % S;
                 if (!mbar_wait_bounded(smem_u32(&ctl.full[slot]), (v / S) & 1, fault,
@@ -606,7 +606,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 mbar_arrive_cluster(lead + static_cast<uint32_t>(slot) * 8u);
             }
         } else if (lane == 1) {
-            const uint32_t lead = map_to(smem_u32(&ctl.pempty), 0);
+            const uint32_t lead = cluster_map(smem_u32(&ctl.pempty), 0);
             const int groups = my_tiles * grp.per_tile;
             for (int g = 0; g < groups && !*abort; ++g) {
                 if (!mbar_wait_bounded(smem_u32(&ctl.pempty), g & 1, fault, kFaultAccumEmpty,
@@ -616,7 +616,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 mbar_arrive_cluster(lead);
             }
         } else {
-            const uint32_t lead = map_to(smem_u32(&ctl.xempty), 0);
+            const uint32_t lead = cluster_map(smem_u32(&ctl.xempty), 0);
             for (int k = 0; k < my_tiles && !*abort; ++k) {
                 if (!mbar_wait_bounded(smem_u32(&ctl.xempty), k & 1, fault, kFaultAccumEmpty,
                                        abort)) {
@@ -650,7 +650,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 const int g = k * grp.per_tile + gi;
                 int st0, st1, c0, c1;
                 h_group_range(grp, P, gi, st0, st1, c0, c1);
-                if (!mbar_wait_cluster(smem_u32(&ctl.pempty), (g & 1) ^ 1, fault,
+                if (!mbar_wait_cluster_bounded(smem_u32(&ctl.pempty), (g & 1) ^ 1, fault,
                                        kFaultAccumEmpty, abort)) {
                     stop = true;
                     break;
@@ -661,7 +661,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                     const int u = k * kStagesPerTile + st / kStepsPerStage;
                     const int slot = u % S;
                     if (u >= ready) {
-                        if (!mbar_wait_cluster(smem_u32(&ctl.full[slot]), (u / S) & 1, fault,
+                        if (!mbar_wait_cluster_bounded(smem_u32(&ctl.full[slot]), (u / S) & 1, fault,
                                                kFaultStageFull, abort)) {
                             stop = true;
                             break;
@@ -685,7 +685,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 }
                 mma_commit_pair(smem_u32(&ctl.pfull));
                 if (gi == 0) {
-                    if (!mbar_wait_cluster(smem_u32(&ctl.xempty), (k & 1) ^ 1, fault,
+                    if (!mbar_wait_cluster_bounded(smem_u32(&ctl.xempty), (k & 1) ^ 1, fault,
                                            kFaultAccumEmpty, abort)) {
                         stop = true;
                         break;
@@ -721,7 +721,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
         }
         // Every MMA issued has completed before tensor memory is released.
         mma_commit_pair(smem_u32(&ctl.teardown));
-        mbar_wait_cluster(smem_u32(&ctl.teardown), 0, fault, kFaultTeardown, nullptr);
+        mbar_wait_cluster_bounded(smem_u32(&ctl.teardown), 0, fault, kFaultTeardown, nullptr);
     }
 
     // After a give-up, TMA copies may still be in flight: give them time to land (bounded).
@@ -732,7 +732,7 @@ fir_tc2_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
     }
     fence_before();
     __syncthreads();
-    cluster_sync();   // the pair's MMAs, remote arrivals and copies are all done
+    cluster_sync_all();   // the pair's MMAs, remote arrivals and copies are all done
     fence_after();
     if (warp == kMmaWarp) {
         tmem_dealloc_pair(tmem, kTmemCols);

@@ -21,6 +21,7 @@ enum FaultCode : unsigned int {
     kFaultAccumEmpty = 1u << 4,   // MMA issuer waited too long for a drained accumulator
     kFaultScale = 1u << 5,        // epilogue waited too long for a tile scale
     kFaultTeardown = 1u << 6,     // final MMA commit never arrived
+    kFaultPeer = 1u << 7,         // a CTA of the cluster never handed over its part
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -100,6 +101,84 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
     }
 }
 
+// ---- thread-block clusters -------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t cluster_ctarank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// The shared::cluster address of this CTA's shared address `addr` in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t cluster_map(uint32_t addr, uint32_t rank)
+{
+    uint32_t d;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(addr), "r"(rank));
+    return d;
+}
+
+__device__ __forceinline__ void st_cluster_u32(uint32_t addr, uint32_t v)
+{
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+// Arrives on a barrier in another CTA of the cluster (shared::cluster address), releasing this
+// thread's earlier writes at cluster scope.
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// mbar_wait_bounded for a barrier that threads of other CTAs arrive on (acquire at cluster
+// scope, so their writes before the arrival are visible).
+__device__ __forceinline__ bool mbar_wait_cluster_bounded(uint32_t bar, uint32_t parity,
+                                                          unsigned int* fault, unsigned int code,
+                                                          volatile int* abort)
+{
+    if (mbar_try_wait_cluster(bar, parity)) {
+        return true;
+    }
+    const unsigned long long start = globaltimer_ns();
+    while (true) {
+        if (mbar_try_wait_cluster(bar, parity)) {
+            return true;
+        }
+        if (abort != nullptr && *abort) {
+            return false;
+        }
+        if (globaltimer_ns() - start > kWaitLimitNs) {
+            atomicOr(fault, code);
+            if (abort != nullptr) {
+                *abort = 1;
+            }
+            return false;
+        }
+    }
+}
+
+// Every thread of every CTA of the cluster arrives, then waits for all (the hardware barrier;
+// reached once after set-up and once before exit by all threads, never skipped).
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release;\n\t"
+                 "barrier.cluster.wait.acquire;" ::: "memory");
+}
+
 // ---- bulk copies (TMA engine, no tensor map) -------------------------------------------
 
 // global -> shared, completion counted on `bar` in bytes. dst/src 16-byte aligned, bytes % 16 == 0.
@@ -121,6 +200,21 @@ __device__ __forceinline__ void bulk_s2g(void* dst, uint32_t src, uint32_t bytes
 }
 
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;"); }
+
+// Waits until at most kPending of this thread's committed shared->global bulk copy groups are
+// unfinished (reads and writes); the hardware completes them, no software spin.
+template <int kPending>
+__device__ __forceinline__ void bulk_wait()
+{
+    asm volatile("cp.async.bulk.wait_group %0;" ::"n"(kPending) : "memory");
+}
+
+// Orders this thread's completed bulk (async-proxy) writes to global memory before its later
+// generic-proxy operations, such as a releasing mbarrier arrival.
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
 
 // Waits until every committed shared->global copy of this thread has finished READING shared
 // memory (the hardware completes it; no unbounded software spin).

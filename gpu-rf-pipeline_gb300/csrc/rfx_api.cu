@@ -6,6 +6,7 @@
 
 #include "chan_plain.cuh"
 #include "chan_tc.cuh"
+#include "chan_wide.cuh"
 #include "fir_plain.cuh"
 #include "fir_tc.cuh"
 #include "fir_tc2.cuh"
@@ -174,7 +175,8 @@ struct rfx_chan_plan {
     cufftHandle fft;
     bool has_fft;
     void* twiddles;       // tensor core: the DFT operand image, built once in FP64
-    void* scratch;        // plain: channel outputs before their magnitude (first such call)
+    void* scratch;        // plain: channel outputs before their magnitude (first such call);
+                          // tensor core, 1024 channels: the branch sums (made with the plan)
 };
 
 extern "C" {
@@ -216,6 +218,11 @@ int rfx_device_fault(unsigned int* code)
     part = 0;
     if ((err = rfx::chan_tc_take_fault(&part)) != cudaSuccess) {
         return cuda_fail(err, "chan_tc fault word");
+    }
+    total |= part;
+    part = 0;
+    if ((err = rfx::chan_wide_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "chan_wide fault word");
     }
     total |= part;
     *code = total;
@@ -427,21 +434,32 @@ int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_p
     auto* p = new rfx_chan_plan{impl, channels, rfx_channelize_frames(max_samples, channels), 0,
                                 false, nullptr, nullptr};
     if (impl == RFX_CHAN_TC) {
-        if (!rfx::chan_tc_supported(channels, 1)) {
+        const bool wide = rfx::chan_wide_supported(channels);
+        if (!wide && !rfx::chan_tc_supported(channels, 1)) {
             delete p;
-            return fail(RFX_ERR_CAPACITY, "channelize: the tensor-core form takes 64 channels, "
-                                          "not %d",
+            return fail(RFX_ERR_CAPACITY, "channelize: the tensor-core form takes 64 or 1024 "
+                                          "channels, not %d",
                         channels);
         }
-        cudaError_t err = cudaMalloc(&p->twiddles, rfx::chan_tc_twiddle_bytes());
+        cudaError_t err = cudaMalloc(&p->twiddles, wide ? rfx::chan_wide_image_bytes()
+                                                        : rfx::chan_tc_twiddle_bytes());
         if (err == cudaSuccess) {
-            err = rfx::chan_tc_build_twiddles(p->twiddles, nullptr);
+            err = wide ? rfx::chan_wide_build_image(p->twiddles, nullptr)
+                       : rfx::chan_tc_build_twiddles(p->twiddles, nullptr);
+        }
+        if (err == cudaSuccess && wide && p->frames > 0) {
+            // The branch sums between the two kernels of the 1024-channel form.
+            err = cudaMalloc(&p->scratch, static_cast<size_t>(p->frames) * channels * 8u);
+            if (err != cudaSuccess) {
+                p->scratch = nullptr;
+            }
         }
         if (err == cudaSuccess) {
             err = cudaDeviceSynchronize();
         }
         if (err != cudaSuccess) {
             cudaFree(p->twiddles);
+            cudaFree(p->scratch);
             delete p;
             return cuda_fail(err, "channelizer twiddles");
         }
@@ -565,6 +583,12 @@ int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void*
             return fail(RFX_ERR_INVALID, "channelize: plan made for up to %lld frames, call has "
                                          "%lld",
                         static_cast<long long>(plan->frames), static_cast<long long>(frames));
+        }
+        if (rfx::chan_wide_supported(plan->channels)) {
+            const cudaError_t err = rfx::chan_wide_launch(x, taps, plan->twiddles, plan->scratch,
+                                                          out, num_samples, num_taps, stream,
+                                                          magnitude, format);
+            return err == cudaSuccess ? RFX_OK : cuda_fail(err, "chan_wide_launch");
         }
         if (!rfx::chan_tc_supported(plan->channels, num_taps)) {
             return fail(RFX_ERR_CAPACITY, "channelize: %d taps exceed the tensor-core form's "

@@ -91,6 +91,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&t)[16])
         : "r"(taddr));
 }
 
+// 8 consecutive 32-bit TMEM columns of this thread's lane (32x32b shape); tmem_wait_ld after.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&t)[8])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]),
+                   "=r"(t[6]), "=r"(t[7])
+                 : "r"(taddr));
+}
+
 // 16 lanes x 256 bits, four times along the columns: for 8-column group j (registers 4j .. 4j+3)
 // thread t holds (lane t/4: columns 2 (t%4), +1) and (lane t/4 + 8: the same columns) of the 16
 // lanes starting at taddr's lane.

@@ -60,8 +60,9 @@ typedef enum rfx_chan_impl {
     /* FP32 branch-sum kernel (bit-identical to the project's channelize_branch_kernel) followed
      * by cuFFT's batched in-place inverse transform, as the project computes it. */
     RFX_CHAN_PLAIN = 0,
-    /* One fused tensor-core kernel: FP32 branch sums into shared memory, then the M-point DFT as
-     * a split-FP16 GEMM on tcgen05 (M = 64 here; M = 1024 as a 32 x 32 factorization). */
+    /* The M-point DFT as a split-FP16 complex GEMM on tcgen05. M = 64: one fused kernel (FP32
+     * branch sums into shared memory, then the GEMM). M = 1024: the plain form's FP32 branch
+     * sums, then the DFT factored 32 x 32 into two GEMMs with an FP32 twiddle between them. */
     RFX_CHAN_TC = 1,
     RFX_CHAN_AUTO = 2
 } rfx_chan_impl;
@@ -158,7 +159,10 @@ typedef struct rfx_chan_plan rfx_chan_plan;
 
 /* Setup for channelizing up to `max_samples` samples into `channels` channels: for
  * RFX_CHAN_PLAIN, the batched inverse cuFFT plan of `channels` points (the project's FftPlan,
- * src/fft_plan.hpp:15-22). Allocates; call outside timed regions. */
+ * src/fft_plan.hpp:15-22); for RFX_CHAN_TC (64 or 1024 channels, RFX_ERR_CAPACITY otherwise),
+ * the DFT operand built in FP64 and, at 1024 channels, a buffer for the branch sums
+ * (max_samples / 1024 frames x 8 KB). RFX_CHAN_AUTO picks RFX_CHAN_TC for 64 channels.
+ * Allocates; call outside timed regions. */
 int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_plan** plan);
 int rfx_chan_plan_destroy(rfx_chan_plan* plan);
 
