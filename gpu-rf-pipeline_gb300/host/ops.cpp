@@ -367,7 +367,8 @@ const std::vector<Impl<ChanFn>>& channelize_impls()
 {
     static const std::vector<Impl<ChanFn>> impls = {
         {"plain", "FP32 branch sums + cuFFT batched inverse FFT", channelize_plain},
-        {"tc_split", "fused: FP32 branch sums + DFT as a split-FP16 tcgen05 GEMM (64 ch)",
+        {"tc_split", "DFT as a split-FP16 tcgen05 GEMM: fused with the FP32 branch sums (64 ch); "
+                     "32 x 32 factored after them (1024 ch)",
          channelize_tc},
         {"auto", "tc_split for 64 channels, plain otherwise", channelize_auto},
     };
