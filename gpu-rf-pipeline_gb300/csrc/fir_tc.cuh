@@ -41,7 +41,7 @@ long long fir_tc_tile_outputs_format(int format, int num_taps, long long n, TcCo
 long long fir_tc_tile_outputs(int num_taps, long long n, TcConfig config);
 
 // Per-capture-taps batch: tensor core (or auto) = one persistent launch of fir_batch.cu per
-// 192 captures; plain = one launch per capture.
+// 96 captures; plain = one launch per capture.
 cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
                              cudaStream_t stream);
 cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cudaStream_t stream);
