@@ -13,7 +13,7 @@ Writes, next to this script:
 * ``reference_outputs.npz`` — tools/reference.py's outputs for the FIR and channelizer cases
   that the project's own tests use (tests/test_pipeline.py:120-135 and :367-383,
   tests/test_reference.py:115-121 and :208-223), for a few extra edge cases, and for prefixes
-  of two benchmark workloads. Long outputs are stored as every element of a deterministic
+  of three benchmark workloads. Long outputs are stored as every element of a deterministic
   index set (the first 1100 and then every 29th) plus three whole-vector checksums (sum,
   energy and a seeded weighted sum), so the file stays small while every element is pinned.
 """
@@ -149,6 +149,10 @@ def main() -> None:
     record("bench/pfb64",
            reference.channelize(w.x.astype(np.complex128), w.taps.astype(np.float64), 64),
            {"op": "channelize", "workload": "pfb64", "n": 1 << 16, "channels": 64})
+    w = signals.channelizer1024(40 * 1024)
+    record("bench/pfb1024",
+           reference.channelize(w.x.astype(np.complex128), w.taps.astype(np.float64), 1024),
+           {"op": "channelize", "workload": "pfb1024", "n": 40 * 1024, "channels": 1024})
 
     out["__cases__"] = np.array(json.dumps(cases))
     np.savez_compressed(HERE / "reference_outputs.npz", **out)

@@ -79,8 +79,9 @@ def case_inputs(case: dict) -> tuple[np.ndarray, np.ndarray]:
         return (signals.fixture_signal(case["signal"]).astype(np.complex128),
                 signals.fixture_taps(case["taps"]).astype(np.float64))
     if "workload" in case:
-        w = (signals.long_fir if case["workload"] == "fir1025" else signals.channelizer64)(
-            case["n"])
+        make = {"fir1025": signals.long_fir, "pfb64": signals.channelizer64,
+                "pfb1024": signals.channelizer1024}[case["workload"]]
+        w = make(case["n"])
         return w.x.astype(np.complex128), w.taps.astype(np.float64)
     if case["op"] == "fir":
         x = random_complex(case["x_seed"], case["n"])
