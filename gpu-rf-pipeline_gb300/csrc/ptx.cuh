@@ -201,21 +201,6 @@ __device__ __forceinline__ void bulk_s2g(void* dst, uint32_t src, uint32_t bytes
 
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;"); }
 
-// Waits until at most kPending of this thread's committed shared->global bulk copy groups are
-// unfinished (reads and writes); the hardware completes them, no software spin.
-template <int kPending>
-__device__ __forceinline__ void bulk_wait()
-{
-    asm volatile("cp.async.bulk.wait_group %0;" ::"n"(kPending) : "memory");
-}
-
-// Orders this thread's completed bulk (async-proxy) writes to global memory before its later
-// generic-proxy operations, such as a releasing mbarrier arrival.
-__device__ __forceinline__ void fence_proxy_async_global()
-{
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-}
-
 // Waits until every committed shared->global copy of this thread has finished READING shared
 // memory (the hardware completes it; no unbounded software spin).
 __device__ __forceinline__ void bulk_wait_read_all()
