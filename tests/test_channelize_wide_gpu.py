@@ -120,3 +120,11 @@ def test_wide_dft_of_the_bit_exact_branch_sums() -> None:
     u = orc.channelize_branch_f32_seq(w.x, w.taps, M).astype(np.complex128)
     ref = np.fft.ifft(u, axis=1) * M
     assert orc.normwise_error(z, ref) <= CHAN_TC_NORMWISE
+
+
+def test_wide_host_path() -> None:
+    # rfx_channelize_host (host buffers in and out, the project's channelize_cuda contract).
+    w = signals.channelizer1024(1 << 18)
+    z, bench = rfx.channelize_host("tc_split", w.x, w.taps, M, warmup=1, runs=2)
+    assert orc.normwise_error(z, orc.channelize_fast(w.x, w.taps, M)) <= CHAN_TC_NORMWISE
+    assert bench.kernel_ms_mean > 0

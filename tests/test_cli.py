@@ -252,6 +252,24 @@ def test_channelize_tc_on_sixty_four_channels(fixtures: Path, tmp_path: Path) ->
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("output", ["complex", "magnitude"])
+def test_channelize_tc_on_1024_channels(tmp_path: Path, output: str) -> None:
+    # The wideband form (branch sums, then the 32 x 32 factored tensor-core DFT) through the CLI.
+    w = signals.channelizer1024(1 << 18)
+    w.x.astype("<c8").tofile(tmp_path / "x.cf32")
+    w.taps.astype("<f4").tofile(tmp_path / "h.f32")
+    out = tmp_path / "ch.out"
+    rfgpu("channelize", "--in", tmp_path / "x.cf32", "--taps", tmp_path / "h.f32",
+          "--channels", 1024, "--out", out, "--impl", "tc_split", "--output", output)
+    ref = orc.channelize_fast(w.x, w.taps, 1024)
+    if output == "complex":
+        assert orc.normwise_error(read_cf32(out).reshape(-1, 1024), ref) <= 2e-6
+    else:
+        mag = np.fromfile(out, dtype="<f4").reshape(-1, 1024)
+        assert orc.normwise_error(mag, np.abs(ref)) <= 2e-6
+
+
+@pytest.mark.gpu
 def test_channelize_puts_a_tone_in_its_channel(fixtures: Path, tmp_path: Path) -> None:
     n = np.arange(16 * 512)
     signals.to_cf32(np.exp(2j * np.pi * 3 * n / 16)).astype("<c8").tofile(tmp_path / "x.cf32")
