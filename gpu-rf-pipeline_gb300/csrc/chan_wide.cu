@@ -33,7 +33,8 @@
 // memory and 128 TMEM columns each) and interleave their groups. Measured at 2^16 frames: 244 us
 // per launch (DRAM 52 %, tensor pipe 18 %), and within 1 % of that with u loaded straight into
 // registers (four CTAs an SM), two warps per frame, padded operand planes, or one accumulator
-// per split product: the cost per group lies in the MMA path, not in the warps' work.
+// per split product; with the MMAs left out (a timing copy) the branch + DFT step still took
+// 418 us against 455 us, so the MMAs are not what bounds it either.
 //
 // Measured and not kept: one fused kernel on clusters of four CTAs (each CTA computing the
 // branch sums of 256 branches and the DFT of every fourth frame group, the sums exchanged
