@@ -261,11 +261,7 @@ class Arm:
             self.outs = [torch.empty((f, m), dtype=torch.complex64, device=device)
                          for _ in range(2)]
             self.plan = rfx.ChanPlan(m, n, impl)
-            # plain: the branch kernel and cuFFT's inverse transform (counted as one of ours);
-            # tensor core: one fused kernel at 64 channels, branch kernel + DFT kernel at 1024.
-            # auto picks the tensor-core form at 64 channels, plain otherwise.
-            chan_tc = impl == "tc_split" or (impl == "auto" and m == 64)
-            self.launches_per_step = 1 if chan_tc and m == 64 else 2
+            self.launches_per_step = chan_launches(m, impl)
         else:
             self.outs = [torch.empty_like(self.xs[0]) for _ in range(2)]
             self.launches_per_step = 1
@@ -393,6 +389,23 @@ class BatchArm:
 def auto_picks_tc(num_taps: int, n: int) -> bool:
     """The library's built-in auto rule (tuning.cu): tensor core from 160 taps and 2^16 samples."""
     return num_taps >= 160 and n >= (1 << 16)
+
+
+def chan_launches(channels: int, impl: str) -> int:
+    """Kernel launches per channelizer step: plain = branch sums + cuFFT's inverse (counted as
+    one of ours); tensor core = one fused kernel at 64 channels, branch sums + DFT kernel at
+    1024; auto = the tensor-core form at 64 channels, plain otherwise."""
+    tc = impl == "tc_split" or (impl == "auto" and channels == 64)
+    return 1 if tc and channels == 64 else 2
+
+
+def arm_order(w) -> list[str]:
+    """Arms to time, the headline first: auto first where it is not simply the tensor-core
+    form (the short FIR, the batch, and the channelizer above 64 channels, whose plain form is
+    faster) — it is the arm a user runs."""
+    auto_first = bool(w.captures or (not w.channels and w.taps.size < 160)
+                      or (w.channels and w.channels != 64))
+    return ["auto", "tc_split", "plain"] if auto_first else ["tc_split", "plain"]
 
 
 def make_arm(rfx, w, impl: str, device):
@@ -734,11 +747,7 @@ def run_ours(args) -> None:
             useful = 4.0 * n * (-(-w.taps.size // w.channels))  # branch FIR flops
         else:
             useful = 4.0 * n * w.taps.size                       # FIR flops
-    # auto first where it is not simply the tensor-core form: it is the arm a user runs (the
-    # short FIR, the batch, and the 1024-channel channelizer, whose plain form is faster).
-    auto_first = (w.captures or (not w.channels and w.taps.size < 160)
-                  or (w.channels and w.channels != 64))
-    order = ["auto", "tc_split", "plain"] if auto_first else ["tc_split", "plain"]
+    order = arm_order(w)
     arms, clocks = measure_arms(rfx, w, order, args, dist, device, sample_clocks=True)
     impl = next(iter(arms))
     prim = arms[impl]

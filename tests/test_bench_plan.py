@@ -1,0 +1,50 @@
+"""bench.py's arm plan on CPU: which implementations each workload times (the headline first)
+and how many kernel launches a step counts (the JSON line's `gpu_launches`), for every
+workload shape, without a GPU."""
+from __future__ import annotations
+
+import importlib.util
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from rfx.signals import Workload
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def bench():
+    spec = importlib.util.spec_from_file_location("bench_under_test", ROOT / "bench.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload(taps: int, channels: int = 0, captures: int = 0) -> Workload:
+    x = np.zeros(16, np.complex64)
+    h = np.zeros(taps, np.float32)
+    return Workload("w", x, h, channels=channels, captures=[(x, h)] * captures)
+
+
+@pytest.mark.parametrize("w,first", [
+    (workload(1025), "tc_split"),                 # long FIR: the tensor-core form leads
+    (workload(63), "auto"),                       # short FIR: auto (= plain) leads
+    (workload(1024, channels=64), "tc_split"),    # 64-channel channelizer
+    (workload(32768, channels=1024), "auto"),     # 1024 channels: auto (= plain) leads
+    (workload(1025, captures=3), "auto"),         # the batch
+])
+def test_headline_arm(bench, w: Workload, first: str) -> None:
+    order = bench.arm_order(w)
+    assert order[0] == first
+    assert "tc_split" in order and "plain" in order
+
+
+@pytest.mark.parametrize("channels,impl,launches", [
+    (64, "tc_split", 1), (64, "auto", 1), (64, "plain", 2),
+    (1024, "tc_split", 2), (1024, "auto", 2), (1024, "plain", 2),
+    (16, "auto", 2), (16, "plain", 2),
+])
+def test_channelizer_launches_per_step(bench, channels: int, impl: str, launches: int) -> None:
+    assert bench.chan_launches(channels, impl) == launches
