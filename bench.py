@@ -2,26 +2,30 @@
 """Benchmark of the complex-baseband filtering path on GB300 — one JSON line on stdout.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload fir1025|fir63|pfb64|pfb1024|batch256]
+                    [--workload fir1025|fir63|pfb64|pfb1024|batch256] [--no-secondary]
 
-A step is one pass of the hot path over one batch of synthetic input: by default the long FIR
-(2^24 cf32 samples = 8 tones over 60 dB + AWGN at 10 dB SNR, 1025 Kaiser-windowed-sinc taps),
-the workload the headline metric (Msamples/s, FIR 1025 taps) is quoted on. The other
-workloads: fir63 (2^24 samples, 63 taps), pfb64 (64-channel channelizer, 2^24 samples, 1024
-taps), pfb1024 (1024-channel channelizer, 2^26 samples, 32768 taps), batch256 (256 captures of
-2^12 .. 2^22 samples, each with its own 31 .. 1025 taps).
+A step is one pass of the hot path over one batch of synthetic input. The headline workload is
+the long FIR (2^24 cf32 samples = 8 tones over 60 dB + AWGN at 10 dB SNR, 1025 Kaiser-windowed-
+sinc taps), the one the headline metric (Msamples/s, FIR 1025 taps) is quoted on; by default
+the line also carries, under "workloads", the same figures for the other four: fir63 (2^24
+samples, 63 taps), pfb64 (64-channel channelizer, 2^24 samples, 1024 taps), pfb1024
+(1024-channel channelizer, 2^26 samples, 32768 taps) and batch256 (256 captures of 2^12 .. 2^22
+samples, each with its own 31 .. 1025 taps). --workload W reports W alone as the headline.
 
-Timing: W untimed steps, then exactly K steps between a barrier + device synchronize on both
-sides, measured with CUDA events on the launching stream; max over ranks. Two input/output
-buffer pairs alternate, so each step touches 536 MB (more than the 129 MB L2) and nothing is
-served from L2 across steps. `value` = all ranks' samples / time; `e2e` = the same metric from
-host buffers through the library's host-facing calls: the FIRs through rfx_fir_stream (the
-project's streaming path: pinned capture, chunks whose upload, kernel and download overlap),
-the channelizers through rfx_channelize_host (upload + compute + download), the batch as one
-upload, the batch launch and one download per step.
+Timing: per workload, every implementation (arm) gets W untimed steps, then R rounds; a round
+times exactly K steps of each arm in turn, between a barrier + device synchronize on both
+sides, with CUDA events on the launching stream (max over ranks). Each arm's figure is the
+median over the rounds; R >= 5 and large enough that the headline arm runs >= 0.5 s in total
+(so the clock sampler sees the load). Two input/output buffer pairs alternate, so each step
+touches more than the 129 MB L2 and nothing is served from L2 across steps. `value` = all
+ranks' samples / time. Errors are over the whole output against the float64 oracle. `e2e` = the
+same metric from host buffers through the library's host-facing calls: the FIRs through
+rfx_fir_stream (pinned capture, chunks whose upload, kernel and download overlap), the
+channelizers through rfx_channelize_host, the batch as one upload, the batch launch and one
+download per step.
 
---impl reference: the oracle's float64 restatement of the project's tools/reference.py FIR,
-threaded over every host core, on a bounded sample of the same workload (rank 0 only).
+--impl reference: the project's CPU implementation of the path in float64 (the oracle's threaded
+C restatement over every host core) on a bounded prefix of the same workload (rank 0 only).
 
 Under torchrun with N > 1 every rank runs its own replica of the workload (the path needs no
 exchange between GPUs): weak scaling.
@@ -223,16 +227,6 @@ def load_workload(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of it on the
-# workload (dram__bytes_read.sum + dram__bytes_write.sum); writes still in L2 at the kernel's end
-# are not counted by that capture.
-NCU_TRAFFIC_BYTES = {
-    ("fir1025_tones", "tc_split"): 134.5e6 + 80.1e6,   # profiles/fir_tc_fir1025_full.md
-    ("fir63_white", "plain"): 134.2e6 + 89.1e6,        # profiles/fir_plain_fir63_full.md
-    ("pfb64", "tc_split"): 134.4e6 + 83.2e6,           # profiles/chan_tc_pfb64_full.md
-}
-
-
 def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -245,7 +239,8 @@ def peaks() -> dict:
 
 
 class Arm:
-    """One implementation on one workload: its device buffers and one step's launch."""
+    """One implementation on one single-capture workload: its device buffers and one step's
+    launch."""
 
     def __init__(self, rfx, w, impl: str, device) -> None:
         import torch
@@ -262,14 +257,13 @@ class Arm:
                          for _ in range(2)]
             self.plan = rfx.ChanPlan(m, n, impl)
             self.launches_per_step = chan_launches(m, impl)
+            uses_tc = impl == "tc_split" or (impl == "auto" and w.channels == 64)
+            self.kernel = "tc_split" if uses_tc else "plain"
         else:
             self.outs = [torch.empty_like(self.xs[0]) for _ in range(2)]
             self.launches_per_step = 1
-        if w.channels:
-            uses_tc = impl == "tc_split" or (impl == "auto" and w.channels == 64)
-        else:
-            uses_tc = impl == "tc_split" or (impl == "auto" and auto_picks_tc(w.taps.size, n))
-        self.dtype = "f16x3->f32" if uses_tc else "f32"
+            self.kernel = rfx.fir_impl_used(impl, w.taps.size, n)
+        self.dtype = "f16x3->f32" if self.kernel == "tc_split" else "f32"
 
     def launch(self, i: int) -> None:
         if self.w.channels:
@@ -277,22 +271,26 @@ class Arm:
         else:
             self.rfx.fir_launch(self.impl, self.xs[i % 2], self.h, self.outs[i % 2])
 
-    def error(self) -> float:
-        """Normwise error of this arm's output against the float64 oracle, first 2^18 samples."""
+    def error(self, ref) -> dict:
+        """This arm's whole output against the float64 oracle's (`ref`): the normwise error
+        max|y - ref| / max|ref|, per channel for a channelizer, and for the plain FIR whether
+        every output equals the float32 chain of the project's kernels bit for bit."""
         import torch
         from oracle import rf_oracle as orc
 
         w = self.w
         self.launch(0)
         torch.cuda.synchronize()
-        check_n = min(self.n, 1 << 18)
+        got = self.outs[0].cpu().numpy()
+        out = {"max_rel_err_vs_f64": orc.normwise_error(got, ref),
+               "checked": f"whole output ({got.size} values)"}
         if w.channels:
-            frames = check_n // w.channels
-            got = self.outs[0][:frames].cpu().numpy()
-            ref = orc.channelize_fast(w.x[: frames * w.channels], w.taps, w.channels)
-            return orc.normwise_error(got, ref)
-        got = self.outs[0][:check_n].cpu().numpy()
-        return orc.normwise_error(got, orc.fir_fast(w.x[:check_n], w.taps))
+            out["max_channel_rel_err_vs_f64"] = float(orc.per_channel_error(got, ref).max())
+        elif self.kernel == "plain":
+            chain = orc.fir_f32_seq(w.x, w.taps)
+            out["bit_exact_vs_f32_chain"] = bool(np.array_equal(got.view(np.uint32),
+                                                                chain.view(np.uint32)))
+        return out
 
     def release(self) -> None:
         self.xs = self.outs = None
@@ -302,9 +300,8 @@ class Arm:
 
 class BatchArm:
     """The batched workload: every capture with its own taps, device-resident; one step is
-    one rfx_fir_batch_launch over all captures (tensor core: one persistent launch per 96
-    captures, replayed from a CUDA graph captured once; plain: one launch per capture, as the
-    project runs a batch)."""
+    one rfx_fir_batch_launch over all captures (tensor core and auto: replayed from a CUDA graph
+    captured once; plain: one launch per capture, as the project runs a batch)."""
 
     def __init__(self, rfx, w, impl: str, device) -> None:
         import torch
@@ -330,18 +327,14 @@ class BatchArm:
             self.arr[i] = rfx.FirCapture(xd.data_ptr(), yd.data_ptr(), hd.data_ptr(), xd.numel(),
                                          hd.numel(), 0)
         self.impl_v = rfx.parse_fir_impl(impl)
-        count = len(self.caps)
-        sizes = [(int(x.size), int(h.size)) for x, h in w.captures if x.size]
-        if impl == "tc_split":
-            self.launches_per_step = -(-count // 96)
-            self.dtype = "f16x3->f32"
-        elif impl == "auto":
-            tc = sum(1 for m, k in sizes if auto_picks_tc(k, m))
-            self.launches_per_step = -(-(len(sizes) - tc) // 256) + -(-tc // 96)
-            self.dtype = "f16x3->f32 (taps >= 160) + f32"
-        else:
-            self.launches_per_step = len(sizes)
-            self.dtype = "f32"
+        self.kernels = [rfx.fir_impl_used(impl, h.size, x.size, batch=True)
+                        for x, h in w.captures]
+        self.launches_per_step = batch_launches(impl, [(int(x.size), int(h.size))
+                                                       for x, h in w.captures], self.kernels)
+        tc = sum(1 for k in self.kernels if k == "tc_split")
+        self.dtype = ("f32" if tc == 0 else "f16x3->f32" if tc == len(self.kernels)
+                      else "f16x3->f32 (tensor-core captures) + f32")
+        self.kernel = "tc_split" if impl == "tc_split" else "plain" if impl == "plain" else "mixed"
         self.graph = None
         if impl != "plain":
             # One step captured into a CUDA graph (after a warm-up launch that sets the kernels'
@@ -367,20 +360,25 @@ class BatchArm:
             self.rfx._check(self.rfx.load().rfx_fir_batch_launch(self.impl_v, self.arr,
                                                                   len(self.caps), None))
 
-    def error(self) -> float:
-        """Largest normwise error against the float64 oracle over every 8th capture (first 2^16
-        samples of each)."""
+    def error(self, ref=None) -> dict:
+        """Every capture's whole output: the largest normwise error against the float64 oracle
+        over the captures, and whether the captures the plain kernel runs equal the float32
+        chain of the project's kernels bit for bit."""
         import torch
         from oracle import rf_oracle as orc
 
         self.launch(0)
         torch.cuda.synchronize()
-        worst = 0.0
-        for (x, h), (_, yd, _) in list(zip(self.w.captures, self.caps))[::8]:
-            m = min(x.size, 1 << 16)
-            got = yd[:m].cpu().numpy()
-            worst = max(worst, orc.normwise_error(got, orc.fir_fast(x[:m], h)))
-        return worst
+        y_all = self.Y.cpu().numpy()
+        worst, exact = 0.0, True
+        for (x, h), o, kernel in zip(self.w.captures, self.offsets, self.kernels):
+            got = y_all[o:o + x.size]
+            worst = max(worst, orc.normwise_error(got, orc.fir_fast(x, h)))
+            if kernel == "plain":
+                exact &= bool(np.array_equal(got.view(np.uint32),
+                                             orc.fir_f32_seq(x, h).view(np.uint32)))
+        return {"max_rel_err_vs_f64": worst, "bit_exact_vs_f32_chain": exact,
+                "checked": f"every capture, whole output ({self.n} values)"}
 
     def release(self) -> None:
         self.caps = self.arr = self.X = self.Y = self.graph = None
@@ -399,6 +397,20 @@ def chan_launches(channels: int, impl: str) -> int:
     return 1 if tc and channels == 64 else 2
 
 
+def batch_launches(impl: str, sizes: list[tuple[int, int]], kernels: list[str]) -> int:
+    """Kernel launches of one rfx_fir_batch_launch: plain = one per non-empty capture; tensor
+    core = one persistent launch per 96 tensor-core captures plus one plain launch per capture
+    it hands over; auto = one plain launch per 256 plain captures plus the tensor-core launches."""
+    live = [(m, k, kern) for (m, k), kern in zip(sizes, kernels) if m > 0]
+    tc = sum(1 for _, _, kern in live if kern == "tc_split")
+    plain = len(live) - tc
+    if impl == "plain":
+        return len(live)
+    if impl == "tc_split":
+        return -(-tc // 96) + plain
+    return -(-plain // 256) + -(-tc // 96)
+
+
 def arm_order(w) -> list[str]:
     """Arms to time, the headline first: auto first where it is not simply the tensor-core
     form (the short FIR, the batch, and the channelizer above 64 channels, whose plain form is
@@ -412,24 +424,11 @@ def make_arm(rfx, w, impl: str, device):
     return BatchArm(rfx, w, impl, device) if w.captures else Arm(rfx, w, impl, device)
 
 
-def available(rfx, w, impl: str, device) -> bool:
-    """Whether this library can run `impl` on workload `w` (tries one launch)."""
-    try:
-        arm = make_arm(rfx, w, impl, device)
-        arm.launch(0)
-        arm.release()
-        return True
-    except rfx.RfxError:
-        return False
-
-
-def time_device(launch, steps: int, warmup: int, dist, device) -> float:
-    """Seconds for `steps` launches: barrier + synchronize on both sides, CUDA events on the
-    current stream, max over ranks."""
+def time_round(launch, steps: int, dist, device, first: int = 0) -> float:
+    """Seconds for exactly `steps` launches: barrier + synchronize on both sides, CUDA events on
+    the current (launching) stream, max over ranks."""
     import torch
 
-    for i in range(warmup):
-        launch(i)
     torch.cuda.synchronize()
     barrier(dist, device)
     torch.cuda.synchronize()
@@ -437,87 +436,134 @@ def time_device(launch, steps: int, warmup: int, dist, device) -> float:
     stop = torch.cuda.Event(enable_timing=True)
     start.record()
     for i in range(steps):
-        launch(i)
+        launch(first + i)
     stop.record()
     torch.cuda.synchronize()
     barrier(dist, device)
-    elapsed = start.elapsed_time(stop) / 1e3
-    return max_over_ranks(elapsed, dist, device)
+    return max_over_ranks(start.elapsed_time(stop) / 1e3, dist, device)
 
 
-def kernel_average_s(launch, count: int) -> float:
-    """Average duration of one launch, CUDA events on the launching stream, after the timed
-    region (for the roofline)."""
-    import torch
-
-    torch.cuda.synchronize()
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    a.record()
-    for i in range(count):
-        launch(i)
-    b.record()
-    torch.cuda.synchronize()
-    return a.elapsed_time(b) / 1e3 / count
+MIN_ROUNDS = 5          # the median is taken over at least this many interleaved rounds
+TIMED_TARGET_S = 0.5    # and over enough rounds that the headline arm runs this long in total
+MAX_ROUNDS = 400
 
 
-def cpu_fir_baseline(x: np.ndarray, h: np.ndarray, target_s: float = 2.0) -> dict:
-    """The oracle's float64 FIR on all host cores over a growing prefix of the workload, until
-    one pass takes at least target_s."""
-    from oracle import rf_oracle as orc
+def rounds_for(round_s: float) -> int:
+    return int(max(MIN_ROUNDS, min(MAX_ROUNDS, -(-TIMED_TARGET_S // max(round_s, 1e-6)))))
 
-    threads = os.cpu_count() or 1
-    n = 1 << 14
+
+def measure_arms(rfx, w, impls, args, dist, device, sampler=None):
+    """Times every available implementation of workload `w`: W warm-up steps each, then R
+    rounds, each round timing exactly K steps of every arm in turn (arms interleaved, so drift
+    in clocks or the host affects them alike); per arm the median over rounds. R >= 5, and
+    enough that the headline arm (the first) runs >= 0.5 s in total. Returns {impl: result}."""
+    arms = {}
+    for impl in impls:
+        try:
+            arm = make_arm(rfx, w, impl, device)
+            arm.launch(0)
+        except rfx.RfxError:
+            continue   # not available for this workload in this library
+        arms[impl] = arm
+    for arm in arms.values():
+        for i in range(args.warmup):
+            arm.launch(i)
+    first = next(iter(arms))
+    rounds = rounds_for(time_round(arms[first].launch, args.steps, dist, device))
+    seconds = {impl: [] for impl in arms}
+    ctx = sampler if sampler is not None else _Null()
+    with ctx:
+        for r in range(rounds):
+            for impl, arm in arms.items():
+                seconds[impl].append(time_round(arm.launch, args.steps, dist, device,
+                                                first=r * args.steps))
+    world = dist.get_world_size() if dist is not None else 1
+    out = {}
+    for impl, arm in arms.items():
+        s = seconds[impl]
+        rates = [world * arm.n * args.steps / t / 1e6 for t in s]
+        step_s = statistics.median(s) / args.steps
+        out[impl] = {"msamples_s": statistics.median(rates), "ms_per_step": step_s * 1e3,
+                     "step_s": step_s, "rounds": rounds, "steps_per_round": args.steps,
+                     "round_msamples_s": [min(rates), max(rates)],
+                     "timed_s": sum(s), "launches_per_step": arm.launches_per_step,
+                     "kernel": arm.kernel, "dtype": arm.dtype}
+    return arms, out
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return None
+
+
+# --- CPU baselines (the oracle, timed on the host cores) --------------------------------------
+
+def _grow(fn, size: int, target_s: float, start: int = 1 << 14) -> tuple[int, float]:
+    """Runs fn(n) on a doubling prefix length until one pass takes target_s (or n = size)."""
+    n = start
     while True:
-        n = min(n, x.size)
+        n = min(n, size)
         t0 = time.perf_counter()
-        orc.fir_fast(x[:n], h, threads=threads)
+        fn(n)
         dt = time.perf_counter() - t0
-        if dt >= target_s or n == x.size:
-            break
+        if dt >= target_s or n == size:
+            return n, dt
         n *= 2
-    return {"value": n / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
-            "sample": f"first {n} samples of the workload, {h.size} taps, float64, "
-                      f"{dt:.2f} s on {threads} threads"}
 
 
-def cpu_chan_baseline(x: np.ndarray, h: np.ndarray, m: int, target_s: float = 2.0) -> dict:
+def cpu_baseline_of(w, target_s: float = 2.0) -> dict:
+    """Two CPU figures for workload `w`, in Msamples/s, each over a bounded prefix:
+    * the oracle's threaded C float64 restatement on every host core (kind "port");
+    * `numpy_one_core`: the algorithm of the project's own CPU implementation
+      (tools/reference.py) on one core — np.convolve in float64 for the FIR, NumPy polyphase
+      branch sums and an inverse FFT for the channelizer."""
     from oracle import rf_oracle as orc
 
     threads = os.cpu_count() or 1
-    n = 1 << 14
-    while True:
-        n = min(n, x.size)
-        t0 = time.perf_counter()
-        orc.channelize_fast(x[:n], h, m, threads=threads)
-        dt = time.perf_counter() - t0
-        if dt >= target_s or n == x.size:
-            break
-        n *= 2
+    if w.captures:
+        def run_caps(fn, target):
+            done, count = 0, 0
+            t0 = time.perf_counter()
+            for x, h in w.captures:
+                fn(x, h)
+                done += x.size
+                count += 1
+                if time.perf_counter() - t0 >= target:
+                    break
+            return done, count, time.perf_counter() - t0
+
+        done, count, dt = run_caps(lambda x, h: orc.fir_fast(x, h, threads=threads), target_s)
+        port = {"value": done / dt / 1e6, "unit": "Msamples/s", "cores": threads,
+                "kind": "port", "sample": f"first {count} captures of the batch ({done} "
+                f"samples, own taps each), float64, {dt:.2f} s on {threads} threads"}
+        done1, count1, dt1 = run_caps(lambda x, h: orc.fir_convolve(x, h), target_s / 2)
+        port["numpy_one_core"] = {"value": done1 / dt1 / 1e6, "cores": 1, "sample":
+                                  f"np.convolve float64 over the first {count1} captures "
+                                  f"({done1} samples), {dt1:.2f} s"}
+        return port
+    if w.channels:
+        m = w.channels
+        n, dt = _grow(lambda k: orc.channelize_fast(w.x[:k], w.taps, m, threads=threads),
+                      w.x.size, target_s)
+        n1, dt1 = _grow(lambda k: orc.channelize(w.x[:k], w.taps, m), w.x.size, target_s / 2,
+                        start=1 << 12)
+        what = f"M={m}, {w.taps.size} taps"
+    else:
+        n, dt = _grow(lambda k: orc.fir_fast(w.x[:k], w.taps, threads=threads), w.x.size,
+                      target_s)
+        n1, dt1 = _grow(lambda k: orc.fir_convolve(w.x[:k], w.taps), w.x.size, target_s / 2,
+                        start=1 << 12)
+        what = f"{w.taps.size} taps"
     return {"value": n / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
-            "sample": f"first {n} samples of the workload, M={m}, {h.size} taps, float64, "
-                      f"{dt:.2f} s on {threads} threads"}
-
-
-def cpu_batch_baseline(captures, target_s: float = 2.0) -> dict:
-    """The oracle's float64 FIR on all host cores over the batch's captures in order, until
-    the captures run so far took at least target_s."""
-    from oracle import rf_oracle as orc
-
-    threads = os.cpu_count() or 1
-    done = 0
-    count = 0
-    t0 = time.perf_counter()
-    for x, h in captures:
-        orc.fir_fast(x, h, threads=threads)
-        done += x.size
-        count += 1
-        if time.perf_counter() - t0 >= target_s:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": done / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
-            "sample": f"first {count} captures of the batch ({done} samples, own taps each), "
-                      f"float64, {dt:.2f} s on {threads} threads"}
+            "sample": f"first {n} samples of the workload, {what}, float64, {dt:.2f} s on "
+                      f"{threads} threads",
+            "numpy_one_core": {"value": n1 / dt1 / 1e6, "cores": 1,
+                               "sample": f"first {n1} samples, {what}, "
+                                         f"{'NumPy branch sums + ifft' if w.channels else 'np.convolve'}"
+                                         f" float64, {dt1:.2f} s"}}
 
 
 def config_of(w, impl: str, n: int) -> dict:
@@ -532,6 +578,8 @@ def config_of(w, impl: str, n: int) -> dict:
             "l2": "inputs larger than L2: two input/output buffer sets alternate",
             "seed": w.meta.get("seed")}
 
+
+# --- end to end through the host-facing calls ----------------------------------------------
 
 STREAM_CHUNK = 1 << 21
 STREAM_DEPTH = 4
@@ -557,7 +605,7 @@ def fir_stream_e2e(rfx, w, impl: str, args) -> dict:
     step_ms = statistics.median(times)
     # Upload per chunk: its outputs widened to the kernel's tile plus one tile (tensor core)
     # or K - 1 samples (plain) of history.
-    tc = impl == "tc_split" or (impl == "auto" and auto_picks_tc(w.taps.size, n))
+    tc = rfx.fir_impl_used(impl, w.taps.size, n) == "tc_split"
     tile = 96 * 128 if tc else 1
     hist = tile if tc else w.taps.size - 1
     up = 0
@@ -572,19 +620,24 @@ def fir_stream_e2e(rfx, w, impl: str, args) -> dict:
                                      f"{chunks} chunks of {STREAM_CHUNK}, depth {STREAM_DEPTH})"}
 
 
+def ci16_recording(x: np.ndarray) -> np.ndarray:
+    """The workload as a ci16 SigMF receiver stores it: each component round(v / max|x| * 0.5 *
+    32767) as int16, interleaved."""
+    scale = 0.5 * 32767 / float(np.max(np.abs(x)))
+    c = np.empty(2 * x.size, dtype="<i2")
+    c[0::2] = np.round(x.real.astype(np.float64) * scale)
+    c[1::2] = np.round(x.imag.astype(np.float64) * scale)
+    return c
+
+
 def fir_stream_e2e_ci16(rfx, w, impl: str, args) -> dict:
-    """The same streamed FIR over the workload recorded as a ci16 SigMF receiver would store
-    it (each component round(v / max|x| * 0.5 * 32767), int16): 4 bytes per sample cross the
+    """The same streamed FIR over the workload recorded as ci16: 4 bytes per sample cross the
     host link instead of 8 and the kernels convert them. The output is the FIR of the
     converted samples (not of the float workload), so this line has no error entry."""
     import torch
 
     n = int(w.x.size)
-    scale = 0.5 * 32767 / float(np.max(np.abs(w.x)))
-    c = np.empty(2 * n, dtype="<i2")
-    c[0::2] = np.round(w.x.real.astype(np.float64) * scale)
-    c[1::2] = np.round(w.x.imag.astype(np.float64) * scale)
-    cp = torch.from_numpy(c).pin_memory()
+    cp = torch.from_numpy(ci16_recording(w.x)).pin_memory()
     yp = torch.empty(n, dtype=torch.complex64).pin_memory()
     times = []
     chunks = 0
@@ -631,42 +684,109 @@ def batch_e2e(rfx, w, impl: str, args, device) -> dict:
     arm.release()
     return {"value": arm.n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
             "h2d_bytes_per_step": bytes_, "d2h_bytes_per_step": bytes_, "step_ms": step_ms,
-            "note": "captures packed in one pinned buffer; one copy each way per step; the "
-                    "taps stay resident"}
+            "via": "rfx_fir_batch_launch between one pinned upload and one download per step "
+                   "(captures packed in one buffer; the taps stay resident)"}
+
+
+def chan_e2e(rfx, w, impl: str, args, fmt: str = "cf32") -> dict:
+    """The channelizer end to end through rfx_channelize_host[_format] (pinned host buffers):
+    upload, compute and download per run, timed by the library with CUDA events."""
+    import torch
+
+    n = int(w.x.size)
+    lib = rfx.load()
+    zp = torch.empty(rfx.frames(n, w.channels) * w.channels, dtype=torch.complex64).pin_memory()
+    b = rfx.Bench(warmup=args.warmup, runs=args.steps)
+    if fmt == "cf32":
+        xp = torch.from_numpy(w.x).pin_memory()
+        rfx._check(lib.rfx_channelize_host(rfx.parse_chan_impl(impl), xp.data_ptr(), n,
+                                           w.taps.ctypes.data, w.taps.size, w.channels,
+                                           zp.data_ptr(), rfx.ctypes.byref(b)))
+        up = n * 8
+        via = "rfx_channelize_host (pinned host buffers)"
+    else:
+        cp = torch.from_numpy(ci16_recording(w.x)).pin_memory()
+        rfx._check(lib.rfx_channelize_host_format(
+            rfx.parse_chan_impl(impl), 1, 0, cp.data_ptr(), n, w.taps.ctypes.data,
+            w.taps.size, w.channels, zp.data_ptr(), rfx.ctypes.byref(b)))
+        up = n * 4
+        via = "rfx_channelize_host_format (ci16, converted in the kernel's load stage)"
+    step_ms = b.h2d_ms_mean + b.kernel_ms_mean + b.d2h_ms_mean
+    return {"value": n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
+            "h2d_bytes_per_step": up + w.taps.size * 4, "d2h_bytes_per_step": zp.numel() * 8,
+            "h2d_ms": b.h2d_ms_mean, "kernel_ms": b.kernel_ms_mean, "d2h_ms": b.d2h_ms_mean,
+            "via": via}
+
+
+def e2e_of(rfx, w, impl: str, args, device, with_ci16: bool) -> tuple[dict, dict | None]:
+    if w.captures:
+        return batch_e2e(rfx, w, impl, args, device), None
+    if w.channels:
+        return (chan_e2e(rfx, w, impl, args),
+                chan_e2e(rfx, w, impl, args, fmt="ci16") if with_ci16 else None)
+    return (fir_stream_e2e(rfx, w, impl, args),
+            fir_stream_e2e_ci16(rfx, w, impl, args) if with_ci16 else None)
 
 
 # --- the reference arm -------------------------------------------------------------------------
 
+WORKLOADS = ["fir1025", "fir63", "pfb64", "pfb1024", "batch256"]
+
+
 def run_reference(args) -> None:
+    """The project's CPU implementation of the path (float64) on the host cores: the oracle's
+    threaded C restatement, each step a bounded prefix of the workload (rank 0 only)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    w = load_workload(args.workload)
+    head = args.workload or WORKLOADS[0]
+    w = load_workload(head)
     times = []
     base = None
     for i in range(args.warmup + args.steps):
-        if w.captures:
-            b = cpu_batch_baseline(w.captures, target_s=1.0)
-        elif w.channels:
-            b = cpu_chan_baseline(w.x, w.taps, w.channels, target_s=1.0)
-        else:
-            b = cpu_fir_baseline(w.x, w.taps, target_s=1.0)
+        b = cpu_baseline_of(w, target_s=1.0) if i == args.warmup + args.steps - 1 else \
+            cpu_port_only(w, target_s=1.0)
         if i >= args.warmup:
             times.append(b["value"])
             base = b
     value = statistics.median(times)
+    n = sum(int(x.size) for x, _ in w.captures) if w.captures else int(w.x.size)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {**config_of(w, "reference", sum(int(x.size) for x, _ in w.captures)
-                              if w.captures else int(w.x.size)), "l2": "n/a (CPU)"},
+        "config": {**config_of(w, "reference", n), "l2": "n/a (CPU)"},
         "cpu_baseline": {**base, "value": value},
         "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    if args.workload is None and not args.no_secondary:
+        line["workloads"] = {name: cpu_baseline_of(load_workload(name), target_s=1.0)
+                             for name in WORKLOADS[1:]}
     print(json.dumps(line), flush=True)
+
+
+def cpu_port_only(w, target_s: float) -> dict:
+    """The threaded C oracle alone (one reference-arm step)."""
+    from oracle import rf_oracle as orc
+
+    threads = os.cpu_count() or 1
+    if w.captures:
+        done, t0 = 0, time.perf_counter()
+        for x, h in w.captures:
+            orc.fir_fast(x, h, threads=threads)
+            done += x.size
+            if time.perf_counter() - t0 >= target_s:
+                break
+        return {"value": done / (time.perf_counter() - t0) / 1e6}
+    if w.channels:
+        n, dt = _grow(lambda k: orc.channelize_fast(w.x[:k], w.taps, w.channels,
+                                                    threads=threads), w.x.size, target_s)
+    else:
+        n, dt = _grow(lambda k: orc.fir_fast(w.x[:k], w.taps, threads=threads), w.x.size,
+                      target_s)
+    return {"value": n / dt / 1e6}
 
 
 def magnitude_fusion(rfx, w, args, dist, device) -> dict:
@@ -690,38 +810,137 @@ def magnitude_fusion(rfx, w, args, dist, device) -> dict:
             plan.launch(xs[i % 2], h, z)
             rfx.magnitude_launch(z, mags[i % 2])
 
-        for name, fn in (("fused", fused), ("unfused", unfused)):
-            s = time_device(fn, args.steps, args.warmup, dist, device)
-            out[name] = {"ms_per_step": s / args.steps * 1e3,
-                         "msamples_s": n * args.steps / s / 1e6}
+        for fn in (fused, unfused):
+            for i in range(args.warmup):
+                fn(i)
+        secs = {"fused": [], "unfused": []}
+        for r in range(MIN_ROUNDS):
+            for name, fn in (("fused", fused), ("unfused", unfused)):
+                secs[name].append(time_round(fn, args.steps, dist, device))
+        for name, s in secs.items():
+            t = statistics.median(s)
+            out[name] = {"ms_per_step": t / args.steps * 1e3,
+                         "msamples_s": n * args.steps / t / 1e6}
     out["speedup_fused"] = out["unfused"]["ms_per_step"] / out["fused"]["ms_per_step"]
     return out
 
 
 # --- our arm ---------------------------------------------------------------------------------
 
-def measure_arms(rfx, w, impls, args, dist, device, sample_clocks=False):
-    """Times every available implementation of workload `w`; returns {impl: result}."""
-    out = {}
-    clocks = None
-    for impl in impls:
-        if not available(rfx, w, impl, device):
-            continue
-        arm = make_arm(rfx, w, impl, device)
-        if sample_clocks and clocks is None:
-            with ClockSampler(device.index if device.index is not None else 0) as cs:
-                seconds = time_device(arm.launch, args.steps, args.warmup, dist, device)
-            clocks = cs.summary()
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of it on the
+# workload (dram__bytes_read.sum + dram__bytes_write.sum); writes still in L2 at the kernel's end
+# are not counted by that capture.
+NCU_TRAFFIC_BYTES = {
+    ("fir1025_tones", "tc_split"): 134.5e6 + 80.1e6,   # profiles/fir_tc_fir1025_full.md
+    ("fir63_white", "plain"): 134.2e6 + 89.1e6,        # profiles/fir_plain_fir63_full.md
+    ("pfb64", "tc_split"): 134.4e6 + 83.2e6,           # profiles/chan_tc_pfb64_full.md
+}
+
+
+def useful_flops(w) -> float:
+    """Useful arithmetic per step: the FIR's 4 N K flops (summed over captures for the batch);
+    the channelizer's branch sums, 4 N ceil(L / M)."""
+    if w.captures:
+        return sum(4.0 * h.size * x.size for x, h in w.captures)
+    n = int(w.x.size)
+    if w.channels:
+        return 4.0 * n * (-(-w.taps.size // w.channels))
+    return 4.0 * n * w.taps.size
+
+
+def roofline_of(w, res: dict, n: int, pk: dict) -> dict:
+    """Roofline of one arm's step: tensor-bound (useful FIR flops over the measured bf16 peak)
+    for the tensor-core FIR and the tensor-core batch; HBM-bound (16 B per sample: 8 read and 8
+    written, over the measured copy bandwidth) for everything else."""
+    step_s = res["step_s"]
+    gbs = 16.0 * n / step_s / 1e9
+    kernel = res["kernel"]
+    if kernel == "tc_split" and not w.channels:
+        tflops = useful_flops(w) / step_s / 1e12
+        r = {"bound": "tensor", "achieved": tflops, "peak": pk["bf16_tflops"],
+             "unit": "TFLOP/s", "frac": tflops / pk["bf16_tflops"], "traffic": None,
+             "hbm_achieved_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"]}
+        if w.captures:
+            r["note"] = "useful FIR flops sum 4 N_i K_i over the captures"
         else:
-            seconds = time_device(arm.launch, args.steps, args.warmup, dist, device)
-        kernel_s = kernel_average_s(arm.launch, max(3, min(args.steps, 10)))
-        world = dist.get_world_size() if dist is not None else 1
-        out[impl] = {"msamples_s": world * arm.n * args.steps / seconds / 1e6,
-                     "ms_per_step": seconds / args.steps * 1e3, "kernel_s": kernel_s,
-                     "seconds": seconds, "launches_per_step": arm.launches_per_step,
-                     "dtype": arm.dtype, "max_rel_err_vs_f64": arm.error()}
+            c = (w.taps.size + 126) // 128
+            r["note"] = ("useful FIR flops 4 N K; executed tensor flops are "
+                         "3 * 4 N (128 + 128 C) with C = floor((K + 126) / 128)")
+            r["tensor_executed_tflops"] = 3.0 * 4.0 * n * 128 * (c + 1) / step_s / 1e12
+    else:
+        r = {"bound": "hbm", "achieved": gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+             "frac": gbs / pk["hbm_gbs"], "traffic": None}
+    r["peak_source"] = pk["source"] + " (MEASURED_PEAKS.json burst figures)" \
+        if pk["source"] == "measured" else pk["source"]
+    r["timing"] = (f"CUDA events over the timed rounds: median of {res['rounds']} rounds of "
+                   f"{res['steps_per_round']} steps, {res['launches_per_step']} launch(es) per "
+                   f"step")
+    traffic = NCU_TRAFFIC_BYTES.get((w.name, kernel))
+    if traffic is not None:
+        r["traffic"] = traffic
+        r["traffic_unit"] = "bytes per launch (ncu, one capture)"
+    return r
+
+
+def measure_workload(rfx, name: str, args, dist, device, rank: int, pk: dict,
+                     headline: bool) -> dict:
+    """Everything the bench line reports for one workload: every arm timed (interleaved rounds),
+    the headline arm's roofline, each arm's error over the whole output, the end-to-end figure,
+    the CPU baselines and the clocks seen during the timed rounds."""
+    import torch
+
+    w = load_workload(name)
+    n = sum(int(x.size) for x, _ in w.captures) if w.captures else int(w.x.size)
+    order = arm_order(w)
+    sampler = ClockSampler(device.index if device.index is not None else 0)
+    arms, res = measure_arms(rfx, w, order, args, dist, device, sampler)
+    clocks = sampler.summary()
+    impl = next(iter(res))
+    prim = res[impl]
+    ref = None
+    if rank == 0 and not w.captures:
+        from oracle import rf_oracle as orc
+
+        ref = (orc.channelize_fast(w.x, w.taps, w.channels) if w.channels
+               else orc.fir_fast(w.x, w.taps))
+    for k, arm in arms.items():
+        if rank == 0:
+            res[k].update(arm.error(ref))
         arm.release()
-    return out, clocks
+    del arms, ref
+    torch.cuda.empty_cache()
+
+    out = {"value": prim["msamples_s"], "ms_per_step": prim["ms_per_step"],
+           "dtype": prim["dtype"], "config": config_of(w, impl, n),
+           "max_rel_err_vs_f64": prim.get("max_rel_err_vs_f64"),
+           "roofline": roofline_of(w, prim, n, pk), "clocks": clocks,
+           "gpu_launches": prim["rounds"] * args.steps * prim["launches_per_step"],
+           "timing": {"rounds": prim["rounds"], "steps_per_round": args.steps,
+                      "statistic": "median over rounds; arms interleaved within each round",
+                      "headline_arm_timed_s": prim["timed_s"]},
+           "compare": {k: {kk: vv for kk, vv in v.items() if kk not in ("step_s", "timed_s")}
+                       for k, v in res.items()}}
+    if "plain" in res and impl != "plain":
+        out["speedup_vs_plain_fp32"] = prim["msamples_s"] / res["plain"]["msamples_s"]
+    if "plain" in res and not w.channels and not w.captures:
+        sm_mhz = clocks.get("sm_mhz") or 1900.0
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        flops = useful_flops(w) / res["plain"]["step_s"] / 1e12
+        out["plain_fp32_simt"] = {"achieved_tflops": flops,
+                                  "peak_tflops_at_sampled_clock": fp32_peak,
+                                  "frac": flops / fp32_peak}
+    if w.channels == 64 and "tc_split" in res:
+        out["channelize_magnitude"] = magnitude_fusion(rfx, w, args, dist, device)
+    if rank == 0:
+        e2e, e2e_ci16 = e2e_of(rfx, w, impl, args, device, with_ci16=headline or w.channels)
+        out["e2e"] = e2e
+        if e2e_ci16 is not None:
+            out["e2e_ci16_recording"] = e2e_ci16
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline_of(w, target_s=2.0 if headline else 1.0)
+    del w
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_ours(args) -> None:
@@ -736,158 +955,28 @@ def run_ours(args) -> None:
     rfx.load()
     pk = peaks()
 
-    w = load_workload(args.workload)
-    if w.captures:
-        ns = [int(x.size) for x, _ in w.captures]
-        n = sum(ns)
-        useful = sum(4.0 * h.size * m for (_, h), m in zip(w.captures, ns))
-    else:
-        n = int(w.x.size)
-        if w.channels:
-            useful = 4.0 * n * (-(-w.taps.size // w.channels))  # branch FIR flops
-        else:
-            useful = 4.0 * n * w.taps.size                       # FIR flops
-    order = arm_order(w)
-    arms, clocks = measure_arms(rfx, w, order, args, dist, device, sample_clocks=True)
-    impl = next(iter(arms))
-    prim = arms[impl]
-    value = prim["msamples_s"]
-    kernel_s = prim["kernel_s"]
-
-    # Roofline of the dominant kernel.
-    extras: dict = {}
-    algo_bytes = 16.0 * n  # 8 B read + 8 B written per sample
-    achieved_gbs = algo_bytes / kernel_s / 1e9
-    if impl == "tc_split" and w.captures:
-        roofline = {"bound": "tensor", "achieved": useful / kernel_s / 1e12,
-                    "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                    "frac": useful / kernel_s / 1e12 / pk["bf16_tflops"], "traffic": None,
-                    "note": "useful FIR flops sum 4*N_i*K_i over the captures; the short-tap "
-                            "captures are bound by HBM instead (hbm_achieved_gbs)"}
-        extras["hbm_achieved_gbs"] = achieved_gbs
-        extras["hbm_frac"] = achieved_gbs / pk["hbm_gbs"]
-    elif impl == "tc_split" and not w.channels:
-        roofline = {"bound": "tensor", "achieved": useful / kernel_s / 1e12,
-                    "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                    "frac": useful / kernel_s / 1e12 / pk["bf16_tflops"], "traffic": None,
-                    "note": "useful FIR flops 4*N*K; executed tensor flops are "
-                            "3*4*N*(128+128*C) with C = floor((K+126)/128)"}
-        c = (w.taps.size + 126) // 128
-        executed = 3.0 * 4.0 * n * 128 * (c + 1)
-        extras["tensor_executed_tflops"] = executed / kernel_s / 1e12
-    else:
-        roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"],
-                    "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None}
-    roofline["peak_source"] = pk["source"]
-    kernel_impl = impl
-    if impl == "auto" and not w.captures and not w.channels:
-        kernel_impl = "tc_split" if auto_picks_tc(w.taps.size, n) else "plain"
-    if impl == "auto" and w.channels:
-        kernel_impl = "tc_split" if w.channels == 64 else "plain"
-    traffic = NCU_TRAFFIC_BYTES.get((w.name, kernel_impl))
-    if traffic is not None:
-        roofline["traffic"] = traffic
-        roofline["traffic_unit"] = "bytes per launch (ncu, one capture)"
-    if "plain" in arms and not w.channels and not w.captures:
-        sm_mhz = (clocks or {}).get("sm_mhz") or 1900.0
-        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-        ks = arms["plain"]["kernel_s"]
-        extras["plain_fp32_simt"] = {"achieved_tflops": useful / ks / 1e12,
-                                     "peak_tflops_at_sampled_clock": fp32_peak,
-                                     "frac": useful / ks / 1e12 / fp32_peak}
-    compare = {k: {kk: vv for kk, vv in v.items() if kk not in ("seconds",)}
-               for k, v in arms.items()}
-    if "plain" in arms and impl != "plain":
-        extras["speedup_vs_plain_fp32"] = value / arms["plain"]["msamples_s"]
-
-    # channelize |> magnitude: fused in the tensor-core epilogue vs the two kernels in turn.
-    if w.channels and "tc_split" in arms:
-        extras["channelize_magnitude"] = magnitude_fusion(rfx, w, args, dist, device)
-
-    # The other headline workload (64-channel PFB) in the same run.
-    if args.workload == "fir1025" and not args.no_secondary:
-        w2 = load_workload("pfb64")
-        arms2, _ = measure_arms(rfx, w2, ["tc_split", "plain"], args, dist, device)
-        extras["pfb64"] = {k: {kk: vv for kk, vv in v.items() if kk != "seconds"}
-                           for k, v in arms2.items()}
-        if "plain" in arms2 and len(arms2) > 1:
-            first = next(iter(arms2))
-            extras["pfb64"]["speedup_vs_plain_fp32"] = (
-                arms2[first]["msamples_s"] / arms2["plain"]["msamples_s"])
-        del w2
-
-    # End to end through the public host-buffer call, pinned host memory.
-    e2e = None
-    if rank == 0:
-        xp = torch.from_numpy(w.x).pin_memory() if not w.captures else None
-        b = rfx.Bench(warmup=args.warmup, runs=args.steps)
-        lib = rfx.load()
-        if w.captures:
-            e2e = batch_e2e(rfx, w, impl, args, device)
-        elif w.channels:
-            zp = torch.empty(rfx.frames(n, w.channels) * w.channels,
-                             dtype=torch.complex64).pin_memory()
-            rfx._check(lib.rfx_channelize_host(rfx.parse_chan_impl(impl), xp.data_ptr(), n,
-                                               w.taps.ctypes.data, w.taps.size, w.channels,
-                                               zp.data_ptr(), rfx.ctypes.byref(b)))
-            d2h = zp.numel() * 8
-        else:
-            e2e = fir_stream_e2e(rfx, w, impl, args)
-            extras["e2e_ci16_recording"] = fir_stream_e2e_ci16(rfx, w, impl, args)
-        if w.channels:
-            step_ms = b.h2d_ms_mean + b.kernel_ms_mean + b.d2h_ms_mean
-            e2e = {"value": n / (step_ms / 1e3) / 1e6, "unit": "Msamples/s",
-                   "h2d_bytes_per_step": n * 8 + w.taps.size * 4, "d2h_bytes_per_step": d2h,
-                   "h2d_ms": b.h2d_ms_mean, "kernel_ms": b.kernel_ms_mean,
-                   "d2h_ms": b.d2h_ms_mean}
-            # The same through rfx_channelize_host_format over the workload as a ci16
-            # recording (components round(v / max|x| * 0.5 * 32767)): half the upload.
-            scale = 0.5 * 32767 / float(np.max(np.abs(w.x)))
-            c = np.empty(2 * n, dtype="<i2")
-            c[0::2] = np.round(w.x.real.astype(np.float64) * scale)
-            c[1::2] = np.round(w.x.imag.astype(np.float64) * scale)
-            cp = torch.from_numpy(c).pin_memory()
-            b2 = rfx.Bench(warmup=args.warmup, runs=args.steps)
-            rfx._check(lib.rfx_channelize_host_format(
-                rfx.parse_chan_impl(impl), 1, 0, cp.data_ptr(), n, w.taps.ctypes.data,
-                w.taps.size, w.channels, zp.data_ptr(), rfx.ctypes.byref(b2)))
-            step2 = b2.h2d_ms_mean + b2.kernel_ms_mean + b2.d2h_ms_mean
-            extras["e2e_ci16_recording"] = {
-                "value": n / (step2 / 1e3) / 1e6, "unit": "Msamples/s",
-                "h2d_bytes_per_step": n * 4 + w.taps.size * 4, "d2h_bytes_per_step": d2h,
-                "h2d_ms": b2.h2d_ms_mean, "kernel_ms": b2.kernel_ms_mean,
-                "d2h_ms": b2.d2h_ms_mean,
-                "via": "rfx_channelize_host_format (ci16, converted in the kernel's load stage)"}
-
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        if w.captures:
-            cpu = cpu_batch_baseline(w.captures)
-        elif w.channels:
-            cpu = cpu_chan_baseline(w.x, w.taps, w.channels)
-        else:
-            cpu = cpu_fir_baseline(w.x, w.taps)
+    names = [args.workload] if args.workload else \
+        (WORKLOADS[:1] if args.no_secondary else WORKLOADS)
+    head = measure_workload(rfx, names[0], args, dist, device, rank, pk, headline=True)
+    others = {name: measure_workload(rfx, name, args, dist, device, rank, pk, headline=False)
+              for name in names[1:]}
 
     fault = rfx.device_fault()
     if fault:
         raise SystemExit(f"a kernel recorded fault code {fault:#x}")
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": prim["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": prim["dtype"],
-            "data": "synthetic",
-            "config": config_of(w, impl, n),
-            "max_rel_err_vs_f64": prim["max_rel_err_vs_f64"],
-            "roofline": roofline,
-            "cpu_baseline": cpu,
-            "e2e": e2e,
-            "clocks": clocks,
-            "gpu_launches": args.steps * prim["launches_per_step"],
-            "compare": compare,
-            **extras,
+            "metric": METRIC, "value": head["value"], "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": head["dtype"], "data": "synthetic",
+            **{k: v for k, v in head.items()
+               if k not in ("value", "ms_per_step", "dtype")},
         }
+        line.setdefault("cpu_baseline", None)
+        line.setdefault("e2e", None)
+        if others:
+            line["workloads"] = others
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -896,14 +985,15 @@ def run_ours(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="fir1025",
-                    choices=["fir1025", "fir63", "pfb64", "pfb1024", "batch256"])
+    ap.add_argument("--workload", default=None, choices=WORKLOADS,
+                    help="one workload as the headline (default: fir1025 as the headline and "
+                         "the other four reported under 'workloads')")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
-                    help="skip the 64-channel PFB measured beside the FIR")
+                    help="only the headline workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

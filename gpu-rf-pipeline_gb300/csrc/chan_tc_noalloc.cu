@@ -15,6 +15,7 @@
 #include "api_error.hpp"
 #include "chan_tc.cuh"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -35,37 +36,97 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_static_twiddles[kStaticTwiddleBytes];
 
 std::mutex g_setup_mutex;
-void* g_twiddles_of[kMaxDevices];  // the array's device address once built, per device
+// Per device: the array's device address and the id of the CUDA context it was built in. A
+// cudaDeviceReset destroys that context and reloads the module with the array zeroed; the next
+// call sees a new context id and builds the operand again.
+void* g_twiddles_of[kMaxDevices];
+unsigned long long g_context_of[kMaxDevices];
 
-// Builds the twiddle image in the static array of the current device on its first call (the
-// image's unused padding must be zero, so the array is cleared first), then waits for it on
-// `stream`, so that calls on any stream of the device see the finished image.
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// The unique id of the calling thread's current CUDA context (0 if there is none), through the
+// driver entry points the runtime hands out (no link against libcuda).
+unsigned long long current_context_id()
+{
+    static CtxGetCurrent get_current = nullptr;
+    static CtxGetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault,
+                                             &qa) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) ==
+                cudaSuccess &&
+            qb == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrent>(a);
+            get_id = reinterpret_cast<CtxGetId>(b);
+        }
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current == nullptr || get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr ||
+        get_id(ctx, &id) != CUDA_SUCCESS) {
+        return 0;
+    }
+    return id;
+}
+
+int cuda_error(cudaError_t err, const char* where)
+{
+    char msg[256];
+    std::snprintf(msg, sizeof(msg), "CUDA error: %s (code %d) in %s", cudaGetErrorString(err),
+                  static_cast<int>(err), where);
+    return set_last_error(RFX_ERR_CUDA, msg);
+}
+
+// Builds the twiddle image in the static array of the current device on the first call in this
+// CUDA context (the image's unused padding must be zero, so the array is cleared first), then
+// waits for it on `stream`, so that calls on any stream of the device see the finished image.
 int static_twiddles(int device, cudaStream_t stream, void** out)
 {
+    // The array's address in this context; this also makes the device's primary context
+    // current, so that the context id below is the one the kernel will run in.
+    void* p = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&p, g_static_twiddles);
+    if (err != cudaSuccess) {
+        return cuda_error(err, "channelize_tc_static setup (cudaGetSymbolAddress)");
+    }
+    const unsigned long long context = current_context_id();
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (g_twiddles_of[device] != nullptr) {
-        *out = g_twiddles_of[device];
+    if (g_twiddles_of[device] == p && context != 0 && g_context_of[device] == context) {
+        *out = p;
         return RFX_OK;
     }
     if (chan_tc_twiddle_bytes() > kStaticTwiddleBytes) {
         return set_last_error(RFX_ERR_CAPACITY,
                               "channelize_tc_static: the twiddle operand outgrew the static array");
     }
-    void* p = nullptr;
-    cudaError_t err = cudaGetSymbolAddress(&p, g_static_twiddles);
-    if (err == cudaSuccess) {
-        err = chan_tc_build_twiddles(p, stream);
+    // The build is stream work followed by a wait: inside a stream capture it would be
+    // recorded into the caller's graph and the wait would break the capture.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    err = cudaStreamIsCapturing(stream, &capture);
+    if (err != cudaSuccess) {
+        return cuda_error(err, "channelize_tc_static setup (cudaStreamIsCapturing)");
     }
+    if (capture != cudaStreamCaptureStatusNone) {
+        return set_last_error(RFX_ERR_INVALID,
+                              "channelize_tc_static: the first call on a device (and the first "
+                              "after cudaDeviceReset) builds the twiddle operand and must be "
+                              "made outside stream capture");
+    }
+    err = chan_tc_build_twiddles(p, stream);
     if (err == cudaSuccess) {
         err = cudaStreamSynchronize(stream);
     }
     if (err != cudaSuccess) {
-        char msg[256];
-        std::snprintf(msg, sizeof(msg), "CUDA error: %s (code %d) in channelize_tc_static setup",
-                      cudaGetErrorString(err), static_cast<int>(err));
-        return set_last_error(RFX_ERR_CUDA, msg);
+        return cuda_error(err, "channelize_tc_static setup");
     }
     g_twiddles_of[device] = p;
+    g_context_of[device] = context;
     *out = p;
     return RFX_OK;
 }
@@ -126,10 +187,5 @@ extern "C" int rfx_channelize_tc_static(const void* x, const float* taps, void* 
         return status;
     }
     err = chan_tc_launch(x, taps, twiddles, out, num_samples, num_taps, stream);
-    if (err != cudaSuccess) {
-        std::snprintf(msg, sizeof(msg), "CUDA error: %s (code %d) in chan_tc_launch",
-                      cudaGetErrorString(err), static_cast<int>(err));
-        return set_last_error(RFX_ERR_CUDA, msg);
-    }
-    return RFX_OK;
+    return err == cudaSuccess ? RFX_OK : cuda_error(err, "chan_tc_launch");
 }

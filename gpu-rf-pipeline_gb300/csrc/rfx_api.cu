@@ -312,6 +312,30 @@ int rfx_fir_launch_format(int impl, int format, const void* x, const float* taps
                              num_samples, num_taps, stream);
 }
 
+int rfx_fir_impl_used(int impl, int num_taps, int64_t num_samples, int batch, int* used)
+{
+    if (used == nullptr) {
+        return fail(RFX_ERR_INVALID, "fir_impl_used: null result pointer");
+    }
+    if (impl < RFX_FIR_PLAIN || impl > RFX_FIR_AUTO) {
+        return fail(RFX_ERR_INVALID, "fir_impl_used: unknown implementation %d", impl);
+    }
+    if (num_taps < 1 || num_taps > rfx::kMaxTaps || num_samples < 0) {
+        return fail(RFX_ERR_INVALID, "fir_impl_used: %d taps, %lld samples", num_taps,
+                    static_cast<long long>(num_samples));
+    }
+    int r = resolve_fir_impl(impl, num_taps, num_samples);
+    constexpr int64_t kBlockOutputs = 128;  // the tensor-core kernels' output block
+    if (r == RFX_FIR_TC && num_samples < kBlockOutputs) {
+        r = RFX_FIR_PLAIN;  // no whole block to compute: the plain kernel is exact
+    }
+    if (r == RFX_FIR_TC && batch != 0 && !rfx::fir_batch_supported(num_taps)) {
+        r = RFX_FIR_PLAIN;  // the persistent batch kernel's shared-memory budget is smaller
+    }
+    *used = r;
+    return RFX_OK;
+}
+
 int rfx_fir_device(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
                    int num_taps)
 {

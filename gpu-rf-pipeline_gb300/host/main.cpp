@@ -1,31 +1,37 @@
-// rfgpu: the command-line front end for this library's filtering path, with the gpu-rf-pipeline
-// tool's grammar for the operations it covers (src/main.cpp:1-13):
+// rfgpu: the command-line front end of this library's filtering path. Its interface — the
+// subcommands, their flags, the JSON reports and the exit codes — is the gpu-rf-pipeline tool's
+// for the operations it covers (src/main.cpp:1-13), because that tool's tests drive it:
 //
-//   rfgpu fir        --in X.cf32 --taps H.f32 --out Y.cf32 [--impl NAME] [--block B]
-//   rfgpu channelize --in X.cf32 --taps H.f32 --channels M --out Z.cf32 [--impl NAME]
-//                    [--output complex|magnitude]   (magnitude: |z| as float32, fused)
-//   rfgpu magnitude  --in X.cf32 --out MAG.f32
-//   rfgpu stream     --in X.cf32 --taps H.f32 --out Y.cf32 [--impl NAME] [--chunk N]
-//                    [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]
+//   rfgpu fir        --in X --taps H.f32 --out Y.cf32 [--impl NAME] [--block B]
+//   rfgpu channelize --in X --taps H.f32 --channels M --out Z [--impl NAME]
+//                    [--output complex|magnitude]
+//   rfgpu magnitude  --in X --out MAG.f32
+//   rfgpu stream     --in X --taps H.f32 --out Y.cf32 [--impl NAME] [--chunk N] [--depth D]
+//                    [--memory copy|registered|zero-copy] [--rate HZ]
 //   rfgpu info
-//   (every X input may be a SigMF recording, NAME.sigmf-meta or NAME.sigmf-data, in cf32_le,
-//    ci16_le or ci8; fir and channelize: [--bench N [--warmup W]] prints phase timings as JSON; stream: the
-//    wall-clock time of whole streamed passes, with the throughput against the sample rate)
 //
-// Exit status: 0 on success, 1 on a runtime error (file, CUDA, cuFFT), 2 on a usage error.
+// X is a .cf32 file or a SigMF recording (either file of the pair) in cf32_le, ci16_le or ci8.
+// fir, channelize, magnitude and stream take [--bench N [--warmup W]].
+// Exit status: 0 success, 1 runtime error (file, CUDA, cuFFT), 2 usage error.
+//
+// Structure: every subcommand is a row of a table (its flags with their value kinds, bounds and
+// choices, and its handler). The whole command line is checked against the row before any file
+// is opened, so a usage error never leaves a partial output behind; the usage text is printed
+// from the same table.
 #include "bench.hpp"
 #include "check.hpp"
 #include "io.hpp"
 #include "ops.hpp"
 #include "stream.hpp"
 
+#include <algorithm>
+#include <cerrno>
 #include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <exception>
 #include <map>
-#include <set>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -36,406 +42,566 @@ struct UsageError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// --- the option grammar ----------------------------------------------------------------------
+
+enum class Kind {
+    Path,   // any text
+    Count,  // an integer in [lo, hi], a multiple of `step`
+    Real,   // a finite number
+    Word,   // one of choices()
+};
+
+struct Flag {
+    const char* name;
+    Kind kind;
+    const char* meta;  // placeholder in the usage text
+    bool required;
+    long lo;
+    long hi;
+    long step;
+    std::vector<std::string> (*choices)();
+    const char* needs;  // another flag this one is only valid with, or nullptr
+};
+
+Flag path_flag(const char* name, const char* meta, bool required)
+{
+    return {name, Kind::Path, meta, required, 0, 0, 1, nullptr, nullptr};
+}
+
+Flag count_flag(const char* name, const char* meta, long lo, long hi = INT_MAX, long step = 1,
+                bool required = false, const char* needs = nullptr)
+{
+    return {name, Kind::Count, meta, required, lo, hi, step, nullptr, needs};
+}
+
+Flag word_flag(const char* name, const char* meta, std::vector<std::string> (*choices)())
+{
+    return {name, Kind::Word, meta, false, 0, 0, 1, choices, nullptr};
+}
+
+Flag real_flag(const char* name, const char* meta)
+{
+    return {name, Kind::Real, meta, false, 0, 0, 1, nullptr, nullptr};
+}
+
 template <class Fn>
-std::string impl_names(const std::vector<Impl<Fn>>& impls, const char* sep)
+std::vector<std::string> names_of(const std::vector<Impl<Fn>>& table)
+{
+    std::vector<std::string> out;
+    for (const Impl<Fn>& row : table) {
+        out.emplace_back(row.name);
+    }
+    return out;
+}
+
+std::vector<std::string> fir_names() { return names_of(fir_impls()); }
+std::vector<std::string> chan_names() { return names_of(channelize_impls()); }
+std::vector<std::string> output_names() { return {"complex", "magnitude"}; }
+std::vector<std::string> memory_names() { return {"copy", "registered", "zero-copy"}; }
+
+std::string joined(const std::vector<std::string>& items, const std::string& glue)
 {
     std::string s;
-    for (const Impl<Fn>& impl : impls) {
-        if (!s.empty()) {
-            s += sep;
-        }
-        s += impl.name;
+    for (std::size_t i = 0; i < items.size(); ++i) {
+        s += (i ? glue : std::string()) + items[i];
     }
     return s;
 }
 
-template <class Fn>
-void print_impls(const char* op, const std::vector<Impl<Fn>>& impls)
-{
-    for (std::size_t i = 0; i < impls.size(); ++i) {
-        std::fprintf(stderr, "  %-10s --impl %-12s %s%s\n", op, impls[i].name, impls[i].summary,
-                     i == 0 ? " (default)" : "");
-    }
-}
-
-void print_usage()
-{
-    std::fprintf(stderr,
-                 "usage:\n"
-                 "  rfgpu fir        --in X.cf32 --taps H.f32 --out OUT.cf32 [--impl NAME] "
-                 "[--block B]\n"
-                 "  rfgpu channelize --in X.cf32 --taps H.f32 --channels M --out OUT.cf32 "
-                 "[--impl NAME]\n"
-                 "                  [--output complex|magnitude]  magnitude: |z| per channel as "
-                 "float32\n"
-                 "  rfgpu magnitude  --in X.cf32 --out OUT.f32\n"
-                 "  rfgpu stream     --in X.cf32 --taps H.f32 --out OUT.cf32 [--impl NAME] "
-                 "[--chunk N]\n"
-                 "                  [--depth D] [--memory copy|registered|zero-copy] [--rate HZ]\n"
-                 "                  FIR in chunks through a ring of D pinned buffers and CUDA streams\n"
-                 "  rfgpu info       GPU, CUDA versions and implementations as JSON\n"
-                 "\n"
-                 "Every .cf32 input may also be a SigMF recording (NAME.sigmf-meta or "
-                 "NAME.sigmf-data)\n"
-                 "in cf32_le, ci16_le or ci8; fir converts integer recordings on the GPU.\n"
-                 "\n"
-                 "benchmark options (fir, channelize, magnitude, stream):\n"
-                 "  --bench N      time N runs with CUDA events and print the result as JSON\n"
-                 "  --warmup W     untimed runs before measuring (default 3, needs --bench)\n"
-                 "\n"
-                 "implementations:\n");
-    print_impls("fir", fir_impls());
-    print_impls("channelize", channelize_impls());
-}
-
-// "--flag value" pairs of one subcommand, each flag at most once and from an allowed set.
-class Args {
+// The validated options of one command line.
+class Options {
 public:
-    Args(int argc, char** argv, const std::set<std::string>& allowed)
+    bool given(const char* flag) const { return text_.count(flag) != 0; }
+    const std::string& text(const char* flag) const { return text_.at(flag); }
+    std::string text_or(const char* flag, const std::string& fallback) const
     {
-        for (int i = 2; i < argc; i += 2) {
-            const std::string flag = argv[i];
-            if (allowed.count(flag) == 0) {
-                throw UsageError("unknown option '" + flag + "' for " + argv[1]);
-            }
-            if (i + 1 >= argc) {
-                throw UsageError("option " + flag + " needs a value");
-            }
-            if (!values_.emplace(flag, argv[i + 1]).second) {
-                throw UsageError("option " + flag + " given twice");
-            }
+        return given(flag) ? text(flag) : fallback;
+    }
+    int count_or(const char* flag, int fallback) const
+    {
+        return given(flag) ? static_cast<int>(std::strtol(text(flag).c_str(), nullptr, 10))
+                           : fallback;
+    }
+    double real(const char* flag) const { return std::strtod(text(flag).c_str(), nullptr); }
+
+    // Bench settings: --bench N timed runs after --warmup W (default 3) untimed ones.
+    BenchConfig bench() const
+    {
+        BenchConfig c;
+        if (given("--bench")) {
+            c.runs = count_or("--bench", 1);
+            c.warmup = count_or("--warmup", 3);
         }
+        return c;
     }
 
-    bool has(const std::string& flag) const { return values_.count(flag) != 0; }
-
-    const std::string& required(const std::string& flag) const
-    {
-        const auto it = values_.find(flag);
-        if (it == values_.end()) {
-            throw UsageError("missing required option " + flag);
-        }
-        return it->second;
-    }
-
-    std::string optional(const std::string& flag, const std::string& fallback) const
-    {
-        const auto it = values_.find(flag);
-        return it == values_.end() ? fallback : it->second;
-    }
-
-    int integer(const std::string& flag, int fallback, int minimum) const
-    {
-        const auto it = values_.find(flag);
-        if (it == values_.end()) {
-            return fallback;
-        }
-        char* end = nullptr;
-        const long v = std::strtol(it->second.c_str(), &end, 10);
-        if (end == it->second.c_str() || *end != '\0' || v < minimum || v > INT_MAX) {
-            throw UsageError(flag + " needs an integer of at least " + std::to_string(minimum) +
-                             ", got '" + it->second + "'");
-        }
-        return static_cast<int>(v);
-    }
-
-private:
-    std::map<std::string, std::string> values_;
+    std::map<std::string, std::string> text_;
 };
 
-template <class Fn>
-const Impl<Fn>& find_impl(const std::vector<Impl<Fn>>& impls, const Args& args, const char* op)
+void check_value(const std::string& command, const Flag& f, const std::string& v)
 {
-    const std::string name = args.optional("--impl", impls.front().name);
-    for (const Impl<Fn>& impl : impls) {
-        if (name == impl.name) {
-            return impl;
+    switch (f.kind) {
+    case Kind::Path:
+        return;
+    case Kind::Count: {
+        errno = 0;
+        char* end = nullptr;
+        const long n = std::strtol(v.c_str(), &end, 10);
+        const bool number = !v.empty() && *end == '\0' && errno == 0;
+        if (!number || n < f.lo || n > f.hi || n % f.step != 0) {
+            std::string want = "an integer >= " + std::to_string(f.lo);
+            if (f.hi != INT_MAX) {
+                want += " and <= " + std::to_string(f.hi);
+            }
+            if (f.step != 1) {
+                want += ", a multiple of " + std::to_string(f.step);
+            }
+            throw UsageError(command + " " + f.name + " '" + v + "': expected " + want);
+        }
+        return;
+    }
+    case Kind::Real: {
+        char* end = nullptr;
+        const double x = std::strtod(v.c_str(), &end);
+        if (v.empty() || *end != '\0' || !std::isfinite(x)) {
+            throw UsageError(command + " " + f.name + " '" + v + "': expected a number");
+        }
+        return;
+    }
+    case Kind::Word: {
+        const std::vector<std::string> ok = f.choices();
+        if (std::find(ok.begin(), ok.end(), v) == ok.end()) {
+            throw UsageError(command + " " + f.name + " '" + v + "' is not one of: " +
+                             joined(ok, ", "));
+        }
+        return;
+    }
+    }
+}
+
+Options parse(const std::string& command, const std::vector<Flag>& flags,
+              const std::vector<std::string>& words)
+{
+    Options o;
+    for (std::size_t i = 0; i < words.size(); i += 2) {
+        const std::string& name = words[i];
+        const auto f = std::find_if(flags.begin(), flags.end(),
+                                    [&](const Flag& g) { return name == g.name; });
+        if (f == flags.end()) {
+            throw UsageError(command + " has no option '" + name + "'");
+        }
+        if (i + 1 == words.size()) {
+            throw UsageError(command + " " + name + " is missing its value");
+        }
+        if (o.given(f->name)) {
+            throw UsageError(command + " " + name + " appears more than once");
+        }
+        check_value(command, *f, words[i + 1]);
+        o.text_[f->name] = words[i + 1];
+    }
+    for (const Flag& f : flags) {
+        if (f.required && !o.given(f.name)) {
+            throw UsageError(command + " needs " + f.name + " " + f.meta);
+        }
+        if (f.needs != nullptr && o.given(f.name) && !o.given(f.needs)) {
+            throw UsageError(command + " " + f.name + " is only valid with " + f.needs);
         }
     }
-    throw UsageError("unknown --impl '" + name + "' for " + op + " (available: " +
-                     impl_names(impls, ", ") + ")");
+    return o;
 }
 
-BenchConfig bench_config(const Args& args)
+// --- JSON reports --------------------------------------------------------------------------
+
+std::string json_text(const std::string& s)
 {
-    BenchConfig config;
-    if (args.has("--bench")) {
-        config.runs = args.integer("--bench", 1, 1);
-        config.warmup = args.integer("--warmup", 3, 0);
-    } else if (args.has("--warmup")) {
-        throw UsageError("--warmup needs --bench");
+    std::string out = "\"";
+    for (const char c : s) {
+        if (c == '"' || c == '\\') {
+            out += '\\';
+            out += c;
+        } else if (static_cast<unsigned char>(c) < 0x20) {
+            char esc[8];
+            std::snprintf(esc, sizeof esc, "\\u%04x", static_cast<unsigned>(c));
+            out += esc;
+        } else {
+            out += c;
+        }
     }
-    return config;
+    return out + "\"";
 }
 
-void require_int_range(std::size_t count, const std::string& what)
+// Shortest decimal that reads back as the same double.
+std::string json_number(double x)
 {
-    if (count > static_cast<std::size_t>(INT_MAX)) {
-        throw std::runtime_error(what + " has " + std::to_string(count) +
-                                 " elements, more than the supported " + std::to_string(INT_MAX));
+    char buf[40];
+    for (int digits = 15; digits <= 17; ++digits) {
+        std::snprintf(buf, sizeof buf, "%.*g", digits, x);
+        if (std::strtod(buf, nullptr) == x) {
+            break;
+        }
     }
+    return buf;
 }
 
-std::string gpu_name()
-{
-    int device = 0;
-    CUDA_CHECK(cudaGetDevice(&device));
+class Json {
+public:
+    Json& put(const char* key, const std::string& v) { return raw(key, json_text(v)); }
+    Json& put(const char* key, const char* v) { return raw(key, json_text(v)); }
+    Json& put(const char* key, double v) { return raw(key, json_number(v)); }
+    Json& put(const char* key, int v) { return raw(key, std::to_string(v)); }
+    Json& put(const char* key, std::size_t v) { return raw(key, std::to_string(v)); }
+    Json& put(const char* key, const PhaseTime& t)
+    {
+        return raw(key, Json().put("mean", t.mean_ms).put("std", t.std_ms).str());
+    }
+    Json& put(const char* key, const std::vector<std::string>& list)
+    {
+        std::vector<std::string> quoted;
+        for (const std::string& s : list) {
+            quoted.push_back(json_text(s));
+        }
+        return raw(key, "[" + joined(quoted, ", ") + "]");
+    }
+    Json& raw(const char* key, const std::string& value)
+    {
+        body_ += (body_.empty() ? "" : ", ") + json_text(key) + ": " + value;
+        return *this;
+    }
+    std::string str() const { return "{" + body_ + "}"; }
+
+private:
+    std::string body_;
+};
+
+struct Device {
     cudaDeviceProp prop{};
-    CUDA_CHECK(cudaGetDeviceProperties(&prop, device));
-    return prop.name;
+    int runtime = 0;
+    int driver = 0;
+
+    static Device current()
+    {
+        Device d;
+        int index = 0;
+        CUDA_CHECK(cudaGetDevice(&index));
+        CUDA_CHECK(cudaGetDeviceProperties(&d.prop, index));
+        CUDA_CHECK(cudaRuntimeGetVersion(&d.runtime));
+        CUDA_CHECK(cudaDriverGetVersion(&d.driver));
+        return d;
+    }
+};
+
+std::string cuda_version(int packed)  // 13000 -> "13.0"
+{
+    return std::to_string(packed / 1000) + "." + std::to_string(packed % 1000 / 10);
 }
 
-void report(const Args& args, const char* op, const char* impl, std::size_t num_in,
-            std::size_t num_out, const Bench& bench);
+// What one compute subcommand did, for its report.
+struct Done {
+    const char* op;
+    std::string impl;
+    std::size_t num_in;
+    std::size_t num_out;
+};
 
-void finish(const Args& args, const char* op, const char* impl, std::size_t num_in,
-            const std::vector<cf32>& out, const Bench& bench)
+// Without --bench, one line for a person; with it, the phase timings as one JSON object.
+void report(const Options& o, const Done& d, const Bench& bench)
 {
-    write_cf32(args.required("--out"), out);
-    report(args, op, impl, num_in, out.size(), bench);
-}
-
-void finish_f32(const Args& args, const char* op, const char* impl, std::size_t num_in,
-                const std::vector<float>& out, const Bench& bench)
-{
-    write_f32(args.required("--out"), out);
-    report(args, op, impl, num_in, out.size(), bench);
-}
-
-void report(const Args& args, const char* op, const char* impl, std::size_t num_in,
-            std::size_t num_out, const Bench& bench)
-{
-    const std::string& path = args.required("--out");
-    if (!args.has("--bench")) {
-        std::printf("%s[%s]: %zu samples in, %zu out -> %s\n", op, impl, num_in, num_out,
-                    path.c_str());
+    if (!o.given("--bench")) {
+        std::printf("rfgpu %s (%s): %zu input samples, %zu outputs written to %s\n", d.op,
+                    d.impl.c_str(), d.num_in, d.num_out, o.text("--out").c_str());
         return;
     }
     const BenchResult& r = bench.result();
-    std::printf("{\"op\": \"%s\", \"impl\": \"%s\", \"gpu\": \"%s\", \"num_in\": %zu, "
-                "\"num_out\": %zu, \"runs\": %d, \"warmup\": %d, "
-                "\"h2d_ms\": {\"mean\": %.6f, \"std\": %.6f}, "
-                "\"kernel_ms\": {\"mean\": %.6f, \"std\": %.6f}, "
-                "\"d2h_ms\": {\"mean\": %.6f, \"std\": %.6f}}\n",
-                op, impl, gpu_name().c_str(), num_in, num_out, bench.config().runs,
-                bench.config().warmup, r.h2d.mean_ms, r.h2d.std_ms, r.kernel.mean_ms,
-                r.kernel.std_ms, r.d2h.mean_ms, r.d2h.std_ms);
+    Json j;
+    j.put("op", d.op).put("impl", d.impl).put("gpu", Device::current().prop.name);
+    j.put("num_in", d.num_in).put("num_out", d.num_out);
+    j.put("runs", bench.config().runs).put("warmup", bench.config().warmup);
+    j.put("h2d_ms", r.h2d).put("kernel_ms", r.kernel).put("d2h_ms", r.d2h);
+    std::printf("%s\n", j.str().c_str());
 }
 
-int run_fir(int argc, char** argv)
+// Rejects inputs whose element count does not fit the library's int lengths.
+void fits_int(std::size_t n, const char* what)
 {
-    const Args args(argc, argv,
-                    {"--in", "--taps", "--out", "--impl", "--block", "--bench", "--warmup"});
-    args.required("--out");
-    const Impl<FirFn>& impl = find_impl(fir_impls(), args, "fir");
-    const int block = args.integer("--block", kDefaultFirBlock, 32);
-    if (block % 32 != 0 || block > 1024) {
-        throw UsageError("--block needs a multiple of 32 up to 1024, got " +
-                         std::to_string(block));
+    if (n > static_cast<std::size_t>(INT_MAX)) {
+        throw std::runtime_error(std::string(what) + ": " + std::to_string(n) +
+                                 " elements exceed the limit of " + std::to_string(INT_MAX));
     }
-    Bench bench(bench_config(args));
-    // Integer recordings go to the device as stored and are converted there (a half or a
-    // quarter of the upload); the results are those of converting on the host first.
-    StoredSamples stored = read_stored(args.required("--in"));
-    const std::vector<float> taps = read_f32(args.required("--taps"));
-    if (taps.empty()) {
-        throw std::runtime_error(args.required("--taps") + ": no taps");
-    }
-    require_int_range(stored.count, "fir input");
-    require_int_range(taps.size(), "tap array");
-    const std::size_t num_in = stored.count;
-    std::vector<cf32> y;
-    if (num_in > 0 && stored.format != SampleFormat::Cf32) {
-        y = fir_stored(impl.name, stored, taps, block, bench);
-    } else if (num_in > 0) {
-        const std::vector<cf32> x = to_cf32(stored);
-        stored.bytes = std::vector<std::uint8_t>();
-        y = impl.fn(x, taps, block, bench);
-    }
-    finish(args, "fir", impl.name, num_in, y, bench);
-    return 0;
 }
 
-int run_channelize(int argc, char** argv)
+std::vector<float> taps_from(const Options& o)
 {
-    const Args args(argc, argv, {"--in", "--taps", "--channels", "--out", "--impl", "--output",
-                                 "--bench", "--warmup"});
-    args.required("--out");
-    if (!args.has("--channels")) {
-        throw UsageError("missing required option --channels");
-    }
-    const int channels = args.integer("--channels", 0, 1);
-    const Impl<ChanFn>& impl = find_impl(channelize_impls(), args, "channelize");
-    const std::string output = args.optional("--output", "complex");
-    if (output != "complex" && output != "magnitude") {
-        throw UsageError("unknown --output '" + output + "' (available: complex, magnitude)");
-    }
-    Bench bench(bench_config(args));
-    StoredSamples stored = read_stored(args.required("--in"));
-    const std::vector<float> taps = read_f32(args.required("--taps"));
+    std::vector<float> taps = read_f32(o.text("--taps"));
     if (taps.empty()) {
-        throw std::runtime_error(args.required("--taps") + ": no taps");
+        throw std::runtime_error(o.text("--taps") + ": the tap file holds no taps");
     }
-    require_int_range(stored.count + static_cast<std::size_t>(channels),
-                      "padded channelizer input");
-    require_int_range(taps.size(), "tap array");
-    if (stored.format != SampleFormat::Cf32) {
-        // Integer recordings go to the device as stored and are converted there.
-        std::vector<cf32> z;
-        std::vector<float> mag;
-        channelize_stored(impl.name, stored, taps, channels, output == "magnitude", z, mag, bench);
-        if (output == "magnitude") {
-            finish_f32(args, "channelize", impl.name, stored.count, mag, bench);
-        } else {
-            finish(args, "channelize", impl.name, stored.count, z, bench);
+    fits_int(taps.size(), "taps");
+    return taps;
+}
+
+template <class Fn>
+const Impl<Fn>& impl_named(const std::vector<Impl<Fn>>& table, const Options& o)
+{
+    const std::string name = o.text_or("--impl", table.front().name);
+    for (const Impl<Fn>& row : table) {
+        if (name == row.name) {
+            return row;
         }
-        return 0;
     }
-    const std::vector<cf32> x = to_cf32(stored);
-    stored.bytes = std::vector<std::uint8_t>();
-    if (output == "magnitude") {
-        finish_f32(args, "channelize", impl.name, x.size(),
-                   channelize_magnitude(impl.name, x, taps, channels, bench), bench);
-        return 0;
+    throw UsageError("no implementation named '" + name + "'");  // parse() checked it already
+}
+
+// --- the subcommands --------------------------------------------------------------------------
+
+int do_fir(const Options& o)
+{
+    const Impl<FirFn>& impl = impl_named(fir_impls(), o);
+    const int block = o.count_or("--block", kDefaultFirBlock);
+    Bench bench(o.bench());
+    StoredSamples x = read_stored(o.text("--in"));
+    const std::vector<float> taps = taps_from(o);
+    fits_int(x.count, "fir input");
+    std::vector<cf32> y;
+    if (x.count > 0 && x.format != SampleFormat::Cf32) {
+        // Integer recordings are uploaded as stored and converted in the kernels' load stage.
+        y = fir_stored(impl.name, x, taps, block, bench);
+    } else if (x.count > 0) {
+        const std::vector<cf32> samples = to_cf32(x);
+        x.bytes.clear();
+        x.bytes.shrink_to_fit();
+        y = impl.fn(samples, taps, block, bench);
     }
-    finish(args, "channelize", impl.name, x.size(), impl.fn(x, taps, channels, bench), bench);
+    write_cf32(o.text("--out"), y);
+    report(o, {"fir", impl.name, x.count, y.size()}, bench);
     return 0;
 }
 
-// |x| of every sample (src/main.cpp:255-267).
-int run_magnitude(int argc, char** argv)
+int do_channelize(const Options& o)
 {
-    const Args args(argc, argv, {"--in", "--out", "--bench", "--warmup"});
-    args.required("--out");
-    Bench bench(bench_config(args));
-    const std::vector<cf32> x = read_cf32(args.required("--in"));
-    require_int_range(x.size(), "magnitude input");
+    const Impl<ChanFn>& impl = impl_named(channelize_impls(), o);
+    const int channels = o.count_or("--channels", 1);
+    const bool magnitude = o.text_or("--output", "complex") == "magnitude";
+    Bench bench(o.bench());
+    StoredSamples x = read_stored(o.text("--in"));
+    const std::vector<float> taps = taps_from(o);
+    fits_int(x.count + static_cast<std::size_t>(channels), "channelizer input with padding");
+    std::vector<cf32> z;
+    std::vector<float> mag;
+    if (x.format != SampleFormat::Cf32) {
+        channelize_stored(impl.name, x, taps, channels, magnitude, z, mag, bench);
+    } else {
+        const std::vector<cf32> samples = to_cf32(x);
+        x.bytes.clear();
+        x.bytes.shrink_to_fit();
+        if (magnitude) {
+            mag = channelize_magnitude(impl.name, samples, taps, channels, bench);
+        } else {
+            z = impl.fn(samples, taps, channels, bench);
+        }
+    }
+    if (magnitude) {
+        write_f32(o.text("--out"), mag);
+    } else {
+        write_cf32(o.text("--out"), z);
+    }
+    report(o, {"channelize", impl.name, x.count, magnitude ? mag.size() : z.size()}, bench);
+    return 0;
+}
+
+// |x| of every sample (the project's magnitude subcommand, src/main.cpp:255-267).
+int do_magnitude(const Options& o)
+{
+    Bench bench(o.bench());
+    const std::vector<cf32> x = read_cf32(o.text("--in"));
+    fits_int(x.size(), "magnitude input");
     const std::vector<float> mag = x.empty() ? std::vector<float>() : magnitude_cuda(x, bench);
-    finish_f32(args, "magnitude", "elementwise", x.size(), mag, bench);
+    write_f32(o.text("--out"), mag);
+    report(o, {"magnitude", "elementwise", x.size(), mag.size()}, bench);
     return 0;
 }
 
-// Streamed FIR (stream.hpp). Without --bench: one pass, written to --out. With --bench N: W
-// untimed passes, then N timed ones, reported as JSON with the throughput against --rate (or
-// the input's sample rate from its metadata).
-int run_stream(int argc, char** argv)
+// The streamed FIR. Without --bench: one pass written to --out. With --bench N: W untimed
+// passes and N timed ones (wall clock of whole passes), reported with the throughput against
+// --rate or the input's own sample rate.
+int do_stream(const Options& o)
 {
-    const Args args(argc, argv, {"--in", "--taps", "--out", "--impl", "--chunk", "--depth",
-                                 "--memory", "--rate", "--bench", "--warmup"});
-    args.required("--out");
     StreamConfig config;
-    const std::string impl = args.optional("--impl", "tiled");
-    if (!parse_fir_impl(impl.c_str(), config.impl)) {
-        throw UsageError("unknown --impl '" + impl + "' for stream (available: " +
-                         impl_names(fir_impls(), ", ") + ")");
-    }
-    const std::string memory = args.optional("--memory", "copy");
-    if (!parse_stream_memory(memory, config.memory)) {
-        throw UsageError("unknown --memory '" + memory +
-                         "' (available: copy, registered, zero-copy)");
-    }
-    config.chunk = args.integer("--chunk", config.chunk, 1);
-    config.depth = args.integer("--depth", config.depth, 1);
-    const BenchConfig bench = bench_config(args);
-    // Integer recordings stream as stored (half or a quarter of the bytes over the host link)
-    // and are converted on the GPU, with the bits of streaming the converted samples.
-    const StoredSamples x = read_stored(args.required("--in"));
-    const std::vector<float> taps = read_f32(args.required("--taps"));
-    if (taps.empty()) {
-        throw std::runtime_error(args.required("--taps") + ": no taps");
-    }
-    require_int_range(x.count, "stream input");
-    require_int_range(static_cast<std::size_t>(config.chunk) + taps.size(), "chunk with history");
-    double rate = sample_rate(args.required("--in"));
-    if (args.has("--rate")) {
-        rate = std::stod(args.required("--rate"));
-    }
-    std::vector<double> times;
+    const std::string impl = o.text_or("--impl", "tiled");
+    parse_fir_impl(impl.c_str(), config.impl);  // parse() checked the name
+    const std::string memory = o.text_or("--memory", "copy");
+    parse_stream_memory(memory, config.memory);
+    config.chunk = o.count_or("--chunk", config.chunk);
+    config.depth = o.count_or("--depth", config.depth);
+    const BenchConfig plan = o.bench();
+    // Integer recordings stream as stored and are converted on the GPU.
+    const StoredSamples x = read_stored(o.text("--in"));
+    const std::vector<float> taps = taps_from(o);
+    fits_int(x.count, "stream input");
+    fits_int(static_cast<std::size_t>(config.chunk) + taps.size(), "chunk with its history");
+    const double rate = o.given("--rate") ? o.real("--rate") : sample_rate(o.text("--in"));
+
+    const bool timed = o.given("--bench");
+    const int passes = timed ? plan.warmup + plan.runs : 1;
+    std::vector<double> pass_ms;
     std::vector<cf32> y;
     StreamTiming timing;
-    const int passes = args.has("--bench") ? bench.warmup + bench.runs : 1;
     for (int i = 0; i < passes; ++i) {
         y = fir_stream(x, taps, config, timing);
-        if (i >= passes - bench.runs) {
-            times.push_back(timing.total_ms);
+        if (timed && i >= plan.warmup) {
+            pass_ms.push_back(timing.total_ms);
         }
     }
-    write_cf32(args.required("--out"), y);
-    if (!args.has("--bench")) {
-        std::printf("stream[%s]: %zu samples in %d chunks of %d, depth %d -> %s\n", impl.c_str(),
-                    x.count, timing.chunks, config.chunk, config.depth,
-                    args.required("--out").c_str());
+    write_cf32(o.text("--out"), y);
+    if (!timed) {
+        std::printf("rfgpu stream (%s): %zu input samples in %d chunks of %d through %d slots, "
+                    "written to %s\n",
+                    impl.c_str(), x.count, timing.chunks, config.chunk, config.depth,
+                    o.text("--out").c_str());
         return 0;
     }
-    double mean = 0.0;
-    for (double t : times) {
-        mean += t / static_cast<double>(times.size());
+    PhaseTime total;
+    for (double t : pass_ms) {
+        total.mean_ms += t / static_cast<double>(pass_ms.size());
     }
-    double var = 0.0;
-    for (double t : times) {
-        var += (t - mean) * (t - mean);
+    if (pass_ms.size() > 1) {
+        double ss = 0.0;
+        for (double t : pass_ms) {
+            ss += (t - total.mean_ms) * (t - total.mean_ms);
+        }
+        total.std_ms = std::sqrt(ss / static_cast<double>(pass_ms.size() - 1));
     }
-    const double std_ms =
-        times.size() > 1 ? std::sqrt(var / static_cast<double>(times.size() - 1)) : 0.0;
-    const double msps = mean > 0 ? static_cast<double>(x.count) / (mean * 1e3) : 0.0;
-    std::printf("{\"op\": \"stream\", \"impl\": \"%s\", \"memory\": \"%s\", \"gpu\": \"%s\", "
-                "\"num_in\": %zu, \"chunk\": %d, \"depth\": %d, \"chunks\": %d, \"runs\": %d, "
-                "\"warmup\": %d, \"total_ms\": {\"mean\": %.6f, \"std\": %.6f}, \"msps\": %.3f, "
-                "\"sample_rate\": %.1f, \"realtime_factor\": %.3f}\n",
-                impl.c_str(), memory.c_str(), gpu_name().c_str(), x.count, config.chunk,
-                config.depth, timing.chunks, bench.runs, bench.warmup, mean, std_ms, msps, rate,
-                rate > 0 ? msps * 1e6 / rate : 0.0);
+    const double msps = total.mean_ms > 0 ? static_cast<double>(x.count) / total.mean_ms / 1e3
+                                          : 0.0;
+    Json j;
+    j.put("op", "stream").put("impl", impl).put("memory", memory);
+    j.put("gpu", Device::current().prop.name).put("num_in", x.count);
+    j.put("chunk", config.chunk).put("depth", config.depth).put("chunks", timing.chunks);
+    j.put("runs", plan.runs).put("warmup", plan.warmup).put("total_ms", total);
+    j.put("msps", msps).put("sample_rate", rate);
+    j.put("realtime_factor", rate > 0 ? msps * 1e6 / rate : 0.0);
+    std::printf("%s\n", j.str().c_str());
     return 0;
 }
 
-std::string version_string(int packed)
+int do_info(const Options&)
 {
-    return std::to_string(packed / 1000) + "." + std::to_string((packed % 1000) / 10);
+    const Device d = Device::current();
+    const Json impls = Json()
+                           .put("fir", fir_names())
+                           .put("channelize", chan_names())
+                           .put("magnitude", std::vector<std::string>{"elementwise"});
+    Json j;
+    j.put("gpu", d.prop.name);
+    j.put("compute_capability",
+          std::to_string(d.prop.major) + "." + std::to_string(d.prop.minor));
+    j.put("memory_mb", static_cast<std::size_t>(d.prop.totalGlobalMem >> 20));
+    j.put("sms", d.prop.multiProcessorCount);
+    j.put("cuda_runtime", cuda_version(d.runtime)).put("cuda_driver", cuda_version(d.driver));
+    j.put("library", rfx_version()).raw("impls", impls.str());
+    std::printf("%s\n", j.str().c_str());
+    return 0;
 }
 
-int run_info(int argc, char** argv)
+struct Command {
+    const char* name;
+    const char* purpose;
+    std::vector<Flag> flags;
+    int (*handler)(const Options&);
+};
+
+std::vector<Flag> with_bench(std::vector<Flag> flags)
 {
-    const Args args(argc, argv, {});
-    int device = 0;
-    CUDA_CHECK(cudaGetDevice(&device));
-    cudaDeviceProp prop{};
-    CUDA_CHECK(cudaGetDeviceProperties(&prop, device));
-    int runtime = 0;
-    int driver = 0;
-    CUDA_CHECK(cudaRuntimeGetVersion(&runtime));
-    CUDA_CHECK(cudaDriverGetVersion(&driver));
-    std::printf("{\"gpu\": \"%s\", \"compute_capability\": \"%d.%d\", \"memory_mb\": %zu, "
-                "\"sms\": %d, \"cuda_runtime\": \"%s\", \"cuda_driver\": \"%s\", "
-                "\"library\": \"%s\", "
-                "\"impls\": {\"fir\": [\"%s\"], \"channelize\": [\"%s\"], "
-                "\"magnitude\": [\"elementwise\"]}}\n",
-                prop.name, prop.major, prop.minor, prop.totalGlobalMem / (1024 * 1024),
-                prop.multiProcessorCount, version_string(runtime).c_str(),
-                version_string(driver).c_str(), rfx_version(),
-                impl_names(fir_impls(), "\", \"").c_str(),
-                impl_names(channelize_impls(), "\", \"").c_str());
-    return 0;
+    flags.push_back(count_flag("--bench", "N", 1));
+    flags.push_back(count_flag("--warmup", "W", 0, INT_MAX, 1, false, "--bench"));
+    return flags;
+}
+
+const std::vector<Command>& commands()
+{
+    static const std::vector<Command> table = {
+        {"fir", "complex FIR filter, one output per input sample",
+         with_bench({path_flag("--in", "X.cf32", true), path_flag("--taps", "H.f32", true),
+                     path_flag("--out", "OUT.cf32", true),
+                     word_flag("--impl", "NAME", fir_names),
+                     count_flag("--block", "B", 32, 1024, 32)}),
+         do_fir},
+        {"channelize", "polyphase channelizer, frame-major channels (magnitude: |z| as float32)",
+         with_bench({path_flag("--in", "X.cf32", true), path_flag("--taps", "H.f32", true),
+                     count_flag("--channels", "M", 1, INT_MAX, 1, true),
+                     path_flag("--out", "OUT", true), word_flag("--impl", "NAME", chan_names),
+                     word_flag("--output", "complex|magnitude", output_names)}),
+         do_channelize},
+        {"magnitude", "|x| of every sample as float32",
+         with_bench({path_flag("--in", "X.cf32", true), path_flag("--out", "OUT.f32", true)}),
+         do_magnitude},
+        {"stream", "FIR in chunks through a ring of D pinned buffers and CUDA streams",
+         with_bench({path_flag("--in", "X.cf32", true), path_flag("--taps", "H.f32", true),
+                     path_flag("--out", "OUT.cf32", true),
+                     word_flag("--impl", "NAME", fir_names), count_flag("--chunk", "N", 1),
+                     count_flag("--depth", "D", 1),
+                     word_flag("--memory", "copy|registered|zero-copy", memory_names),
+                     real_flag("--rate", "HZ")}),
+         do_stream},
+        {"info", "GPU, CUDA versions and implementations as JSON", {}, do_info},
+    };
+    return table;
+}
+
+template <class Fn>
+void list_impls(const char* command, const std::vector<Impl<Fn>>& table)
+{
+    for (std::size_t i = 0; i < table.size(); ++i) {
+        std::fprintf(stderr, "  %-11s --impl %-12s %s%s\n", command, table[i].name,
+                     table[i].summary, i == 0 ? "  [default]" : "");
+    }
+}
+
+void usage()
+{
+    std::fprintf(stderr, "usage: rfgpu COMMAND [--option value ...]\n\ncommands:\n");
+    for (const Command& c : commands()) {
+        std::string line = std::string("  rfgpu ") + c.name;
+        for (const Flag& f : c.flags) {
+            if (std::string(f.name) == "--bench" || std::string(f.name) == "--warmup") {
+                continue;
+            }
+            const std::string item = std::string(f.name) + " " + f.meta;
+            line += f.required ? " " + item : " [" + item + "]";
+        }
+        std::fprintf(stderr, "%s\n      %s\n", line.c_str(), c.purpose);
+    }
+    std::fprintf(stderr,
+                 "\nSample inputs: .cf32 files or SigMF recordings (NAME.sigmf-meta or "
+                 "NAME.sigmf-data)\nin cf32_le, ci16_le or ci8; integer recordings are "
+                 "converted on the GPU.\n"
+                 "Timing (fir, channelize, magnitude, stream): --bench N times N runs after "
+                 "--warmup W\n(default 3) untimed ones and prints JSON.\n\nimplementations:\n");
+    list_impls("fir", fir_impls());
+    list_impls("channelize", channelize_impls());
 }
 
 }  // namespace
 
 int main(int argc, char** argv)
 {
+    const std::string name = argc > 1 ? argv[1] : "";
     try {
-        const std::string op = argc > 1 ? argv[1] : "";
-        if (op == "fir") return run_fir(argc, argv);
-        if (op == "channelize") return run_channelize(argc, argv);
-        if (op == "stream") return run_stream(argc, argv);
-        if (op == "magnitude") return run_magnitude(argc, argv);
-        if (op == "info") return run_info(argc, argv);
-        if (op == "--help" || op == "-h" || op == "help") {
-            print_usage();
+        if (name == "--help" || name == "-h" || name == "help") {
+            usage();
             return 0;
         }
-        throw UsageError(op.empty() ? "missing subcommand" : "unknown subcommand '" + op + "'");
+        const auto& table = commands();
+        const auto c = std::find_if(table.begin(), table.end(),
+                                    [&](const Command& row) { return name == row.name; });
+        if (c == table.end()) {
+            throw UsageError(name.empty() ? "no command given"
+                                          : "'" + name + "' is not a command");
+        }
+        const std::vector<std::string> words(argv + std::min(argc, 2), argv + argc);
+        return c->handler(parse(c->name, c->flags, words));
     } catch (const UsageError& e) {
         std::fprintf(stderr, "rfgpu: %s\n\n", e.what());
-        print_usage();
+        usage();
         return 2;
     } catch (const std::exception& e) {
         std::fprintf(stderr, "rfgpu: %s\n", e.what());

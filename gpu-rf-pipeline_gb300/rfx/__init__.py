@@ -60,6 +60,7 @@ SIGNATURES = {
     "rfx_fir_launch": (_I, [_I, _VP, _VP, _VP, _I64, _I, _VP]),
     "rfx_fir_launch_format": (_I, [_I, _I, _VP, _VP, _VP, _I64, _I, _VP]),
     "rfx_fir_device": (_I, [_I, _VP, _VP, _VP, _I64, _I]),
+    "rfx_fir_impl_used": (_I, [_I, _I, _I64, _I, ctypes.POINTER(_I)]),
     "rfx_fir_load_const_taps": (_I, [_VP, _I, _VP]),
     "rfx_fir_batched_device": (_I, [_I, ctypes.POINTER(_VP), ctypes.POINTER(_VP),
                                     ctypes.POINTER(_I64), _I, _VP, _I, _VP]),
@@ -130,6 +131,15 @@ def parse_fir_impl(name: str) -> int:
     out = ctypes.c_int()
     _check(load().rfx_parse_fir_impl(name.encode(), ctypes.byref(out)))
     return out.value
+
+
+def fir_impl_used(impl, num_taps: int, num_samples: int, batch: bool = False) -> str:
+    """Name of the kernel ("plain" or "tc_split") a FIR call with these arguments runs
+    (rfx_fir_impl_used): auto resolved, and tc_split's hand-offs to the plain kernel shown."""
+    out = ctypes.c_int()
+    _check(load().rfx_fir_impl_used(_impl(impl), int(num_taps), int(num_samples), int(batch),
+                                    ctypes.byref(out)))
+    return "tc_split" if out.value == FIR_TC else "plain"
 
 
 def parse_chan_impl(name: str) -> int:

@@ -49,7 +49,9 @@ typedef enum rfx_fir_impl {
     RFX_FIR_PLAIN = 0,
     /* Tensor-core kernel (tcgen05): the FIR as a block-Toeplitz GEMM in split FP16
      * (hi + lo operands, three products, FP32 accumulation in tensor memory) with one
-     * power-of-two scale per tile. Tolerance-tested, not bit-exact; one tap uses RFX_FIR_PLAIN. */
+     * power-of-two scale per tile. Tolerance-tested, not bit-exact. Calls it cannot take run
+     * RFX_FIR_PLAIN instead: one tap, more than 3457 taps (the shared-memory budget), fewer
+     * than 128 samples; rfx_fir_impl_used() says in advance which kernel a call runs. */
     RFX_FIR_TC = 1,
     /* Chooses per call from the tuned table (rfx_autotune) or a built-in rule. */
     RFX_FIR_AUTO = 2
@@ -98,6 +100,13 @@ int rfx_parse_chan_impl(const char* name, int* impl);
  * Replaces fir_launch (src/device_ops.hpp:88-89). */
 int rfx_fir_launch(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
                    int num_taps, cudaStream_t stream);
+
+/* Which kernel rfx_fir_launch (batch == 0) or rfx_fir_batch_launch (batch != 0, for one
+ * capture) runs for these arguments: writes RFX_FIR_PLAIN or RFX_FIR_TC to *used. Resolves
+ * RFX_FIR_AUTO through the tuned table, and reports where RFX_FIR_TC hands a call to the plain
+ * kernel (see RFX_FIR_TC; the batch kernel's budget is smaller). Host-only, no GPU work.
+ * No counterpart in the project, whose --impl always names the kernel that runs. */
+int rfx_fir_impl_used(int impl, int num_taps, int64_t num_samples, int batch, int* used);
 
 /* rfx_fir_launch on the legacy default stream. Replaces fir_device (src/device_ops.hpp:81-82). */
 int rfx_fir_device(int impl, const void* x, const float* taps, void* y, int64_t num_samples,
@@ -216,8 +225,10 @@ int rfx_magnitude_launch(const void* x, float* mag, int64_t num_samples, cudaStr
  * start-up: a memory budget fixed at initialization, a device allocator owned by another
  * framework, or no room for the implicit synchronization of cudaMalloc and cudaFree.
  * The FIRST call on each device builds that operand on `stream` and waits for it
- * (cudaStreamSynchronize); make it during initialization, before any stream capture. Later
- * calls only enqueue the kernel. The array is read-only after the first call, so calls may
+ * (cudaStreamSynchronize); make it during initialization, before any stream capture (a first
+ * call on a capturing stream returns RFX_ERR_INVALID and leaves the capture intact). Later
+ * calls only enqueue the kernel. cudaDeviceReset clears the array; the next call notices the
+ * new CUDA context and builds the operand again, as a first call. The array is read-only after the first call, so calls may
  * overlap; concurrent first calls on one device are serialized by a lock.
  * channels must be 64 (RFX_ERR_CAPACITY otherwise: the array holds that operand only);
  * num_samples 0 or at least 64 (one frame); taps as for the RFX_CHAN_TC plan.

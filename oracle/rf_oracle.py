@@ -232,3 +232,13 @@ def per_channel_error(z: np.ndarray, ref: np.ndarray) -> np.ndarray:
     with np.errstate(divide="ignore", invalid="ignore"):
         return np.where(scale > 0, diff / np.where(scale > 0, scale, 1.0),
                         np.where(diff > 0, np.inf, 0.0))
+
+
+def fir_convolve(x: np.ndarray, taps: np.ndarray) -> np.ndarray:
+    """``fir`` by the project's own method (tools/reference.py:103-111): the first len(x)
+    samples of NumPy's full convolution in float64, on one core. Timed as the CPU baseline of
+    the project's implementation; same values as ``fir`` to rounding."""
+    x = np.asarray(x)
+    if x.size == 0:
+        return np.zeros(0, dtype=np.complex128)
+    return np.convolve(x.astype(np.complex128), np.asarray(taps, dtype=np.float64))[: x.size]

@@ -4,7 +4,7 @@ float64 reference (tools/reference.py, imported unchanged from a checkout of tha
 
 Run where the project is checked out (it is not needed anywhere else):
 
-    python tests/golden/make_golden.py --reference /root/reference
+    python tests/golden/make_golden.py --reference PATH/TO/gpu-rf-pipeline
 
 Writes, next to this script:
 
@@ -66,7 +66,8 @@ def random_complex(seed: int, n: int) -> np.ndarray:
 
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("--reference", type=Path, default=Path("/root/reference"))
+    ap.add_argument("--reference", type=Path, required=True,
+                    help="checkout of the gpu-rf-pipeline project (holds tools/reference.py)")
     args = ap.parse_args()
     sys.path.insert(0, str(args.reference / "tools"))
     import reference  # noqa: E402  (the project's tools/reference.py, unchanged)

@@ -148,3 +148,23 @@ def test_channelize_format_argument_errors(lib) -> None:
     assert lib.rfx_channelize_host_format(0, 4, 0, None, 10, None, 5, 4, None, None) == 1
     assert lib.rfx_channelize_host_format(0, 1, 0, None, 10, None, 5, 0, None, None) == 1
     assert lib.rfx_fir_stream_format(9, None, 10, None, 5, None, None, None, None) == 1
+
+
+def test_impl_used_reports_the_kernel_that_runs(lib) -> None:
+    # tc_split hands calls it cannot take to the plain kernel; the query says so in advance.
+    assert rfx.fir_impl_used("tc_split", 1025, 1 << 24) == "tc_split"
+    assert rfx.fir_impl_used("tc_split", 1, 1 << 24) == "plain"          # one tap
+    assert rfx.fir_impl_used("tc_split", 3458, 1 << 24) == "plain"       # beyond the budget
+    assert rfx.fir_impl_used("tc_split", 3457, 1 << 24) == "tc_split"
+    assert rfx.fir_impl_used("tc_split", 1025, 127) == "plain"           # under one block
+    assert rfx.fir_impl_used("plain", 1025, 1 << 24) == "plain"
+    for name in ["naive", "tiled", "tiled_const", "register"]:
+        assert rfx.fir_impl_used(name, 1025, 1 << 24) == "plain"
+    # auto's built-in rule: the tensor core from 160 taps and 2^16 samples.
+    assert rfx.fir_impl_used("auto", 1025, 1 << 24) == "tc_split"
+    assert rfx.fir_impl_used("auto", 63, 1 << 24) == "plain"
+    assert rfx.fir_impl_used("auto", 1025, 1 << 12) == "plain"
+    with pytest.raises(rfx.RfxError):
+        rfx.fir_impl_used("tc_split", 0, 100)
+    with pytest.raises(rfx.RfxError):
+        rfx.fir_impl_used(7, 10, 100)

@@ -150,3 +150,32 @@ def test_tc_host_path() -> None:
     y, bench = rfx.fir_host("tc_split", x, h, warmup=1, runs=2)
     assert orc.normwise_error(y, orc.fir_fast(x, h)) <= TC_NORMWISE
     assert bench.kernel_ms_mean > 0
+
+
+@pytest.mark.parametrize("k", [255, 1025])
+def test_tc_sixty_db_level_steps_per_block(k: int) -> None:
+    # Every 128-output block at its own level, 1 or 1e-3 at random (60 dB steps inside every
+    # tile, the workload's dynamic range). The split operands are floating point, so a quiet
+    # sample keeps its relative precision under its tile's scale; each output block is held to
+    # 2e-6 of its own level, or, where an output block's own level is far below the inputs that
+    # reach it through the taps, to within 4x of the exact FP32 chain's error there (the plain
+    # kernel's, which no float32 arithmetic beats by much).
+    n = 40 * TILE // 8
+    rng = np.random.default_rng(k)
+    x = signals.to_cf32(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    levels = np.where(rng.random(n // 128) < 0.5, 1.0, 1e-3)
+    x = (x * np.repeat(levels, 128).astype(np.float32)).astype(np.complex64)
+    h = signals.long_fir(1 << 12).taps if k == 1025 else rand_case(1, k, seed=k)[1]
+    ref = orc.fir_fast(x, h)
+    y_tc = run(x, h)
+    y_plain = run(x, h, impl="plain")
+    blocks = n // 128
+
+    def per_block(y):
+        d = np.abs(y.astype(np.complex128) - ref).reshape(blocks, 128).max(axis=1)
+        return d / np.abs(ref).reshape(blocks, 128).max(axis=1)
+
+    e_tc, e_plain = per_block(y_tc), per_block(y_plain)
+    print(f"\nK={k}: tensor-core per-block error max {e_tc.max():.3g}, median "
+          f"{np.median(e_tc):.3g}; plain FP32 max {e_plain.max():.3g}")
+    assert np.all(e_tc <= np.maximum(TC_NORMWISE, 4 * e_plain))

@@ -249,3 +249,13 @@ def test_normwise_error_definition() -> None:
     y = ref + np.array([0.0, 1e-6, 0.0])
     assert orc.normwise_error(y, ref) == pytest.approx(0.25e-6)
     assert orc.normwise_error(np.zeros(3), np.zeros(3)) == 0.0
+
+
+def test_convolve_baseline_equals_the_direct_form() -> None:
+    # The CPU baseline's method (np.convolve, the project's tools/reference.py fir) gives the
+    # oracle's values.
+    rng = np.random.default_rng(7)
+    x = (rng.standard_normal(3000) + 1j * rng.standard_normal(3000)).astype(np.complex64)
+    h = rng.standard_normal(257).astype(np.float32)
+    np.testing.assert_allclose(orc.fir_convolve(x, h), orc.fir(x, h), rtol=1e-12, atol=1e-12)
+    assert orc.fir_convolve(x[:0], h).size == 0

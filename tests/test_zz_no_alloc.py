@@ -1,7 +1,16 @@
-"""rfx_channelize_tc_static (the 64-channel tensor-core channelizer with its twiddle operand in
-a static device array, no plan, no allocation) through the C ABI, against rfx_channelize_launch
-with an RFX_CHAN_TC plan on the same inputs: two calls in a row, each within 1e-6 normwise (the
-same kernel and operand, so normally identical). Collected last; also passes alone."""
+"""rfx_channelize_tc_static: the 64-channel tensor-core channelizer for callers that cannot
+allocate device memory once they are running (a memory budget fixed at start-up, a device
+allocator owned by another framework, or a loop that must not take cudaMalloc's implicit
+synchronization). Its twiddle operand lives in a static device array instead of a plan.
+
+Checked through the C ABI, two calls in a row on the same inputs:
+* against rfx_channelize_launch with an RFX_CHAN_TC plan (the same kernel and operand, so the
+  results agree to 1e-6 normwise and are normally identical);
+* against the float64 oracle at the tensor-core bar (2e-6 normwise), so that an operand laid
+  out wrongly in both paths would still fail;
+* that a call after the first leaves the device's free memory and PyTorch's reserved memory
+  unchanged (it allocates nothing).
+Collected last (a failure here leaves every other test already run); passes alone too."""
 from __future__ import annotations
 
 import ctypes
@@ -17,18 +26,19 @@ from rfx import signals
 pytestmark = pytest.mark.gpu
 
 DEV = torch.device("cuda:0")
+TC_NORMWISE = 2e-6
 RFX_ERR_INVALID, RFX_ERR_CAPACITY = 1, 2   # include/rfx.h status codes
 
 
-def call_static(lib, x, taps, out, n, channels=64):
+def call_static(lib, x, taps, out, n, channels=64, stream=0):
     return lib.rfx_channelize_tc_static(ctypes.c_void_p(x.data_ptr()),
                                         ctypes.c_void_p(taps.data_ptr()),
                                         ctypes.c_void_p(out.data_ptr()), n, taps.numel(),
-                                        channels, ctypes.c_void_p(0))
+                                        channels, ctypes.c_void_p(stream))
 
 
 @pytest.mark.parametrize("n,k", [(1 << 20, 1024), (8192 * 3 + 65, 1000)])
-def test_static_entry_matches_plan_entry(n: int, k: int) -> None:
+def test_static_entry_matches_plan_entry_and_oracle(n: int, k: int) -> None:
     lib = rfx.load()
     rng = np.random.default_rng(n + k)
     x = signals.to_cf32(rng.standard_normal(n) + 1j * rng.standard_normal(n))
@@ -41,12 +51,22 @@ def test_static_entry_matches_plan_entry(n: int, k: int) -> None:
         plan.launch(xd, hd, ref)
     torch.cuda.synchronize()
     want = ref.cpu().numpy()
-    for _ in range(2):
-        out = torch.full((frames, 64), float("nan"), dtype=torch.complex64, device=DEV)
+    exact = orc.channelize_fast(x, h, 64)
+    outs = [torch.full((frames, 64), float("nan"), dtype=torch.complex64, device=DEV)
+            for _ in range(2)]
+    for i, out in enumerate(outs):
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info(DEV)
+        reserved0 = torch.cuda.memory_reserved(DEV)
         assert call_static(lib, xd, hd, out, n) == rfx.RFX_OK, lib.rfx_last_error()
         torch.cuda.synchronize()
+        if i > 0:   # the first call on the device may still load the module's code
+            assert torch.cuda.mem_get_info(DEV)[0] == free0
+            assert torch.cuda.memory_reserved(DEV) == reserved0
         got = out.cpu().numpy()
         assert orc.normwise_error(got, want) <= 1e-6
+        assert orc.normwise_error(got, exact) <= TC_NORMWISE
+        assert float(orc.per_channel_error(got, exact).max()) <= TC_NORMWISE
     assert rfx.device_fault() == 0
 
 
