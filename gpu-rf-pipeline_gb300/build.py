@@ -22,6 +22,9 @@ CSRC = PKG / "csrc"
 HOST = PKG / "host"
 BUILD = PKG / "_build"
 LIB = PKG / "lib" / "librfx.so"
+# The C++ drop-in layer (host/*.cpp without the CLI's main): the project's device_ops.hpp /
+# ops.hpp / stream.hpp functions over the C ABI, for programs written against those headers.
+HOSTLIB = PKG / "lib" / "librfxhost.a"
 CLI = PKG / "bin" / "rfgpu"
 INCLUDE = ROOT / "include"
 
@@ -87,6 +90,14 @@ def build(verbose: bool = False) -> Path:
         if proc.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{proc.stderr}")
     host_objs = [BUILD / ("host_" + s.stem + ".o") for s in host_srcs]
+    layer_objs = [o for o in host_objs if o.name != "host_main.o"]
+    if layer_objs and (not HOSTLIB.exists()
+                       or HOSTLIB.stat().st_mtime < max(o.stat().st_mtime for o in layer_objs)):
+        HOSTLIB.unlink(missing_ok=True)
+        proc = subprocess.run(["ar", "rcs", str(HOSTLIB), *map(str, layer_objs)],
+                              capture_output=True, text=True)
+        if proc.returncode != 0:
+            raise RuntimeError(f"ar failed:\n{proc.stderr}")
     if host_objs and (not CLI.exists()
                       or CLI.stat().st_mtime < max(o.stat().st_mtime
                                                    for o in host_objs + [LIB])):

@@ -443,7 +443,7 @@ int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_p
     }
     *plan = nullptr;
     if (impl == RFX_CHAN_AUTO) {
-        impl = rfx::chan_tc_supported(channels, 1) ? RFX_CHAN_TC : RFX_CHAN_PLAIN;
+        impl = rfx::tuned_chan_impl(channels, max_samples);
     }
     if (impl != RFX_CHAN_PLAIN && impl != RFX_CHAN_TC) {
         return fail(RFX_ERR_INVALID, "channelize: unknown implementation %d", impl);

@@ -1,15 +1,27 @@
-// The tuned-configuration table: which FIR implementation RFX_FIR_AUTO runs and which tile
-// shape the tensor-core FIR uses, per (tap-count bucket, length bucket). Filled by timing the
-// candidates on the current device (rfx_autotune_fir), persisted as text keyed by GPU name
-// and driver version (rfx_autotune_save / rfx_autotune_load).
+// The tuned-configuration tables behind the `auto` implementations.
+//
+// * FIR: which implementation RFX_FIR_AUTO runs and which tile shape the tensor-core FIR uses,
+//   per (tap-count bucket, length bucket). rfx_fir_batch_launch's auto form places each capture
+//   by the same table, so tuning a capture's (taps, length) bucket tunes the batch's partition.
+// * Channelizer: which implementation RFX_CHAN_AUTO plans use, per (channel count, length
+//   bucket).
+//
+// Entries come from timing the candidates on the current device over seeded pseudo-random
+// inputs (rfx_autotune_fir, rfx_autotune_channelize); a lookup that finds none applies the
+// built-in rule. The tables are saved and loaded as text keyed by GPU name and driver version
+// (rfx_autotune_save / rfx_autotune_load); the file named by the environment variable
+// RFX_TUNE_FILE, if set, is loaded automatically before the first lookup.
 #include "rfx.h"
 #include "tuning.hpp"
+#include "chan_tc.cuh"
+#include "chan_wide.cuh"
 #include "fir_plain.cuh"
 #include "fir_tc.cuh"
 
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -21,9 +33,14 @@ namespace rfx {
 
 namespace {
 
-struct Entry {
+struct FirEntry {
     int impl;
     TcConfig config;
+    double ms;
+};
+
+struct ChanEntry {
+    int impl;
     double ms;
 };
 
@@ -39,17 +56,184 @@ int bucket(long long v)
 }
 
 std::mutex g_mutex;
-std::map<std::pair<int, int>, Entry> g_table;
+std::map<std::pair<int, int>, FirEntry> g_fir;    // (taps bucket, length bucket)
+std::map<std::pair<int, int>, ChanEntry> g_chan;  // (channels, length bucket)
 
-bool lookup(int num_taps, long long n, Entry* out)
+int load_table(const char* path);  // below; takes g_mutex
+
+// Loads $RFX_TUNE_FILE once, before the first lookup (a missing file is not an error).
+void load_environment_table()
 {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char* path = std::getenv("RFX_TUNE_FILE");
+        if (path != nullptr && path[0] != '\0') {
+            load_table(path);
+        }
+    });
+}
+
+bool lookup_fir(int num_taps, long long n, FirEntry* out)
+{
+    load_environment_table();
     std::lock_guard<std::mutex> lock(g_mutex);
-    const auto it = g_table.find({bucket(num_taps), bucket(n)});
-    if (it == g_table.end()) {
+    const auto it = g_fir.find({bucket(num_taps), bucket(n)});
+    if (it == g_fir.end()) {
         return false;
     }
     *out = it->second;
     return true;
+}
+
+bool lookup_chan(int channels, long long n, ChanEntry* out)
+{
+    load_environment_table();
+    std::lock_guard<std::mutex> lock(g_mutex);
+    const auto it = g_chan.find({channels, bucket(n)});
+    if (it == g_chan.end()) {
+        return false;
+    }
+    *out = it->second;
+    return true;
+}
+
+std::string device_key()
+{
+    int dev = 0;
+    cudaDeviceProp prop{};
+    int driver = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return "unknown";
+    }
+    cudaDriverGetVersion(&driver);
+    std::string name = prop.name;
+    for (char& ch : name) {
+        if (ch == ' ') {
+            ch = '_';
+        }
+    }
+    return name + "/" + std::to_string(driver);
+}
+
+// Text format, one entry per line:
+//   fir  <device key> <taps bucket> <length bucket> <impl> <tile blocks> <stages> <ms>
+//   chan <device key> <channels> <length bucket> <impl> <ms>
+int load_table(const char* path)
+{
+    FILE* f = std::fopen(path, "r");
+    if (f == nullptr) {
+        return RFX_ERR_INVALID;
+    }
+    const std::string key = device_key();
+    char line[512];
+    std::lock_guard<std::mutex> lock(g_mutex);
+    while (std::fgets(line, sizeof(line), f) != nullptr) {
+        char kind[8];
+        char dev[256];
+        int a, b, impl, blocks, stages;
+        double ms;
+        if (std::sscanf(line, "%7s %255s", kind, dev) != 2 || key != dev) {
+            continue;
+        }
+        if (std::strcmp(kind, "fir") == 0 &&
+            std::sscanf(line, "%*s %*s %d %d %d %d %d %lf", &a, &b, &impl, &blocks, &stages,
+                        &ms) == 6 &&
+            (impl == RFX_FIR_PLAIN || impl == RFX_FIR_TC)) {
+            g_fir[{a, b}] = FirEntry{impl, TcConfig{blocks, stages}, ms};
+        } else if (std::strcmp(kind, "chan") == 0 &&
+                   std::sscanf(line, "%*s %*s %d %d %d %lf", &a, &b, &impl, &ms) == 4 &&
+                   (impl == RFX_CHAN_PLAIN || impl == RFX_CHAN_TC)) {
+            g_chan[{a, b}] = ChanEntry{impl, ms};
+        }
+    }
+    std::fclose(f);
+    return RFX_OK;
+}
+
+// Seeded pseudo-random values in [-scale, scale): the tuner's inputs (timing on zeros could
+// flatter data-dependent paths such as the tensor-core FIR's per-tile scale search).
+__global__ void fill_kernel(float* p, long long count, unsigned seed, float scale)
+{
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += stride) {
+        unsigned h = static_cast<unsigned>(i) * 0x9E3779B1u ^ seed;
+        h ^= h >> 16;
+        h *= 0x85EBCA6Bu;
+        h ^= h >> 13;
+        h *= 0xC2B2AE35u;
+        h ^= h >> 16;
+        p[i] = scale * (static_cast<float>(h >> 8) * (1.0f / 8388608.0f) - 1.0f);
+    }
+}
+
+cudaError_t fill(void* p, long long floats, unsigned seed, float scale)
+{
+    fill_kernel<<<1024, 256>>>(static_cast<float*>(p), floats, seed, scale);
+    return cudaGetLastError();
+}
+
+// Scratch inputs for one tuning call: x and an output of `samples` cf32, `taps` floats.
+struct Scratch {
+    void* x = nullptr;
+    void* y = nullptr;
+    float* h = nullptr;
+
+    cudaError_t make(long long samples, long long out_samples, int taps)
+    {
+        cudaError_t err = cudaMalloc(&x, static_cast<size_t>(samples) * 8);
+        if (err == cudaSuccess) {
+            err = cudaMalloc(&y, static_cast<size_t>(out_samples) * 8);
+        }
+        if (err == cudaSuccess) {
+            err = cudaMalloc(&h, sizeof(float) * taps);
+        }
+        if (err == cudaSuccess) {
+            err = fill(x, 2 * samples, 0x5eedu, 1.0f);
+        }
+        if (err == cudaSuccess) {
+            err = fill(h, taps, 0x7a95u, 1.0f / static_cast<float>(taps));
+        }
+        if (err == cudaSuccess) {
+            err = cudaDeviceSynchronize();
+        }
+        return err;
+    }
+
+    ~Scratch()
+    {
+        cudaFree(x);
+        cudaFree(y);
+        cudaFree(h);
+    }
+};
+
+// Best of five timed runs after one untimed run; a negative value when `run` fails.
+template <class Run>
+double best_ms(Run run)
+{
+    if (run() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        return -1.0;
+    }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(a, nullptr);
+        run();
+        cudaEventRecord(b, nullptr);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        best = ms < best ? ms : best;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return best;
 }
 
 }  // namespace
@@ -60,8 +244,8 @@ bool lookup(int num_taps, long long n, Entry* out)
 // plain kernel otherwise.
 int tuned_fir_impl(int num_taps, long long n)
 {
-    Entry e;
-    if (lookup(num_taps, n, &e)) {
+    FirEntry e;
+    if (lookup_fir(num_taps, n, &e)) {
         return e.impl;
     }
     constexpr int kTcMinTaps = 160;
@@ -73,34 +257,38 @@ int tuned_fir_impl(int num_taps, long long n)
 
 TcConfig tuned_fir_tc_config(int num_taps, long long n)
 {
-    Entry e;
-    if (lookup(num_taps, n, &e) && e.impl == RFX_FIR_TC) {
+    FirEntry e;
+    if (lookup_fir(num_taps, n, &e) && e.impl == RFX_FIR_TC) {
         return e.config;
     }
     return TcConfig{96, 6};
 }
 
+// Built-in rule: the fused tensor-core form at 64 channels (one HBM pass against the plain
+// form's two); cuFFT's plain form elsewhere, including 1024 channels, where the branch-sum
+// kernel + cuFFT measured faster than the factored tensor-core DFT on GB300.
+int tuned_chan_impl(int channels, long long n)
+{
+    ChanEntry e;
+    if (lookup_chan(channels, n, &e)) {
+        return e.impl;
+    }
+    return chan_tc_supported(channels, 1) ? RFX_CHAN_TC : RFX_CHAN_PLAIN;
+}
+
 }  // namespace rfx
 
-extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, double* best_ms)
+extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, double* best_out)
 {
     using namespace rfx;
     if (num_taps < 1 || num_taps > kMaxTaps || num_samples < 1 || num_samples > INT32_MAX) {
         return RFX_ERR_INVALID;
     }
-    void* x = nullptr;
-    void* y = nullptr;
-    float* h = nullptr;
-    const size_t bytes = static_cast<size_t>(num_samples) * 8;
-    if (cudaMalloc(&x, bytes) != cudaSuccess || cudaMalloc(&y, bytes) != cudaSuccess ||
-        cudaMalloc(&h, sizeof(float) * num_taps) != cudaSuccess) {
-        cudaFree(x);
-        cudaFree(y);
-        cudaFree(h);
+    Scratch s;
+    if (s.make(num_samples, num_samples, num_taps) != cudaSuccess) {
+        cudaGetLastError();
         return RFX_ERR_CUDA;
     }
-    cudaMemset(x, 0, bytes);
-    cudaMemset(h, 0, sizeof(float) * num_taps);
     struct Candidate {
         int impl;
         TcConfig config;
@@ -117,74 +305,72 @@ extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, dou
             candidates.push_back({RFX_FIR_TC, TcConfig{kTcPairTile, st}});
         }
     }
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    Entry best{RFX_FIR_PLAIN, TcConfig{96, 6}, 1e30};
+    FirEntry best{RFX_FIR_PLAIN, TcConfig{96, 6}, 1e30};
     for (const Candidate& c : candidates) {
-        auto run = [&]() {
+        const double ms = best_ms([&]() {
             return c.impl == RFX_FIR_TC
-                       ? fir_tc_launch(x, h, y, num_samples, num_taps, c.config, nullptr)
-                       : fir_plain_launch(x, h, y, num_samples, num_taps, nullptr);
-        };
-        if (run() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
-            cudaGetLastError();
-            continue;  // a candidate this device cannot run is skipped
-        }
-        float best_c = 1e30f;
-        for (int rep = 0; rep < 5; ++rep) {
-            cudaEventRecord(a, nullptr);
-            run();
-            cudaEventRecord(b, nullptr);
-            cudaEventSynchronize(b);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, a, b);
-            best_c = ms < best_c ? ms : best_c;
-        }
-        if (best_c < best.ms) {
-            best = Entry{c.impl, c.config, best_c};
+                       ? fir_tc_launch(s.x, s.h, s.y, num_samples, num_taps, c.config, nullptr)
+                       : fir_plain_launch(s.x, s.h, s.y, num_samples, num_taps, nullptr);
+        });
+        if (ms >= 0 && ms < best.ms) {
+            best = FirEntry{c.impl, c.config, ms};
         }
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    cudaFree(x);
-    cudaFree(y);
-    cudaFree(h);
     if (best.ms >= 1e29) {
         return RFX_ERR_CUDA;
     }
     {
         std::lock_guard<std::mutex> lock(g_mutex);
-        g_table[{bucket(num_taps), bucket(num_samples)}] = best;
+        g_fir[{bucket(num_taps), bucket(num_samples)}] = best;
     }
-    if (best_ms != nullptr) {
-        *best_ms = best.ms;
+    if (best_out != nullptr) {
+        *best_out = best.ms;
     }
     return RFX_OK;
 }
 
-namespace {
-
-std::string device_key()
+extern "C" int rfx_autotune_channelize(int channels, int num_taps, int64_t num_samples,
+                                       double* best_out)
 {
-    int dev = 0;
-    cudaDeviceProp prop{};
-    int driver = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
-        return "unknown";
+    using namespace rfx;
+    if (channels < 1 || num_taps < 1 || num_samples < channels || num_samples > INT32_MAX) {
+        return RFX_ERR_INVALID;
     }
-    cudaDriverGetVersion(&driver);
-    std::string name = prop.name;
-    for (char& ch : name) {
-        if (ch == ' ') {
-            ch = '_';
+    const long long frames = rfx_channelize_frames(num_samples, channels);
+    Scratch s;
+    if (s.make(num_samples, frames * channels, num_taps) != cudaSuccess) {
+        cudaGetLastError();
+        return RFX_ERR_CUDA;
+    }
+    ChanEntry best{RFX_CHAN_PLAIN, 1e30};
+    for (int impl : {RFX_CHAN_PLAIN, RFX_CHAN_TC}) {
+        rfx_chan_plan* plan = nullptr;
+        if (rfx_chan_plan_create(impl, channels, num_samples, &plan) != RFX_OK) {
+            continue;  // e.g. no tensor-core form at this channel count
+        }
+        const double ms = best_ms([&]() {
+            return rfx_channelize_launch(plan, s.x, s.h, s.y, num_samples, num_taps, nullptr) ==
+                           RFX_OK
+                       ? cudaSuccess
+                       : cudaErrorUnknown;
+        });
+        rfx_chan_plan_destroy(plan);
+        if (ms >= 0 && ms < best.ms) {
+            best = ChanEntry{impl, ms};
         }
     }
-    return name + "/" + std::to_string(driver);
+    if (best.ms >= 1e29) {
+        return RFX_ERR_CUDA;
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        g_chan[{channels, bucket(num_samples)}] = best;
+    }
+    if (best_out != nullptr) {
+        *best_out = best.ms;
+    }
+    return RFX_OK;
 }
-
-}  // namespace
 
 extern "C" int rfx_autotune_save(const char* path)
 {
@@ -198,10 +384,14 @@ extern "C" int rfx_autotune_save(const char* path)
     }
     const std::string key = device_key();
     std::lock_guard<std::mutex> lock(g_mutex);
-    for (const auto& kv : g_table) {
-        std::fprintf(f, "%s %d %d %d %d %d %.6f\n", key.c_str(), kv.first.first, kv.first.second,
-                     kv.second.impl, kv.second.config.tile_blocks, kv.second.config.stages,
-                     kv.second.ms);
+    for (const auto& kv : g_fir) {
+        std::fprintf(f, "fir %s %d %d %d %d %d %.6f\n", key.c_str(), kv.first.first,
+                     kv.first.second, kv.second.impl, kv.second.config.tile_blocks,
+                     kv.second.config.stages, kv.second.ms);
+    }
+    for (const auto& kv : g_chan) {
+        std::fprintf(f, "chan %s %d %d %d %.6f\n", key.c_str(), kv.first.first, kv.first.second,
+                     kv.second.impl, kv.second.ms);
     }
     std::fclose(f);
     return RFX_OK;
@@ -209,25 +399,13 @@ extern "C" int rfx_autotune_save(const char* path)
 
 extern "C" int rfx_autotune_load(const char* path)
 {
-    using namespace rfx;
-    if (path == nullptr) {
-        return RFX_ERR_INVALID;
-    }
-    FILE* f = std::fopen(path, "r");
-    if (f == nullptr) {
-        return RFX_ERR_INVALID;
-    }
-    const std::string key = device_key();
-    char dev[256];
-    int tb, lb, impl, blocks, stages;
-    double ms;
-    std::lock_guard<std::mutex> lock(g_mutex);
-    while (std::fscanf(f, "%255s %d %d %d %d %d %lf", dev, &tb, &lb, &impl, &blocks, &stages,
-                       &ms) == 7) {
-        if (key == dev && (impl == RFX_FIR_PLAIN || impl == RFX_FIR_TC)) {
-            g_table[{tb, lb}] = Entry{impl, TcConfig{blocks, stages}, ms};
-        }
-    }
-    std::fclose(f);
+    return path == nullptr ? RFX_ERR_INVALID : rfx::load_table(path);
+}
+
+extern "C" int rfx_autotune_clear(void)
+{
+    std::lock_guard<std::mutex> lock(rfx::g_mutex);
+    rfx::g_fir.clear();
+    rfx::g_chan.clear();
     return RFX_OK;
 }

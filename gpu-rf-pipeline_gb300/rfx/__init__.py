@@ -87,6 +87,8 @@ SIGNATURES = {
     "rfx_channelize_host_format": (_I, [_I, _I, _I, _VP, _I64, _VP, _I, _I, _VP,
                                         ctypes.POINTER(Bench)]),
     "rfx_autotune_fir": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),
+    "rfx_autotune_channelize": (_I, [_I, _I, _I64, ctypes.POINTER(ctypes.c_double)]),
+    "rfx_autotune_clear": (_I, []),
     "rfx_autotune_save": (_I, [ctypes.c_char_p]),
     "rfx_autotune_load": (_I, [ctypes.c_char_p]),
 }
@@ -462,3 +464,21 @@ def autotune_fir(impl, num_taps: int, num_samples: int) -> float:
     ms = ctypes.c_double()
     _check(load().rfx_autotune_fir(_impl(impl), num_taps, num_samples, ctypes.byref(ms)))
     return ms.value
+
+
+def autotune_channelize(channels: int, num_taps: int, num_samples: int) -> float:
+    ms = ctypes.c_double()
+    _check(load().rfx_autotune_channelize(channels, num_taps, num_samples, ctypes.byref(ms)))
+    return ms.value
+
+
+def autotune_clear() -> None:
+    _check(load().rfx_autotune_clear())
+
+
+def autotune_save(path) -> None:
+    _check(load().rfx_autotune_save(str(path).encode()))
+
+
+def autotune_load(path) -> None:
+    _check(load().rfx_autotune_load(str(path).encode()))

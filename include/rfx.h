@@ -66,6 +66,8 @@ typedef enum rfx_chan_impl {
      * branch sums into shared memory, then the GEMM). M = 1024: the plain form's FP32 branch
      * sums, then the DFT factored 32 x 32 into two GEMMs with an FP32 twiddle between them. */
     RFX_CHAN_TC = 1,
+    /* Chosen when the plan is made, from the tuned table (rfx_autotune_channelize) or the
+     * built-in rule (the tensor-core form at 64 channels, the plain form otherwise). */
     RFX_CHAN_AUTO = 2
 } rfx_chan_impl;
 
@@ -170,7 +172,8 @@ typedef struct rfx_chan_plan rfx_chan_plan;
  * RFX_CHAN_PLAIN, the batched inverse cuFFT plan of `channels` points (the project's FftPlan,
  * src/fft_plan.hpp:15-22); for RFX_CHAN_TC (64 or 1024 channels, RFX_ERR_CAPACITY otherwise),
  * the DFT operand built in FP64 and, at 1024 channels, a buffer for the branch sums
- * (max_samples / 1024 frames x 8 KB). RFX_CHAN_AUTO picks RFX_CHAN_TC for 64 channels.
+ * (max_samples / 1024 frames x 8 KB). RFX_CHAN_AUTO picks by the tuned table, else the
+ * tensor-core form at 64 channels.
  * Allocates; call outside timed regions. */
 int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_plan** plan);
 int rfx_chan_plan_destroy(rfx_chan_plan* plan);
@@ -316,14 +319,30 @@ int rfx_magnitude_host(const void* x_iq, int64_t num_samples, float* mag, rfx_be
 
 /* ---- tuning --------------------------------------------------------------------------- */
 
-/* Times every candidate tile shape of `impl` for one (num_taps, num_samples) FIR case on the
- * current device and stores the fastest in the in-process table RFX_FIR_AUTO consults.
- * Allocates scratch buffers; synchronizes. `best_ms` may be NULL. */
+/* The `auto` implementations consult in-process tables filled by the calls below, and apply
+ * a built-in rule where an entry is missing (FIR: the tensor core from 160 taps and 2^16
+ * samples; channelizer: the tensor core at 64 channels). The batch's auto form places each
+ * capture by the FIR table. If the environment variable RFX_TUNE_FILE names a file saved by
+ * rfx_autotune_save, it is loaded before the first lookup (entries of other GPUs or drivers
+ * are skipped). The tuner is this library's own: the project picks kernels by name only
+ * (src/main.cpp:156-167), and its plan object for a channelizer is a cuFFT plan. */
+
+/* Times every candidate of `impl` (RFX_FIR_AUTO: the plain kernel and every tensor-core tile
+ * shape) for one (num_taps, num_samples) FIR case on the current device, over seeded
+ * pseudo-random samples and taps, and stores the fastest for that (taps, length) bucket (powers
+ * of two). Allocates scratch buffers; synchronizes. `best_ms` may be NULL. */
 int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, double* best_ms);
 
-/* Writes / reads the tuned table as text (one line per entry, keyed by GPU name and driver). */
+/* The same for the channelizer: times the plain and (where it exists) the tensor-core form
+ * for `channels` channels, `num_taps` taps, `num_samples` samples, and stores the faster for
+ * RFX_CHAN_AUTO plans of that channel count and length bucket. */
+int rfx_autotune_channelize(int channels, int num_taps, int64_t num_samples, double* best_ms);
+
+/* Writes / reads the tuned tables as text (one line per entry, keyed by GPU name and driver).
+ * rfx_autotune_clear empties them (the built-in rules apply again). */
 int rfx_autotune_save(const char* path);
 int rfx_autotune_load(const char* path);
+int rfx_autotune_clear(void);
 
 #ifdef __cplusplus
 }
