@@ -299,9 +299,10 @@ class Arm:
 
 
 class BatchArm:
-    """The batched workload: every capture with its own taps, device-resident; one step is
-    one rfx_fir_batch_launch over all captures (tensor core and auto: replayed from a CUDA graph
-    captured once; plain: one launch per capture, as the project runs a batch)."""
+    """The batched workload: every capture with its own taps, device-resident. auto and tc_split:
+    one step is one run of a batch plan (rfx_fir_batch_plan_create, made once before timing):
+    ONE persistent launch over all captures, replayed from a CUDA graph captured once. plain:
+    one rfx_fir_batch_launch that runs one launch per capture, as the project runs a batch."""
 
     def __init__(self, rfx, w, impl: str, device) -> None:
         import torch
@@ -322,43 +323,42 @@ class BatchArm:
             self.caps.append((self.X[o:o + x.size], self.Y[o:o + x.size],
                               torch.from_numpy(h).to(device)))
         self.n = int(sum(x.size for x, _ in w.captures))
-        self.arr = (rfx.FirCapture * len(self.caps))()
-        for i, (xd, yd, hd) in enumerate(self.caps):
-            self.arr[i] = rfx.FirCapture(xd.data_ptr(), yd.data_ptr(), hd.data_ptr(), xd.numel(),
-                                         hd.numel(), 0)
-        self.impl_v = rfx.parse_fir_impl(impl)
         self.kernels = [rfx.fir_impl_used(impl, h.size, x.size, batch=True)
                         for x, h in w.captures]
-        self.launches_per_step = batch_launches(impl, [(int(x.size), int(h.size))
-                                                       for x, h in w.captures], self.kernels)
         tc = sum(1 for k in self.kernels if k == "tc_split")
         self.dtype = ("f32" if tc == 0 else "f16x3->f32" if tc == len(self.kernels)
                       else "f16x3->f32 (tensor-core captures) + f32")
         self.kernel = "tc_split" if impl == "tc_split" else "plain" if impl == "plain" else "mixed"
         self.graph = None
-        if impl != "plain":
-            # One step captured into a CUDA graph (after a warm-up launch that sets the kernels'
-            # attributes), replayed per step.
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.stream(side):
-                self._launch_on(side)
-            side.synchronize()
-            self.graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self.graph, stream=side, capture_error_mode="relaxed"):
-                self._launch_on(side)
-            torch.cuda.synchronize()
-
-    def _launch_on(self, stream) -> None:
-        self.rfx._check(self.rfx.load().rfx_fir_batch_launch(
-            self.impl_v, self.arr, len(self.caps), self.rfx._stream_ptr(stream)))
+        self.plan = None
+        if impl == "plain":
+            self.arr = (rfx.FirCapture * len(self.caps))()
+            for i, (xd, yd, hd) in enumerate(self.caps):
+                self.arr[i] = rfx.FirCapture(xd.data_ptr(), yd.data_ptr(), hd.data_ptr(),
+                                             xd.numel(), hd.numel(), 0)
+            self.launches_per_step = sum(1 for x, _ in w.captures if x.size)
+            return
+        self.plan = rfx.FirBatchPlan(self.caps, impl)
+        info = self.plan.info()
+        self.launches_per_step = info["launches"]
+        self.plan_info = info
+        # One step captured into a CUDA graph (after a warm-up run), replayed per step.
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.plan.run(side)
+        side.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=side, capture_error_mode="relaxed"):
+            self.plan.run(side)
+        torch.cuda.synchronize()
 
     def launch(self, i: int) -> None:
         if self.graph is not None:
             self.graph.replay()
         else:
-            self.rfx._check(self.rfx.load().rfx_fir_batch_launch(self.impl_v, self.arr,
-                                                                  len(self.caps), None))
+            self.rfx._check(self.rfx.load().rfx_fir_batch_launch(
+                self.rfx.parse_fir_impl(self.impl), self.arr, len(self.caps), None))
 
     def error(self, ref=None) -> dict:
         """Every capture's whole output against the float64 oracle: the largest normwise error
@@ -388,7 +388,9 @@ class BatchArm:
         return out
 
     def release(self) -> None:
-        self.caps = self.arr = self.X = self.Y = self.graph = None
+        if self.plan is not None:
+            self.plan.close()
+        self.caps = self.X = self.Y = self.graph = self.plan = None
 
 
 def auto_picks_tc(num_taps: int, n: int) -> bool:
@@ -402,20 +404,6 @@ def chan_launches(channels: int, impl: str) -> int:
     1024; auto = the tensor-core form at 64 channels, plain otherwise."""
     tc = impl == "tc_split" or (impl == "auto" and channels == 64)
     return 1 if tc and channels == 64 else 2
-
-
-def batch_launches(impl: str, sizes: list[tuple[int, int]], kernels: list[str]) -> int:
-    """Kernel launches of one rfx_fir_batch_launch: plain = one per non-empty capture; tensor
-    core = one persistent launch per 96 tensor-core captures plus one plain launch per capture
-    it hands over; auto = one plain launch per 256 plain captures plus the tensor-core launches."""
-    live = [(m, k, kern) for (m, k), kern in zip(sizes, kernels) if m > 0]
-    tc = sum(1 for _, _, kern in live if kern == "tc_split")
-    plain = len(live) - tc
-    if impl == "plain":
-        return len(live)
-    if impl == "tc_split":
-        return -(-tc // 96) + plain
-    return -(-plain // 256) + -(-tc // 96)
 
 
 def arm_order(w) -> list[str]:

@@ -25,13 +25,16 @@
 //  * the drain's scale is per tile: 2^-(ex + eh), eh the tile's capture's tap scale.
 #include "fir_tc.cuh"
 #include "fir_plain.cuh"
+#include "fir_plain_tile.cuh"
 #include "tc_common.cuh"
 #include "tmap.hpp"
+#include "tuning.hpp"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 namespace rfx {
@@ -83,6 +86,37 @@ struct BatchParams {
     int cta_item[kBatchCtas + 1];
 };
 static_assert(sizeof(BatchParams) <= 32000, "kernel parameter space");
+
+// A capture the batch runs on the plain kernel's tile function: its tiles of 2304 outputs are
+// plain tiles tile0 .. tile0 + ceil(n / 2304) - 1 of the launch.
+struct PlainCapDev {
+    const float2* x;
+    float2* y;
+    const float* taps;
+    long long n;
+    int num_taps;
+    int tile0;
+};
+
+// Where a launch finds its work: the tensor-core captures (table, tensor maps, item ranges per
+// block) and the plain captures (table, plain-tile ranges per block). For rfx_fir_batch_launch
+// the arrays are in the kernel parameters (BatchParams; no plain captures); for a batch plan
+// they are in device memory, written once when the plan is made.
+struct BatchView {
+    const BatchCap* cap;
+    const CUtensorMap* xmap;
+    const CUtensorMap* smap;
+    const int* cta_item;
+    const PlainCapDev* pcap;
+    const int* cta_plain;
+    int count;
+    int pcount;
+    int cmax;
+    int sbufs;
+    int plain_groups;        // groups of 256 threads running plain tiles (0: none)
+    uint32_t plain_region;   // shared-memory bytes per group
+    int maps_global;         // tensor maps in global memory: fence them before first use
+};
 
 // Per-capture window geometry.
 struct Geo {
@@ -165,7 +199,7 @@ struct Ctrl {
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
 // Capture of a work-list item, searched forward from a cursor (items only increase).
-__device__ __forceinline__ int capture_of(const BatchParams& p, int item, int cursor)
+__device__ __forceinline__ int capture_of(const BatchView& p, int item, int cursor)
 {
     while (cursor + 1 < p.count && p.cap[cursor + 1].item0 <= item) {
         ++cursor;
@@ -217,11 +251,19 @@ __device__ __forceinline__ void h_group_range(const HGroups& g, int P, int gi, i
 
 }  // namespace
 
-template <int S>
-__global__ void __launch_bounds__(kThreads, 1)
-fir_batch_kernel(const __grid_constant__ BatchParams p)
+// Makes a tensor map that the host wrote into global memory visible to the tensor-map proxy
+// of the calling thread before its first TMA copy through it.
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap* map)
 {
-    extern __shared__ __align__(1024) unsigned char smem[];
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
+
+// The tensor-core items first_item .. first_item + my_items - 1 of the work list (my_items > 0,
+// the same for every thread of the block). Every thread returns after a final block barrier.
+template <int S>
+__device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_item, int my_items,
+                                               unsigned char* smem)
+{
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
     const int sbufs = p.sbufs;
     const Layout lay = batch_layout(p.cmax, S, sbufs);
@@ -230,11 +272,17 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
     const uint32_t sbase = smem_u32(smem);
     volatile int* abort = &ctl.abort;
     unsigned int* fault = &g_fault_fir_batch;
-    const int first_item = p.cta_item[blockIdx.x];
-    const int my_items = p.cta_item[blockIdx.x + 1] - first_item;
-    if (my_items <= 0) {
-        return;  // uniform for the whole block: nothing allocated yet
-    }
+    // The last capture whose tensor maps the calling thread has fenced (each thread that
+    // issues copies keeps its own; captures are met in increasing order).
+    int fenced = -1;
+    auto acquire_maps = [&](int cursor) {
+        if (p.maps_global) {
+            for (; fenced < cursor; ++fenced) {
+                tmap_acquire(p.xmap + fenced + 1);
+                tmap_acquire(p.smap + fenced + 1);
+            }
+        }
+    };
     const int my_steps = my_items * kStagesPerTile;
     const int scan_slices = (my_items - 1) * kStagesPerTile;
     // Tile index of item k within its capture.
@@ -275,8 +323,9 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
         cursor = capture_of(p, first_item + k, cursor);
         const BatchCap& c = p.cap[cursor];
         const Geo g = geo_of(c.C, c.n);
+        acquire_maps(cursor);
         mbar_arrive_expect_tx(bar, g.raw_tx);
-        tma_load_2d(dst, &p.xmap[cursor], 32 * (u % kStagesPerTile), tile_in(c, k) * kNB - c.C,
+        tma_load_2d(dst, p.xmap + cursor, 32 * (u % kStagesPerTile), tile_in(c, k) * kNB - c.C,
                     bar);
         return cursor;
     };
@@ -287,8 +336,10 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
         const BatchCap& c = p.cap[cursor];
         const Geo g = geo_of(c.C, c.n);
         const uint32_t bar = smem_u32(&ctl.scan_full[q % sbufs]);
+        acquire_maps(cursor);
         mbar_arrive_expect_tx(bar, g.scan_tx);
-        tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(q % sbufs) * lay.scan, &p.smap[cursor], 0,
+        tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(q % sbufs) * lay.scan,
+                    p.smap + cursor, 0,
                     tile_in(c, kn) * kNB - c.C + (q % kStagesPerTile) * g.srows, bar);
         return cursor;
     };
@@ -772,6 +823,89 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
     if (warp == kMmaWarp) {
         tmem_dealloc(tmem, kTmemCols);
     }
+    __syncthreads();
+}
+
+// True on every thread of plain group `id` if `v` is true on all of them (one barrier).
+__device__ __forceinline__ bool group_all(bool v, uint32_t id)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(static_cast<uint32_t>(v)), "r"(id), "n"(kPlainThreads)
+        : "memory");
+    return r != 0;
+}
+
+// Plain tiles t0 .. t1 - 1 of the work list, by plain_groups groups of 256 threads (group g
+// takes tiles t0 + g, t0 + g + groups, ...), each with its own shared-memory region and named
+// barrier: the plain kernel's tile function, so the same bits as fir_plain_kernel.
+__device__ __forceinline__ void batch_plain_tiles(const BatchView& p, int t0, int t1,
+                                                  unsigned char* smem)
+{
+    const int group = static_cast<int>(threadIdx.x) / kPlainThreads;
+    if (group >= p.plain_groups) {
+        return;
+    }
+    const int gtid = static_cast<int>(threadIdx.x) % kPlainThreads;
+    unsigned char* region = smem + 1024 + static_cast<uint32_t>(group) * p.plain_region;
+    const PlainGroupSync sync{static_cast<uint32_t>(2 + group)};
+    uint32_t phase = 0;
+    bool init = true;
+    int c = 0;
+    for (int t = t0 + group; t < t1; t += p.plain_groups) {
+        while (c + 1 < p.pcount && p.pcap[c + 1].tile0 <= t) {
+            ++c;
+        }
+        const PlainCapDev& pc = p.pcap[c];
+        const bool ok = fir_plain_tile<0>(pc.x, pc.taps, pc.y, pc.n, pc.num_taps, t - pc.tile0,
+                                          region, &g_fault_fir_batch, gtid, sync, phase, init);
+        init = false;
+        if (!group_all(ok, sync.id)) {
+            break;   // a copy gave up (fault recorded): the whole group stops together
+        }
+    }
+}
+
+template <int S>
+__device__ __forceinline__ void batch_body(const BatchView& v, unsigned char* smem)
+{
+    const int first_item = v.cta_item[blockIdx.x];
+    const int my_items = v.cta_item[blockIdx.x + 1] - first_item;
+    if (my_items > 0) {
+        batch_tc_items<S>(v, first_item, my_items, smem);
+    }
+    if (v.plain_groups > 0) {
+        const int t0 = v.cta_plain[blockIdx.x];
+        const int t1 = v.cta_plain[blockIdx.x + 1];
+        if (t1 > t0) {
+            batch_plain_tiles(v, t0, t1, smem);
+        }
+    }
+}
+
+// rfx_fir_batch_launch: the work list in the kernel parameters (tensor-core captures only).
+template <int S>
+__global__ void __launch_bounds__(kThreads, 1)
+fir_batch_kernel(const __grid_constant__ BatchParams p)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const BatchView v{p.cap, p.xmap, p.smap, p.cta_item, nullptr, nullptr, p.count, 0,
+                      p.cmax, p.sbufs, 0, 0u, 0};
+    batch_body<S>(v, smem);
+}
+
+// A batch plan: the work list in device memory, tensor-core and plain captures in one launch.
+template <int S>
+__global__ void __launch_bounds__(kThreads, 1)
+fir_batch_list_kernel(const __grid_constant__ BatchView v)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    batch_body<S>(v, smem);
 }
 
 namespace {
@@ -924,6 +1058,269 @@ cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cuda
         }
     }
     return cudaSuccess;
+}
+
+// ---- batch plans: the work list in device memory, one launch ---------------------------------
+
+namespace {
+
+// Cost of a work unit in microseconds of one SM, for the partition (measured on GB300 with the
+// single-capture kernels: a tensor-core tile of 96 blocks takes 12.8 us at 63 taps and 16.0 us
+// at 1025; a plain tile of 2304 outputs 1.7 us at 63 taps with four blocks per SM, here run by
+// three groups of 256 threads per SM, and about proportional to the taps beyond that).
+double tc_tile_us(int C) { return 12.4 + 0.4 * static_cast<double>(C + 1); }
+double plain_tile_us(int num_taps)
+{
+    return 2.2 * (0.5 + 0.5 * static_cast<double>(num_taps) / 63.0);
+}
+
+constexpr int kPlainGroupsMax = kThreads / kPlainThreads;   // 3
+constexpr uint32_t kSmemMax = 227u * 1024u;
+
+uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct BatchPlan {
+    void* dev = nullptr;
+    BatchView view{};
+    int grid = 0;
+    int stages = 0;
+    uint32_t smem = 0;
+    int tc_caps = 0;
+    int plain_caps = 0;
+};
+
+void fir_batch_plan_free(BatchPlan* plan)
+{
+    if (plan != nullptr) {
+        cudaFree(plan->dev);
+        delete plan;
+    }
+}
+
+void fir_batch_plan_counts(const BatchPlan* plan, int* tc_captures, int* plain_captures,
+                           int* launches)
+{
+    *tc_captures = plan->tc_caps;
+    *plain_captures = plan->plain_caps;
+    *launches = plan->grid > 0 ? 1 : 0;
+}
+
+cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int count,
+                                BatchPlan** out)
+{
+    *out = nullptr;
+    int device = 0;
+    int sms = 0;
+    cudaError_t err = cudaGetDevice(&device);
+    if (err != cudaSuccess ||
+        (err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) !=
+            cudaSuccess) {
+        return err;
+    }
+    // Which kernel takes each capture: the tensor-core pipeline where the call's implementation
+    // (auto: the tuned table) puts it and the batch kernel can take it, the plain tile otherwise.
+    std::vector<BatchCap> tc;
+    std::vector<CUtensorMap> xmaps, smaps;
+    std::vector<PlainCapDev> pl;
+    std::vector<double> cost;       // per work unit: tensor-core items, then plain tiles
+    int kmax_plain = 0;
+    int cmax = 0;
+    int items = 0;
+    int ptiles = 0;
+    std::vector<double> plain_cost;
+    for (int i = 0; i < count; ++i) {
+        const rfx_fir_capture& c = captures[i];
+        if (c.num_samples == 0) {
+            continue;
+        }
+        const int want = impl == RFX_FIR_AUTO ? tuned_fir_impl(c.num_taps, c.num_samples) : impl;
+        const bool use_tc = want == RFX_FIR_TC && c.num_samples >= kB &&
+                            fir_batch_supported(c.num_taps);
+        if (use_tc) {
+            BatchCap b{};
+            b.x = static_cast<const float2*>(c.x);
+            b.y = static_cast<float2*>(c.y);
+            b.taps = c.taps;
+            b.n = c.num_samples;
+            b.num_taps = c.num_taps;
+            b.C = (c.num_taps + kB - 2) / kB;
+            const long long blocks = (c.num_samples + kB - 1) / kB;
+            b.tiles = static_cast<int>((blocks + kNB - 1) / kNB);
+            b.item0 = items;
+            items += b.tiles;
+            cmax = std::max(cmax, b.C);
+            const Geo g = geo_of(b.C, b.n);
+            CUtensorMap xm, sm;
+            err = encode_rows(&xm, c.x, 4, b.n / kB, 2 * kB, 32, static_cast<uint32_t>(g.rows));
+            if (err == cudaSuccess) {
+                err = encode_rows(&sm, c.x, 4, b.n / kB, 2 * kB, 2 * kB,
+                                  static_cast<uint32_t>(g.srows));
+            }
+            if (err != cudaSuccess) {
+                return err;
+            }
+            for (int t = 0; t < b.tiles; ++t) {
+                cost.push_back(tc_tile_us(b.C));
+            }
+            tc.push_back(b);
+            xmaps.push_back(xm);
+            smaps.push_back(sm);
+        } else {
+            PlainCapDev q{};
+            q.x = static_cast<const float2*>(c.x);
+            q.y = static_cast<float2*>(c.y);
+            q.taps = c.taps;
+            q.n = c.num_samples;
+            q.num_taps = c.num_taps;
+            q.tile0 = ptiles;
+            const int tiles =
+                static_cast<int>((c.num_samples + kPlainTileOutputs - 1) / kPlainTileOutputs);
+            ptiles += tiles;
+            for (int t = 0; t < tiles; ++t) {
+                plain_cost.push_back(plain_tile_us(c.num_taps));
+            }
+            kmax_plain = std::max(kmax_plain, c.num_taps);
+            pl.push_back(q);
+        }
+    }
+    cost.insert(cost.end(), plain_cost.begin(), plain_cost.end());
+    const int units = static_cast<int>(cost.size());
+    auto* plan = new BatchPlan{};
+    plan->tc_caps = static_cast<int>(tc.size());
+    plan->plain_caps = static_cast<int>(pl.size());
+    if (units == 0) {
+        *out = plan;   // nothing to run
+        return cudaSuccess;
+    }
+    // Shared memory: the tensor-core pipeline for the largest filter (the deepest scan ring,
+    // then the most operand stages that fit), and up to three plain-tile regions.
+    Layout lay{};
+    int stages = 0;
+    int sbufs = 0;
+    if (!tc.empty()) {
+        for (int sb = kScanBufsMax; sb >= 2 && stages == 0; sb -= 2) {
+            for (int st : {6, 4, 2}) {
+                if (batch_layout(cmax, st, sb).bytes <= kSmemMax) {
+                    stages = st;
+                    sbufs = sb;
+                    lay = batch_layout(cmax, st, sb);
+                    break;
+                }
+            }
+        }
+        if (stages == 0) {
+            delete plan;
+            return cudaErrorInvalidValue;
+        }
+    }
+    uint32_t region = 0;
+    int groups = 0;
+    if (!pl.empty()) {
+        region = align_up(plain_layout(kmax_plain).bytes, 128);
+        groups = std::min<int>(kPlainGroupsMax, static_cast<int>((kSmemMax - 1024u) / region));
+        if (groups < 1) {
+            delete plan;
+            return cudaErrorInvalidValue;
+        }
+    }
+    plan->stages = stages == 0 ? 2 : stages;
+    plan->smem = std::max({tc.empty() ? 0u : lay.bytes, 1024u + groups * region, 120u * 1024u});
+
+    // Partition: the units on one line (tensor-core items, then plain tiles), cut into grid
+    // contiguous pieces of about equal cost; blocks of the first pieces run tensor-core items
+    // while the last ones run plain tiles, so tensor-bound and memory-bound work overlap.
+    const int grid = std::min({sms, kBatchCtas, units});
+    std::vector<double> prefix(units + 1, 0.0);
+    for (int u = 0; u < units; ++u) {
+        prefix[u + 1] = prefix[u] + cost[u];
+    }
+    std::vector<int> cta_item(grid + 1), cta_plain(grid + 1);
+    for (int b = 0; b <= grid; ++b) {
+        int u = b == grid ? units
+                          : static_cast<int>(std::lower_bound(prefix.begin(), prefix.end(),
+                                                              prefix[units] * b / grid) -
+                                             prefix.begin());
+        u = std::min(u, units);
+        cta_item[b] = std::min(u, items);
+        cta_plain[b] = std::max(u - items, 0);
+    }
+    for (int b = 1; b <= grid; ++b) {   // monotone after rounding
+        cta_item[b] = std::max(cta_item[b], cta_item[b - 1]);
+        cta_plain[b] = std::max(cta_plain[b], cta_plain[b - 1]);
+    }
+
+    // One device buffer: capture table, tensor maps (128-byte aligned), block ranges, plain
+    // captures.
+    const uint32_t n_tc = static_cast<uint32_t>(tc.size());
+    const uint32_t off_cap = 0;
+    const uint32_t off_xmap = align_up(off_cap + n_tc * sizeof(BatchCap), 128);
+    const uint32_t off_smap = off_xmap + n_tc * sizeof(CUtensorMap);
+    const uint32_t off_item = align_up(off_smap + n_tc * sizeof(CUtensorMap), 16);
+    const uint32_t off_plain = align_up(off_item + (grid + 1) * sizeof(int), 16);
+    const uint32_t off_pcap = align_up(off_plain + (grid + 1) * sizeof(int), 16);
+    const uint32_t bytes = align_up(off_pcap + pl.size() * sizeof(PlainCapDev), 128);
+    std::vector<unsigned char> host(bytes, 0);
+    std::memcpy(host.data() + off_cap, tc.data(), n_tc * sizeof(BatchCap));
+    std::memcpy(host.data() + off_xmap, xmaps.data(), n_tc * sizeof(CUtensorMap));
+    std::memcpy(host.data() + off_smap, smaps.data(), n_tc * sizeof(CUtensorMap));
+    std::memcpy(host.data() + off_item, cta_item.data(), (grid + 1) * sizeof(int));
+    std::memcpy(host.data() + off_plain, cta_plain.data(), (grid + 1) * sizeof(int));
+    std::memcpy(host.data() + off_pcap, pl.data(), pl.size() * sizeof(PlainCapDev));
+    unsigned char* dev = nullptr;
+    if ((err = cudaMalloc(&dev, bytes)) != cudaSuccess ||
+        (err = cudaMemcpy(dev, host.data(), bytes, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        cudaFree(dev);
+        delete plan;
+        return err;
+    }
+    plan->dev = dev;
+    plan->grid = grid;
+    BatchView& v = plan->view;
+    v.cap = reinterpret_cast<const BatchCap*>(dev + off_cap);
+    v.xmap = reinterpret_cast<const CUtensorMap*>(dev + off_xmap);
+    v.smap = reinterpret_cast<const CUtensorMap*>(dev + off_smap);
+    v.cta_item = reinterpret_cast<const int*>(dev + off_item);
+    v.cta_plain = reinterpret_cast<const int*>(dev + off_plain);
+    v.pcap = reinterpret_cast<const PlainCapDev*>(dev + off_pcap);
+    v.count = static_cast<int>(n_tc);
+    v.pcount = static_cast<int>(pl.size());
+    v.cmax = cmax;
+    v.sbufs = sbufs == 0 ? 2 : sbufs;
+    v.plain_groups = groups;
+    v.plain_region = region;
+    v.maps_global = 1;
+    const void* fn = plan->stages == 6   ? reinterpret_cast<const void*>(fir_batch_list_kernel<6>)
+                     : plan->stages == 4 ? reinterpret_cast<const void*>(fir_batch_list_kernel<4>)
+                                         : reinterpret_cast<const void*>(fir_batch_list_kernel<2>);
+    if ((err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(plan->smem))) != cudaSuccess) {
+        fir_batch_plan_free(plan);
+        return err;
+    }
+    *out = plan;
+    return cudaSuccess;
+}
+
+cudaError_t fir_batch_plan_run(const BatchPlan* plan, cudaStream_t stream)
+{
+    if (plan->grid == 0) {
+        return cudaSuccess;
+    }
+    const dim3 grid(static_cast<unsigned>(plan->grid));
+    switch (plan->stages) {
+    case 6:
+        fir_batch_list_kernel<6><<<grid, kThreads, plan->smem, stream>>>(plan->view);
+        break;
+    case 4:
+        fir_batch_list_kernel<4><<<grid, kThreads, plan->smem, stream>>>(plan->view);
+        break;
+    default:
+        fir_batch_list_kernel<2><<<grid, kThreads, plan->smem, stream>>>(plan->view);
+        break;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t fir_batch_take_fault(unsigned int* code)

@@ -1,27 +1,8 @@
-// Plain FP32 FIR for sm_103a.
-//
-//   y[n] = sum_{k=0}^{K-1} h[k] x[n-k],  x[m] = 0 for m < 0,  n < N      (src/fir.cu:1-5)
-//
-// Arithmetic: every output is one chain of fused multiply-adds over k = 0, 1, ..., K-1 starting
-// from +0.0f, separately for I and Q. That is the order of the project's naive, tiled and
-// register kernels (src/fir.cu:35-40, :377-395), so the results are bit-identical to theirs.
-// Taps past the start of the input multiply zeros, which leaves the chain unchanged.
-//
-// Work decomposition: a block of 256 threads owns a tile of 2304 consecutive outputs; thread t
-// owns outputs t0 + 9t ... t0 + 9t + 8. Nine (odd) outputs per thread put the 64-bit shared
-// loads of a warp (stride 72 bytes) on distinct bank pairs.
-//
-// Staging: the tile's samples x[t0 - (K-1) .. t0 + 2303] (start rounded down to an even index so
-// the copy is 16-byte aligned) arrive in shared memory through ONE bulk copy on the TMA engine,
-// completed on an mbarrier; tiles that touch either end of the input are filled by the threads
-// with zeros outside [0, N). Results go back through shared memory and one bulk store.
-//
-// Inner loop: taps are taken nine at a time. For taps 9g .. 9g+8 a thread needs the 17 samples
-// x[n0 - 9g - 8 .. n0 - 9g + 8] (n0 = its first output), i.e. the sample blocks
-// S_g = x[n0 - 9g .. +8] and S_{g+1}. Two register blocks alternate between those roles, so
-// sliding the window costs nine 64-bit loads per nine taps and no register moves. Each
-// tap-sample product is one packed fma.rn.f32x2 on (I, Q) with the tap duplicated in both lanes.
+// Plain FP32 FIR kernels for sm_103a: one tile of 2304 outputs per block of 256 threads
+// (fir_plain_tile.cuh holds the tile function, its arithmetic and its staging), for one capture,
+// for captures sharing one tap set, for captures with their own taps, and for integer input.
 #include "fir_plain.cuh"
+#include "fir_plain_tile.cuh"
 #include "ptx.cuh"
 
 #include <cuda_runtime.h>
@@ -33,225 +14,27 @@ static __device__ unsigned int g_fault_fir_plain;
 namespace {
 
 constexpr int kThreads = kPlainThreads;
-constexpr int kR = kPlainOutputsPerThread;
 constexpr int kTile = kPlainTileOutputs;
-constexpr int kGuard = 16;  // zero samples in front of the tile: the last window block may
-                            // reach up to 10 samples before it (those values are never used)
 
-struct Layout {
-    uint32_t taps_off;   // (h, h) pairs, K entries
-    uint32_t tile_off;   // guard + tile samples
-    uint32_t raw_off;    // integer input formats: the tile's raw components as copied
-    uint32_t bytes;
-};
-
-// Bytes per sample of each input format (rfx_sample_format): cf32, ci16, ci8.
-__host__ __device__ constexpr uint32_t sample_bytes(int fmt) { return fmt == 0 ? 8u : fmt == 1 ? 4u : 2u; }
-
-__host__ __device__ inline Layout plain_layout(int num_taps, int fmt = 0)
+// One tile per block, the whole block as the tile's thread group.
+template <int kFmt = 0>
+__device__ __forceinline__ void plain_block_tile(const void* x, const float* taps, float2* y,
+                                                 long long n, int num_taps, long long tile,
+                                                 unsigned char* smem)
 {
-    Layout l;
-    l.taps_off = 16;
-    l.tile_off = (l.taps_off + 8u * static_cast<uint32_t>(num_taps) + 15u) & ~15u;
-    const uint32_t tile_samples = kGuard + kTile + static_cast<uint32_t>(num_taps) + 8u;
-    l.raw_off = (l.tile_off + 8u * tile_samples + 15u) & ~15u;
-    l.bytes = l.raw_off + (fmt == 0 ? 0u : sample_bytes(fmt) * (kTile + static_cast<uint32_t>(num_taps) + 8u));
-    return l;
-}
-
-// Sample i of an integer-format input, decoded as the project's SigMF reader does
-// (src/io.cpp:110-124): component x (1/32768) for ci16_le, x (1/128) for ci8.
-template <int kFmt>
-__device__ __forceinline__ f32x2 decode_sample(const void* raw, long long i)
-{
-    if (kFmt == 1) {
-        const short2 v = static_cast<const short2*>(raw)[i];
-        return pack2(static_cast<float>(v.x) * (1.0f / 32768.0f),
-                     static_cast<float>(v.y) * (1.0f / 32768.0f));
-    }
-    const char2 v = static_cast<const char2*>(raw)[i];
-    return pack2(static_cast<float>(v.x) * (1.0f / 128.0f), static_cast<float>(v.y) * (1.0f / 128.0f));
-}
-
-// Nine taps 9g + q (q < nq) against output window blocks: cur = S_g, nxt = S_{g+1}.
-__device__ __forceinline__ void tap_group(f32x2 (&acc)[kR], const f32x2 (&cur)[kR],
-                                          const f32x2 (&nxt)[kR], const f32x2* taps2, int k0,
-                                          int nq)
-{
-#pragma unroll
-    for (int q = 0; q < kR; ++q) {
-        if (q < nq) {
-            const f32x2 h = taps2[k0 + q];
-#pragma unroll
-            for (int j = 0; j < kR; ++j) {
-                acc[j] = fma2(h, j >= q ? cur[j - q] : nxt[kR + j - q], acc[j]);
-            }
-        }
-    }
-}
-
-__device__ __forceinline__ void load_block(f32x2 (&blk)[kR], const f32x2* tile, int p, int m)
-{
-    // S_m[i] = x[n0 - 9m + i] = tile[p - 9m + i]
-    const f32x2* src = tile + (p - kR * m);
-#pragma unroll
-    for (int i = 0; i < kR; ++i) {
-        blk[i] = src[i];
-    }
-}
-
-// Computes this thread's nine outputs of the tile staged at `tile` (tile[i] = x[base + i]).
-__device__ __forceinline__ void compute_outputs(f32x2 (&acc)[kR], const f32x2* tile,
-                                                const f32x2* taps2, int p, int num_taps)
-{
-#pragma unroll
-    for (int j = 0; j < kR; ++j) {
-        acc[j] = 0ull;  // +0.0f, +0.0f
-    }
-    const int groups = num_taps / kR;
-    const int rem = num_taps - groups * kR;
-    f32x2 a[kR];
-    f32x2 b[kR];
-    load_block(a, tile, p, 0);
-    int g = 0;
-    for (; g + 2 <= groups; g += 2) {
-        load_block(b, tile, p, g + 1);
-        tap_group(acc, a, b, taps2, kR * g, kR);
-        load_block(a, tile, p, g + 2);
-        tap_group(acc, b, a, taps2, kR * (g + 1), kR);
-    }
-    if (g < groups) {
-        load_block(b, tile, p, g + 1);
-        tap_group(acc, a, b, taps2, kR * g, kR);
-        if (rem > 0) {
-            load_block(a, tile, p, g + 2);
-            tap_group(acc, b, a, taps2, kR * (g + 1), rem);
-        }
-    } else if (rem > 0) {
-        load_block(b, tile, p, g + 1);
-        tap_group(acc, a, b, taps2, kR * g, rem);
-    }
+    uint32_t phase = 0;
+    fir_plain_tile<kFmt>(x, taps, y, n, num_taps, tile, smem, &g_fault_fir_plain,
+                         static_cast<int>(threadIdx.x), PlainBlockSync{}, phase, true);
 }
 
 }  // namespace
-
-// One tile of one capture. Shared by the single-capture and the batched kernels. kFmt: the
-// input's sample format (0 cf32; 1 ci16, 2 ci8: decoded into cf32 in shared memory).
-template <int kFmt = 0>
-__device__ __forceinline__ void fir_plain_tile(const void* __restrict__ xv,
-                                               const float* __restrict__ taps,
-                                               float2* __restrict__ y, long long n,
-                                               int num_taps, long long tile_index,
-                                               unsigned char* smem)
-{
-    const float2* x = static_cast<const float2*>(xv);
-    const Layout lay = plain_layout(num_taps, kFmt);
-    const uint32_t sbase = smem_u32(smem);
-    const uint32_t bar = sbase;  // mbarrier at offset 0
-    f32x2* taps2 = reinterpret_cast<f32x2*>(smem + lay.taps_off);
-    f32x2* guard = reinterpret_cast<f32x2*>(smem + lay.tile_off);
-    f32x2* tile = guard + kGuard;
-    const int tid = threadIdx.x;
-
-    const long long t0 = tile_index * kTile;
-    // First staged sample: a multiple of 2 (cf32) or 8 (integer formats) so that the copy
-    // starts on a 16-byte boundary; the length is then a multiple of 16 bytes too.
-    const long long base = (t0 - (num_taps - 1)) & (kFmt == 0 ? ~1ll : ~7ll);
-    const int tile_len = static_cast<int>(t0 + kTile - base);
-    const bool interior = base >= 0 && t0 + kTile <= n;
-
-    if (tid == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    if (interior && tid == 0) {
-        const uint32_t bytes = sample_bytes(kFmt) * static_cast<uint32_t>(tile_len);
-        mbar_arrive_expect_tx(bar, bytes);
-        if (kFmt == 0) {
-            bulk_g2s(smem_u32(tile), x + base, bytes, bar);
-        } else {
-            bulk_g2s(sbase + lay.raw_off,
-                     static_cast<const unsigned char*>(xv) + sample_bytes(kFmt) * base, bytes, bar);
-        }
-    }
-    // Taps (duplicated into both lanes) and the guard while the copy is in flight.
-    for (int k = tid; k < num_taps; k += kThreads) {
-        const float h = __ldg(taps + k);
-        taps2[k] = pack2(h, h);
-    }
-    if (tid < kGuard) {
-        guard[tid] = 0ull;
-    }
-    if (!interior) {
-        for (int i = tid; i < tile_len; i += kThreads) {
-            const long long m = base + i;
-            f32x2 v = 0ull;
-            if (m >= 0 && m < n) {
-                if (kFmt == 0) {
-                    const float2 s = x[m];
-                    v = pack2(s.x, s.y);
-                } else {
-                    v = decode_sample<kFmt>(xv, m);
-                }
-            }
-            tile[i] = v;
-        }
-    }
-    __syncthreads();
-    bool ok = true;
-    if (interior) {
-        ok = mbar_wait_bounded(bar, 0, &g_fault_fir_plain, kFaultTileLoad, nullptr);
-        if (kFmt != 0) {
-            // Decode the staged components into the sample tile.
-            const unsigned char* raw = smem + lay.raw_off;
-            for (int i = tid; i < tile_len; i += kThreads) {
-                tile[i] = decode_sample<kFmt>(raw, i);
-            }
-            __syncthreads();
-        }
-    }
-
-    const long long n0 = t0 + static_cast<long long>(kR) * tid;
-    f32x2 acc[kR];
-    if (ok && n0 < n) {
-        compute_outputs(acc, tile, taps2, static_cast<int>(n0 - base), num_taps);
-    }
-    __syncthreads();  // every thread is done reading the tile: reuse it for the results
-    if (ok && n0 < n) {
-#pragma unroll
-        for (int j = 0; j < kR; ++j) {
-            tile[kR * tid + j] = acc[j];
-        }
-    }
-    if (interior) {
-        fence_proxy_async_smem();
-    }
-    __syncthreads();
-    if (!ok) {
-        return;
-    }
-    if (interior) {
-        if (tid == 0) {
-            bulk_s2g(y + t0, smem_u32(tile), 8u * kTile);
-            bulk_commit();
-            bulk_wait_read_all();
-        }
-    } else {
-        const long long valid = n - t0 < kTile ? n - t0 : kTile;
-        for (int i = tid; i < valid; i += kThreads) {
-            const float2 v = unpack2(tile[i]);
-            y[t0 + i] = v;
-        }
-    }
-}
 
 __global__ void __launch_bounds__(kThreads, 4)
 fir_plain_kernel(const float2* __restrict__ x, const float* __restrict__ taps,
                  float2* __restrict__ y, long long n, int num_taps)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    fir_plain_tile(x, taps, y, n, num_taps, blockIdx.x, smem);
+    plain_block_tile(x, taps, y, n, num_taps, blockIdx.x, smem);
 }
 
 // Several captures sharing one tap set: blockIdx.y picks the capture; blocks past a shorter
@@ -265,8 +48,8 @@ fir_plain_batched_kernel(PlainBatch batch, const float* __restrict__ taps, int n
     if (static_cast<long long>(blockIdx.x) * kTile >= n) {
         return;
     }
-    fir_plain_tile(static_cast<const float2*>(batch.x[c]), taps, static_cast<float2*>(batch.y[c]),
-                   n, num_taps, blockIdx.x, smem);
+    plain_block_tile(batch.x[c], taps, static_cast<float2*>(batch.y[c]), n, num_taps, blockIdx.x,
+                     smem);
 }
 
 // Captures with their own taps: block b takes tile b - tile0[c] of the capture c whose tiles
@@ -286,9 +69,8 @@ fir_plain_caps_kernel(const __grid_constant__ PlainCaps caps)
             hi = mid;
         }
     }
-    fir_plain_tile(static_cast<const float2*>(caps.x[lo]), caps.taps[lo],
-                   static_cast<float2*>(caps.y[lo]), caps.num_samples[lo], caps.num_taps[lo],
-                   block - caps.tile0[lo], smem);
+    plain_block_tile(caps.x[lo], caps.taps[lo], static_cast<float2*>(caps.y[lo]),
+                     caps.num_samples[lo], caps.num_taps[lo], block - caps.tile0[lo], smem);
 }
 
 // Integer I/Q input (ci16, ci8), decoded in the load stage.
@@ -298,7 +80,7 @@ fir_plain_fmt_kernel(const void* __restrict__ x, const float* __restrict__ taps,
                      float2* __restrict__ y, long long n, int num_taps)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    fir_plain_tile<kFmt>(x, taps, y, n, num_taps, blockIdx.x, smem);
+    plain_block_tile<kFmt>(x, taps, y, n, num_taps, blockIdx.x, smem);
 }
 
 size_t fir_plain_smem_bytes(int num_taps) { return plain_layout(num_taps).bytes; }

@@ -46,6 +46,17 @@ cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int coun
                              cudaStream_t stream);
 cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cudaStream_t stream);
 bool fir_batch_supported(int num_taps);
+
+// A batch plan: the work list of one batch (capture tables, tensor maps, per-block ranges) in
+// device memory, built once; every run is ONE persistent launch of fir_batch.cu that takes the
+// tensor-core captures and, with groups of its threads, the plain captures' tiles.
+struct BatchPlan;
+cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int count,
+                                BatchPlan** out);
+cudaError_t fir_batch_plan_run(const BatchPlan* plan, cudaStream_t stream);
+void fir_batch_plan_free(BatchPlan* plan);
+void fir_batch_plan_counts(const BatchPlan* plan, int* tc_captures, int* plain_captures,
+                           int* launches);
 cudaError_t fir_batch_take_fault(unsigned int* code);
 
 }  // namespace rfx

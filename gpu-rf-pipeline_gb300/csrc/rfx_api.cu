@@ -426,6 +426,71 @@ int rfx_fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
     return err == cudaSuccess ? RFX_OK : cuda_fail(err, "fir_batch_launch");
 }
 
+struct rfx_fir_batch_plan {
+    rfx::BatchPlan* plan;
+};
+
+int rfx_fir_batch_plan_create(int impl, const rfx_fir_capture* captures, int count,
+                              rfx_fir_batch_plan** plan)
+{
+    if (plan == nullptr) {
+        return fail(RFX_ERR_INVALID, "fir batch plan: null plan pointer");
+    }
+    *plan = nullptr;
+    if (count < 1 || count > rfx::kTcBatchMax || captures == nullptr) {
+        return fail(RFX_ERR_INVALID, "fir batch plan: %d captures, expected 1 to %d", count,
+                    rfx::kTcBatchMax);
+    }
+    for (int c = 0; c < count; ++c) {
+        const rfx_fir_capture& cap = captures[c];
+        const int rc = check_fir_args(impl, cap.x, cap.taps, cap.y, cap.num_samples,
+                                      cap.num_taps);
+        if (rc != RFX_OK) {
+            return rc;
+        }
+        if (cap.reserved != 0) {
+            return fail(RFX_ERR_INVALID, "fir batch plan: capture %d: reserved field must be 0",
+                        c);
+        }
+    }
+    rfx::BatchPlan* p = nullptr;
+    const cudaError_t err = rfx::fir_batch_plan_make(impl, captures, count, &p);
+    if (err != cudaSuccess) {
+        return cuda_fail(err, "fir_batch_plan_make");
+    }
+    *plan = new rfx_fir_batch_plan{p};
+    return RFX_OK;
+}
+
+int rfx_fir_batch_run(rfx_fir_batch_plan* plan, cudaStream_t stream)
+{
+    if (plan == nullptr) {
+        return fail(RFX_ERR_INVALID, "fir batch run: null plan");
+    }
+    const cudaError_t err = rfx::fir_batch_plan_run(plan->plan, stream);
+    return err == cudaSuccess ? RFX_OK : cuda_fail(err, "fir_batch_plan_run");
+}
+
+int rfx_fir_batch_plan_info(const rfx_fir_batch_plan* plan, int* tc_captures,
+                            int* plain_captures, int* launches)
+{
+    if (plan == nullptr || tc_captures == nullptr || plain_captures == nullptr ||
+        launches == nullptr) {
+        return fail(RFX_ERR_INVALID, "fir batch plan info: null pointer");
+    }
+    rfx::fir_batch_plan_counts(plan->plan, tc_captures, plain_captures, launches);
+    return RFX_OK;
+}
+
+int rfx_fir_batch_plan_destroy(rfx_fir_batch_plan* plan)
+{
+    if (plan != nullptr) {
+        rfx::fir_batch_plan_free(plan->plan);
+        delete plan;
+    }
+    return RFX_OK;
+}
+
 // ---- channelizer --------------------------------------------------------------------------
 
 int64_t rfx_channelize_frames(int64_t num_samples, int channels)

@@ -65,6 +65,12 @@ SIGNATURES = {
     "rfx_fir_batched_device": (_I, [_I, ctypes.POINTER(_VP), ctypes.POINTER(_VP),
                                     ctypes.POINTER(_I64), _I, _VP, _I, _VP]),
     "rfx_fir_batch_launch": (_I, [_I, ctypes.POINTER(FirCapture), _I, _VP]),
+    "rfx_fir_batch_plan_create": (_I, [_I, ctypes.POINTER(FirCapture), _I,
+                                       ctypes.POINTER(_VP)]),
+    "rfx_fir_batch_run": (_I, [_VP, _VP]),
+    "rfx_fir_batch_plan_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                     ctypes.POINTER(_I)]),
+    "rfx_fir_batch_plan_destroy": (_I, [_VP]),
     "rfx_channelize_frames": (_I64, [_I64, _I]),
     "rfx_chan_plan_create": (_I, [_I, _I, _I64, ctypes.POINTER(_VP)]),
     "rfx_chan_plan_destroy": (_I, [_VP]),
@@ -239,6 +245,50 @@ def fir_batch(captures, impl="plain", stream=None) -> None:
         arr[i] = FirCapture(x.data_ptr(), y.data_ptr(), taps.data_ptr(), x.numel(),
                             taps.numel(), 0)
     _check(load().rfx_fir_batch_launch(_impl(impl), arr, len(captures), _stream_ptr(stream)))
+
+
+class FirBatchPlan:
+    """rfx_fir_batch_plan: a batch of (x, y, taps) device tensors (cf32, cf32, float32), each
+    capture with its own taps, run by ONE persistent launch per run(). The tensors must stay
+    alive while the plan is used."""
+
+    def __init__(self, captures, impl="auto") -> None:
+        self._p = ctypes.c_void_p()
+        self.count = len(captures)
+        arr = (FirCapture * self.count)()
+        for i, (x, y, taps) in enumerate(captures):
+            arr[i] = FirCapture(x.data_ptr(), y.data_ptr(), taps.data_ptr(), x.numel(),
+                                taps.numel(), 0)
+        self._arr = arr
+        _check(load().rfx_fir_batch_plan_create(_impl(impl), arr, self.count,
+                                                ctypes.byref(self._p)))
+
+    def run(self, stream=None) -> None:
+        _check(load().rfx_fir_batch_run(self._p, _stream_ptr(stream)))
+
+    def info(self) -> dict:
+        tc, plain, launches = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(load().rfx_fir_batch_plan_info(self._p, ctypes.byref(tc), ctypes.byref(plain),
+                                              ctypes.byref(launches)))
+        return {"tc_captures": tc.value, "plain_captures": plain.value,
+                "launches": launches.value}
+
+    def close(self) -> None:
+        if self._p:
+            load().rfx_fir_batch_plan_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __enter__(self) -> "FirBatchPlan":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class ChanPlan:

@@ -161,6 +161,30 @@ typedef struct rfx_fir_capture {
 int rfx_fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
                          cudaStream_t stream);
 
+/* A batch plan: the work list of one batch of captures (each with its own taps) built once in
+ * device memory — capture tables, TMA tensor maps, each block's share of the work — so that
+ * every run of the batch is ONE persistent kernel launch, replayable from a CUDA graph. The
+ * launch takes every capture of the batch: those the implementation puts on the tensor cores
+ * (RFX_FIR_TC: all it can take; RFX_FIR_AUTO: as the tuned table or the built-in rule places
+ * each capture) run the block-Toeplitz pipeline, the others (short filters under auto, one tap,
+ * shorter than 128 samples, beyond the kernel's tap budget, or everything under RFX_FIR_PLAIN)
+ * run the plain kernel's tile function with groups of the same blocks' threads, with its bits.
+ * The blocks are given contiguous shares of tensor-core tiles and plain tiles of about equal
+ * cost, so tensor-bound and memory-bound work run side by side on different SMs.
+ * Create allocates and copies (setup; call outside timed regions and stream capture); the
+ * capture pointers are bound at creation (the buffers' contents may change between runs).
+ * No counterpart in the project, which runs such a batch as one fir_launch per capture, and
+ * whose fir_batched_device (src/fused.cu:92-109) takes at most 8 channels sharing one tap set. */
+typedef struct rfx_fir_batch_plan rfx_fir_batch_plan;
+int rfx_fir_batch_plan_create(int impl, const rfx_fir_capture* captures, int count,
+                              rfx_fir_batch_plan** plan);
+/* Enqueues the plan's one launch on `stream`; allocates nothing. */
+int rfx_fir_batch_run(rfx_fir_batch_plan* plan, cudaStream_t stream);
+/* How the plan split the captures, and kernel launches per run (1; 0 for an empty batch). */
+int rfx_fir_batch_plan_info(const rfx_fir_batch_plan* plan, int* tc_captures,
+                            int* plain_captures, int* launches);
+int rfx_fir_batch_plan_destroy(rfx_fir_batch_plan* plan);
+
 /* ---- channelizer ---------------------------------------------------------------------- */
 
 /* ceil(num_samples / channels). Replaces channelize_frames (src/device_ops.hpp:145). */

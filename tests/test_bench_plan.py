@@ -50,17 +50,6 @@ def test_channelizer_launches_per_step(bench, channels: int, impl: str, launches
     assert bench.chan_launches(channels, impl) == launches
 
 
-@pytest.mark.parametrize("impl,kernels,launches", [
-    ("plain", ["plain", "plain", "tc_split"], 3),
-    ("tc_split", ["tc_split"] * 97 + ["plain"], 2 + 1),
-    ("auto", ["plain"] * 257 + ["tc_split"] * 5, 2 + 1),
-    ("auto", ["plain"] * 3, 1),
-])
-def test_batch_launches_per_step(bench, impl: str, kernels: list, launches: int) -> None:
-    sizes = [(1000, 63)] * len(kernels)
-    assert bench.batch_launches(impl, sizes, kernels) == launches
-
-
 def test_rounds_cover_half_a_second_and_at_least_five(bench) -> None:
     assert bench.rounds_for(1.0) == bench.MIN_ROUNDS
     assert bench.rounds_for(0.0028) == 179          # 20 steps of 0.14 ms

@@ -1,0 +1,151 @@
+"""Batch plans (rfx_fir_batch_plan_create / rfx_fir_batch_run) on the GPU: the whole batch in ONE
+persistent launch, whatever its captures — tensor-core captures through the block-Toeplitz
+pipeline, the rest (short filters under auto, one tap, fewer than 128 samples, more taps than
+the batch kernel holds, or everything under plain) through the plain kernel's tile function
+run by groups of the same blocks' threads.
+
+Bars: tensor-core captures <= 2e-6 normwise against float64 (the tensor-core FIR's target);
+captures on the plain tile function bit-exact against the float32 chain of the project's
+kernels. rfx_fir_impl_used(..., batch=True) names the kernel of each capture, and the plan's
+own count agrees with it."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import rfx
+from oracle import rf_oracle as orc
+from rfx import signals
+
+pytestmark = pytest.mark.gpu
+
+TC_NORMWISE = 2e-6
+DEV = torch.device("cuda:0")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def no_faults():
+    rfx.load()
+    yield
+    assert rfx.device_fault() == 0
+
+
+def to_dev(captures):
+    out = []
+    for x, h in captures:
+        xd = torch.from_numpy(np.ascontiguousarray(x)).to(DEV)
+        out.append((xd, torch.full_like(xd, float("nan")),
+                    torch.from_numpy(np.ascontiguousarray(h)).to(DEV)))
+    return out
+
+
+def check(captures, dev, impl: str) -> dict:
+    torch.cuda.synchronize()
+    kinds = {"tc_split": 0, "plain": 0}
+    for i, ((x, h), (_, y, _)) in enumerate(zip(captures, dev)):
+        if x.size == 0:
+            continue
+        got = y.cpu().numpy()
+        kind = rfx.fir_impl_used(impl, h.size, x.size, batch=True)
+        kinds[kind] += 1
+        if kind == "plain":
+            want = orc.fir_f32_seq(x, h)
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (i, x.size, h.size)
+        else:
+            err = orc.normwise_error(got, orc.fir_fast(x, h))
+            assert err <= TC_NORMWISE, (i, x.size, h.size, err)
+    return kinds
+
+
+def rand_caps(spec, seed: int):
+    rng = np.random.default_rng(seed)
+    caps = []
+    for n, k in spec:
+        x = signals.to_cf32(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+        h = (rng.standard_normal(k) / np.sqrt(k)).astype(np.float32)
+        caps.append((x, h))
+    return caps
+
+
+MIXED = [(0, 63), (5, 31), (127, 1025), (128, 1025), (129, 2), (20000, 1), (16384, 255),
+         (16385, 511), (70000, 1025), (3, 1), (70000, 31), (3000, 63), (1 << 17, 127),
+         (200000, 1025), (4096, 2), (1 << 16, 255), (2305, 159), (90001, 160), (40000, 3458),
+         (30000, 8192)]
+
+
+@pytest.mark.parametrize("impl", ["auto", "tc_split", "plain"])
+def test_plan_runs_every_capture_in_one_launch(impl: str) -> None:
+    caps = rand_caps(MIXED, seed=51)
+    dev = to_dev(caps)
+    with rfx.FirBatchPlan(dev, impl) as plan:
+        info = plan.info()
+        assert info["launches"] == 1
+        plan.run()
+        kinds = check(caps, dev, impl)
+    assert info["tc_captures"] == kinds["tc_split"]
+    assert info["plain_captures"] == kinds["plain"]
+    if impl == "plain":
+        assert kinds["tc_split"] == 0
+    else:
+        assert kinds["tc_split"] > 0 and kinds["plain"] > 0
+
+
+def test_plan_holds_more_captures_than_the_parameter_table() -> None:
+    # 300 captures (the kernel-parameter form holds 96 tensor-core captures per launch).
+    caps = signals.batched_fir(count=300, log2_min=8.0, log2_max=13.0, seed=52).captures
+    dev = to_dev(caps)
+    with rfx.FirBatchPlan(dev, "tc_split") as plan:
+        assert plan.info()["launches"] == 1
+        plan.run()
+        check(caps, dev, "tc_split")
+
+
+@pytest.mark.parametrize("impl", ["auto", "tc_split"])
+def test_plan_replays_from_a_cuda_graph(impl: str) -> None:
+    caps = signals.batched_fir(count=40, log2_min=10.0, log2_max=17.0, seed=53).captures
+    dev = to_dev(caps)
+    with rfx.FirBatchPlan(dev, impl) as plan:
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(stream):
+            plan.run(stream)                      # warm-up outside the capture
+        stream.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream, capture_error_mode="relaxed"):
+            plan.run(stream)
+        for _ in range(2):
+            for _, y, _ in dev:
+                y.fill_(float("nan"))
+            graph.replay()
+            check(caps, dev, impl)
+
+
+def test_plan_sees_new_samples_between_runs() -> None:
+    caps = rand_caps([(50000, 255), (20000, 63), (1 << 16, 1025)], seed=54)
+    dev = to_dev(caps)
+    with rfx.FirBatchPlan(dev, "auto") as plan:
+        plan.run()
+        check(caps, dev, "auto")
+        caps2 = rand_caps([(50000, 255), (20000, 63), (1 << 16, 1025)], seed=55)
+        for (x2, _), (xd, _, _) in zip(caps2, dev):
+            xd.copy_(torch.from_numpy(x2))
+        plan.run()
+        check([(x2, h) for (x2, _), (_, h) in zip(caps2, caps)], dev, "auto")
+
+
+def test_plan_of_only_empty_captures_launches_nothing() -> None:
+    caps = rand_caps([(0, 63), (0, 1025)], seed=56)
+    dev = to_dev(caps)
+    with rfx.FirBatchPlan(dev, "auto") as plan:
+        assert plan.info() == {"tc_captures": 0, "plain_captures": 0, "launches": 0}
+        plan.run()
+    torch.cuda.synchronize()
+
+
+def test_plan_single_long_capture_matches_the_single_capture_kernel() -> None:
+    w = signals.long_fir(1 << 20)
+    dev = to_dev([(w.x, w.taps)])
+    with rfx.FirBatchPlan(dev, "tc_split") as plan:
+        plan.run()
+    check([(w.x, w.taps)], dev, "tc_split")

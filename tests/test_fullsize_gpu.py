@@ -15,8 +15,9 @@ the C ABI; the complete output is compared with the oracle:
   tolerance (rtol 1e-5, atol 1e-4, tests/test_pipeline.py:363-364);
 * pfb1024 (2^26 samples, 1024 channels, 32768 taps): the same bars; the per-channel error of
   each form is printed (pytest -s shows it);
-* batch256 (256 captures of 2^12 .. 2^22 samples, own taps each): every capture completely,
-  auto and tc_split; filters the library runs on the plain kernel are bit-exact.
+* batch256 (256 captures of 2^12 .. 2^22 samples, own taps each), run as one batch plan (one
+  launch): every capture completely, auto and tc_split; captures the plan runs on the plain
+  tile function are bit-exact.
 
 The oracle is the C restatement (oracle/rf_oracle.c) on every host core.
 """
@@ -193,8 +194,10 @@ def test_batch256_every_capture(batch256, impl: str) -> None:
     for x, h in caps:
         xd = torch.from_numpy(np.ascontiguousarray(x)).to(DEV)
         dev.append((xd, torch.empty_like(xd), torch.from_numpy(h).to(DEV)))
-    rfx.fir_batch(dev, impl=impl)
-    torch.cuda.synchronize()
+    with rfx.FirBatchPlan(dev, impl) as plan:   # the whole batch in one launch
+        assert plan.info()["launches"] == 1
+        plan.run()
+        torch.cuda.synchronize()
     worst = 0.0
     for i, ((x, h), (_, yd, _)) in enumerate(zip(caps, dev)):
         y = yd.cpu().numpy()
