@@ -115,6 +115,7 @@ struct BatchView {
     int sbufs;
     int plain_groups;        // groups of 256 threads running plain tiles (0: none)
     uint32_t plain_region;   // shared-memory bytes per group
+    uint32_t plain_slot;     // bytes per tile slot: region = 2 slots (pipelined) or 1
     int maps_global;         // tensor maps in global memory: fence them before first use
 };
 
@@ -854,6 +855,24 @@ __device__ __forceinline__ void batch_plain_tiles(const BatchView& p, int t0, in
     const int gtid = static_cast<int>(threadIdx.x) % kPlainThreads;
     unsigned char* region = smem + 1024 + static_cast<uint32_t>(group) * p.plain_region;
     const PlainGroupSync sync{static_cast<uint32_t>(2 + group)};
+    if (p.plain_region >= 2 * p.plain_slot) {
+        // Two slots: each tile's copy overlaps the previous tile's computation.
+        int c = 0;
+        auto source = [&](int i) {
+            const int t = t0 + group + i * p.plain_groups;
+            while (c + 1 < p.pcount && p.pcap[c + 1].tile0 <= t) {
+                ++c;
+            }
+            const PlainCapDev& pc = p.pcap[c];
+            return PlainTileRef{pc.x, pc.taps, pc.y, pc.n, pc.num_taps,
+                                static_cast<long long>(t - pc.tile0)};
+        };
+        const int count = t1 - t0 > group ? (t1 - t0 - group + p.plain_groups - 1) / p.plain_groups
+                                          : 0;
+        fir_plain_group_tiles(source, count, region, p.plain_slot, &g_fault_fir_batch, gtid, sync,
+                              [&](bool v) { return group_all(v, sync.id); });
+        return;
+    }
     uint32_t phase = 0;
     bool init = true;
     int c = 0;
@@ -894,8 +913,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 fir_batch_kernel(const __grid_constant__ BatchParams p)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const BatchView v{p.cap, p.xmap, p.smap, p.cta_item, nullptr, nullptr, p.count, 0,
-                      p.cmax, p.sbufs, 0, 0u, 0};
+    const BatchView v{p.cap,   p.xmap,  p.smap, p.cta_item, nullptr, nullptr, p.count,
+                      0,       p.cmax,  p.sbufs, 0,         0u,      0u,      0};
     batch_body<S>(v, smem);
 }
 
@@ -1064,15 +1083,12 @@ cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cuda
 
 namespace {
 
-// Cost of a work unit in microseconds of one SM, for the partition (measured on GB300 with the
-// single-capture kernels: a tensor-core tile of 96 blocks takes 12.8 us at 63 taps and 16.0 us
-// at 1025; a plain tile of 2304 outputs 1.7 us at 63 taps with four blocks per SM, here run by
-// three groups of 256 threads per SM, and about proportional to the taps beyond that).
-double tc_tile_us(int C) { return 12.4 + 0.4 * static_cast<double>(C + 1); }
-double plain_tile_us(int num_taps)
-{
-    return 2.2 * (0.5 + 0.5 * static_cast<double>(num_taps) / 63.0);
-}
+// Cost of a work unit in microseconds of one SM, for the partition. Measured on GB300 with this
+// kernel (batch plans of each tap count of the 256-capture workload alone): a tensor-core tile
+// of 96 blocks takes 18.0 to 21.2 SM-us (C = 1 .. 8); a plain tile of 2304 outputs 1.66, 2.27,
+// 3.90, 6.54, 12.6 and 24.7 SM-us at 31, 63, 127, 255, 511 and 1025 taps.
+double tc_tile_us(int C) { return 17.6 + 0.4 * static_cast<double>(C + 1); }
+double plain_tile_us(int num_taps) { return 1.0 + 0.0233 * static_cast<double>(num_taps); }
 
 constexpr int kPlainGroupsMax = kThreads / kPlainThreads;   // 3
 constexpr uint32_t kSmemMax = 227u * 1024u;
@@ -1215,11 +1231,20 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
             return cudaErrorInvalidValue;
         }
     }
+    // Plain tiles: three groups of two slots each where they fit (short filters), else as many
+    // one-slot groups as fit.
     uint32_t region = 0;
+    uint32_t slot = 0;
     int groups = 0;
     if (!pl.empty()) {
-        region = align_up(plain_layout(kmax_plain).bytes, 128);
-        groups = std::min<int>(kPlainGroupsMax, static_cast<int>((kSmemMax - 1024u) / region));
+        slot = align_up(plain_layout(kmax_plain).bytes, 128);
+        if (1024u + kPlainGroupsMax * 2u * slot <= kSmemMax) {
+            region = 2u * slot;
+            groups = kPlainGroupsMax;
+        } else {
+            region = slot;
+            groups = std::min<int>(kPlainGroupsMax, static_cast<int>((kSmemMax - 1024u) / slot));
+        }
         if (groups < 1) {
             delete plan;
             return cudaErrorInvalidValue;
@@ -1290,6 +1315,7 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
     v.sbufs = sbufs == 0 ? 2 : sbufs;
     v.plain_groups = groups;
     v.plain_region = region;
+    v.plain_slot = slot;
     v.maps_global = 1;
     const void* fn = plan->stages == 6   ? reinterpret_cast<const void*>(fir_batch_list_kernel<6>)
                      : plan->stages == 4 ? reinterpret_cast<const void*>(fir_batch_list_kernel<4>)

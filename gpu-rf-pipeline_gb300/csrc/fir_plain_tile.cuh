@@ -267,6 +267,173 @@ __device__ __forceinline__ bool fir_plain_tile(const void* __restrict__ xv,
     return true;
 }
 
+// One plain tile of a group's list (fir_plain_group_tiles).
+struct PlainTileRef {
+    const float2* x;
+    const float* taps;
+    float2* y;
+    long long n;
+    int num_taps;
+    long long tile;
+};
+
+// The tiles i = 0 .. count - 1 of one group of 256 threads (source(i) gives tile i), two slots
+// in flight: while tile i is computed from one slot, tile i + 1's samples arrive by bulk copy in
+// the other, and tile i - 1's results leave by bulk store. Per tile the arithmetic, staging and
+// results are fir_plain_tile's (same bits). Each slot (slot_bytes, at region + s * slot_bytes)
+// holds an mbarrier at offset 0 and a tile in plain_layout(K) of its tile's K. `group_all`
+// (a barrier of the group with an AND over its threads) also keeps the group in step. Returns
+// false if a copy did not arrive within the wait limit (recorded in *fault; the group stops).
+template <class Source, class Sync, class All>
+__device__ __forceinline__ bool fir_plain_group_tiles(Source source, int count,
+                                                      unsigned char* region, uint32_t slot_bytes,
+                                                      unsigned int* fault, int tid, Sync sync,
+                                                      All group_all)
+{
+    using namespace plain;
+    if (count <= 0) {
+        return true;
+    }
+    struct Geo {
+        long long t0;
+        long long base;
+        int tile_len;
+        bool interior;
+        Layout lay;
+    };
+    auto geo = [](const PlainTileRef& r) {
+        Geo g;
+        g.lay = plain_layout(r.num_taps);
+        g.t0 = r.tile * kTile;
+        g.base = (g.t0 - (r.num_taps - 1)) & ~1ll;
+        g.tile_len = static_cast<int>(g.t0 + kTile - g.base);
+        g.interior = g.base >= 0 && g.t0 + kTile <= r.n;
+        return g;
+    };
+    auto slot_of = [&](int s) { return region + static_cast<uint32_t>(s) * slot_bytes; };
+    // Bulk copy of an interior tile's samples into slot s (tid 0).
+    auto issue = [&](int s, const PlainTileRef& r, const Geo& g) {
+        if (g.interior) {
+            unsigned char* sl = slot_of(s);
+            const uint32_t bar = smem_u32(sl);
+            const uint32_t bytes = 8u * static_cast<uint32_t>(g.tile_len);
+            fence_proxy_async_smem();   // after the slot's last generic reads
+            mbar_arrive_expect_tx(bar, bytes);
+            bulk_g2s(smem_u32(sl + g.lay.tile_off) + 8u * kGuard, r.x + g.base, bytes, bar);
+        }
+    };
+    auto load_taps = [&](int s, const PlainTileRef& r, const Geo& g) {
+        f32x2* taps2 = reinterpret_cast<f32x2*>(slot_of(s) + g.lay.taps_off);
+        for (int k = tid; k < r.num_taps; k += kThreads) {
+            const float h = __ldg(r.taps + k);
+            taps2[k] = pack2(h, h);
+        }
+    };
+    // The guard and, for tiles at either end of their capture, the samples (zero outside).
+    auto fill = [&](int s, const PlainTileRef& r, const Geo& g) {
+        f32x2* guard = reinterpret_cast<f32x2*>(slot_of(s) + g.lay.tile_off);
+        f32x2* tile = guard + kGuard;
+        if (tid < kGuard) {
+            guard[tid] = 0ull;
+        }
+        if (!g.interior) {
+            for (int i = tid; i < g.tile_len; i += kThreads) {
+                const long long m = g.base + i;
+                f32x2 v = 0ull;
+                if (m >= 0 && m < r.n) {
+                    const float2 q = r.x[m];
+                    v = pack2(q.x, q.y);
+                }
+                tile[i] = v;
+            }
+        }
+    };
+
+    uint32_t phase[2] = {0u, 0u};
+    if (tid == 0) {
+        mbar_init(smem_u32(slot_of(0)), 1);
+        mbar_init(smem_u32(slot_of(1)), 1);
+        fence_mbar_init();
+    }
+    sync();
+    PlainTileRef cur = source(0);
+    {
+        const Geo g = geo(cur);
+        if (tid == 0) {
+            issue(0, cur, g);
+        }
+        load_taps(0, cur, g);
+        fill(0, cur, g);
+    }
+    sync();
+    bool ok = true;
+    for (int i = 0; i < count; ++i) {
+        const int b = i & 1;
+        const int nb = b ^ 1;
+        const bool more = i + 1 < count;
+        const PlainTileRef nxt = more ? source(i + 1) : cur;
+        // Slot nb last held tile i - 1, whose results tid 0 stored from it.
+        if (tid == 0) {
+            bulk_wait_read_all();
+            if (more) {
+                issue(nb, nxt, geo(nxt));
+            }
+        }
+        if (more) {
+            load_taps(nb, nxt, geo(nxt));
+        }
+        const Geo gc = geo(cur);
+        unsigned char* sl = slot_of(b);
+        f32x2* tile = reinterpret_cast<f32x2*>(sl + gc.lay.tile_off) + kGuard;
+        if (gc.interior) {
+            ok = mbar_wait_bounded(smem_u32(sl), phase[b], fault, kFaultTileLoad, nullptr);
+            phase[b] ^= 1u;
+        }
+        const long long n0 = gc.t0 + static_cast<long long>(kR) * tid;
+        f32x2 acc[kR];
+        if (ok && n0 < cur.n) {
+            compute_outputs(acc, tile, reinterpret_cast<f32x2*>(sl + gc.lay.taps_off),
+                            static_cast<int>(n0 - gc.base), cur.num_taps);
+        }
+        sync();   // tile i read by every thread; tid 0's wait for slot nb done
+        if (ok && n0 < cur.n) {
+#pragma unroll
+            for (int j = 0; j < kR; ++j) {
+                tile[kR * tid + j] = acc[j];
+            }
+        }
+        if (gc.interior) {
+            fence_proxy_async_smem();
+        }
+        if (more) {
+            fill(nb, nxt, geo(nxt));
+        }
+        sync();
+        if (gc.interior) {
+            if (tid == 0 && ok) {
+                bulk_s2g(cur.y + gc.t0, smem_u32(tile), 8u * kTile);
+                bulk_commit();
+            }
+        } else if (ok) {
+            const long long valid = cur.n - gc.t0 < kTile ? cur.n - gc.t0 : kTile;
+            for (int k = tid; k < valid; k += kThreads) {
+                cur.y[gc.t0 + k] = unpack2(tile[k]);
+            }
+        }
+        // Every thread is past its reads of slot b before it is refilled (next iteration's
+        // issue into slot (i + 2) & 1), and the group agrees on stopping.
+        if (!group_all(ok)) {
+            ok = false;
+            break;
+        }
+        cur = nxt;
+    }
+    if (tid == 0) {
+        bulk_wait_read_all();
+    }
+    return ok;
+}
+
 using plain::plain_layout;
 
 }  // namespace rfx

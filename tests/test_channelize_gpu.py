@@ -134,3 +134,42 @@ def test_branch_sums_are_bit_exact(n: int, k: int, m: int) -> None:
     torch.cuda.synchronize()
     want = orc.channelize_branch_f32_seq(x, h, m)
     assert np.array_equal(u.cpu().numpy().view(np.uint32), want.view(np.uint32))
+
+
+# The plain form runs in chunks of 2^21 samples (branch sums, then the inverse FFT in place,
+# chunk by chunk) once the input spans two chunks; a last chunk shorter than the others uses its
+# own FFT plan. The chunked results must match the oracle as the one-pass form does, with the
+# branch sums unchanged bit for bit.
+@pytest.mark.parametrize("m,p", [(64, 16), (1024, 32), (256, 8)])
+def test_plain_chunked_matches_oracle(m: int, p: int) -> None:
+    n = (1 << 21) * 2 + (1 << 20) + 3 * m + 5      # two whole chunks, a tail, a partial frame
+    rng = np.random.default_rng(m)
+    x = signals.to_cf32(rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    h = (rng.standard_normal(m * p) / np.sqrt(m * p)).astype(np.float32)
+    z = run(x, h, m)
+    np.testing.assert_allclose(z, orc.channelize_fast(x, h, m), rtol=CHANNELIZE_RTOL,
+                               atol=CHANNELIZE_ATOL)
+    u = rfx.channelize_branches(dev(x), dev(h), m)
+    torch.cuda.synchronize()
+    want = orc.channelize_branch_f32_seq(x, h, m)
+    assert np.array_equal(u.cpu().numpy().reshape(-1).view(np.uint32),
+                          want.reshape(-1).view(np.uint32))
+
+
+def test_plain_chunked_magnitude_and_ci16() -> None:
+    m, p = 64, 16
+    n = (1 << 21) * 3 + 1000
+    rng = np.random.default_rng(9)
+    comps = rng.integers(-32768, 32767, size=2 * n, dtype=np.int16)
+    h = (rng.standard_normal(m * p) / np.sqrt(m * p)).astype(np.float32)
+    x = orc.decode(comps, "ci16")
+    ref = orc.channelize_fast(x, h, m)
+    z = rfx.channelize_format(dev(comps), dev(h), m, "ci16", impl="plain")
+    mag = rfx.channelize_format(dev(comps), dev(h), m, "ci16", impl="plain", magnitude=True)
+    zm = rfx.channelize_magnitude(dev(x), dev(h), m, impl="plain")
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(z.cpu().numpy(), ref, rtol=CHANNELIZE_RTOL, atol=CHANNELIZE_ATOL)
+    np.testing.assert_allclose(mag.cpu().numpy(), np.abs(ref), rtol=CHANNELIZE_RTOL,
+                               atol=CHANNELIZE_ATOL)
+    np.testing.assert_allclose(zm.cpu().numpy(), np.abs(ref), rtol=CHANNELIZE_RTOL,
+                               atol=CHANNELIZE_ATOL)
