@@ -379,9 +379,6 @@ __device__ __forceinline__ bool fir_plain_group_tiles(Source source, int count,
                 issue(nb, nxt, geo(nxt));
             }
         }
-        if (more) {
-            load_taps(nb, nxt, geo(nxt));
-        }
         const Geo gc = geo(cur);
         unsigned char* sl = slot_of(b);
         f32x2* tile = reinterpret_cast<f32x2*>(sl + gc.lay.tile_off) + kGuard;
@@ -406,6 +403,9 @@ __device__ __forceinline__ bool fir_plain_group_tiles(Source source, int count,
             fence_proxy_async_smem();
         }
         if (more) {
+            // After the barrier above, so after tid 0 saw tile i - 1's store finish reading
+            // slot nb: a longer filter's taps reach into where that tile's results were.
+            load_taps(nb, nxt, geo(nxt));
             fill(nb, nxt, geo(nxt));
         }
         sync();

@@ -279,15 +279,14 @@ int tuned_chan_impl(int channels, long long n)
     return chan_tc_supported(channels, 1) ? RFX_CHAN_TC : RFX_CHAN_PLAIN;
 }
 
-// Built-in chunk: 2^21 samples (16 MB of branch sums, well inside L2 with the chunk's input
-// and output).
+// Built-in: one pass (no chunks).
 int tuned_chan_chunk_log2(int channels, long long n)
 {
     ChanEntry e;
     if (lookup_chan(channels, n, &e) && e.impl == RFX_CHAN_PLAIN) {
         return e.chunk_log2;
     }
-    return 21;
+    return 0;
 }
 
 }  // namespace rfx

@@ -149,3 +149,20 @@ def test_plan_single_long_capture_matches_the_single_capture_kernel() -> None:
     with rfx.FirBatchPlan(dev, "tc_split") as plan:
         plan.run()
     check([(w.x, w.taps)], dev, "tc_split")
+
+
+@pytest.mark.parametrize("impl", ["plain", "auto"])
+def test_plan_plain_tiles_with_tap_counts_changing_between_captures(impl: str) -> None:
+    # Plain tiles of consecutive captures share each thread group's two slots: a capture with
+    # more taps than the one before lays its taps over where the previous tile's results sat
+    # while they were being stored. Tap counts rise and fall from capture to capture, lengths
+    # put several tiles of each capture in every group, and the edge tiles of each capture
+    # (its first and last) are among them.
+    ks = [31, 63, 127, 159, 2, 159, 31, 127, 63, 159, 1, 95]
+    spec = [(2304 * 7 + 17 * i + 1, k) for i, k in enumerate(ks)]
+    caps = rand_caps(spec, seed=57)
+    dev = to_dev(caps)
+    with rfx.FirBatchPlan(dev, impl) as plan:
+        plan.run()
+        kinds = check(caps, dev, impl)
+    assert kinds["plain"] == len(ks)
