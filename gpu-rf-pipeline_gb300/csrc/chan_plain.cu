@@ -218,11 +218,9 @@ __device__ __forceinline__ f32x2 ring_lds(uint32_t addr)
 template <int kPG, int kFmt>
 __global__ void __launch_bounds__(kRingThreads, 3)
 chan_branch_ring_kernel(const void* __restrict__ x, const float* __restrict__ taps,
-                        float2* __restrict__ u, long long n, long long frame0, long long frames,
-                        int channels, int width, long long seg_frames, int guard_frames)
+                        float2* __restrict__ u, long long n, long long frames, int channels,
+                        int width, long long seg_frames, int guard_frames)
 {
-    // Frames frame0 .. frames - 1 (absolute indices; `frames` is the end), frame t written to
-    // row t - frame0 of u.
     constexpr int kN = kPG + 1;                  // register blocks
     constexpr int kP = kR * kPG;                 // taps per branch
     constexpr int kSb = kFmt == 0 ? 8 : 4;       // bytes per stored sample
@@ -232,7 +230,7 @@ chan_branch_ring_kernel(const void* __restrict__ x, const float* __restrict__ ta
     const int j = tid % width;
     const int m = static_cast<int>(blockIdx.y) * width + j;
     const long long seg = static_cast<long long>(blockIdx.x) * (kRingThreads / width) + tid / width;
-    const long long f0 = frame0 + seg * seg_frames;
+    const long long f0 = seg * seg_frames;
     if (m >= channels || f0 >= frames) {
         return;
     }
@@ -253,7 +251,7 @@ chan_branch_ring_kernel(const void* __restrict__ x, const float* __restrict__ ta
 #pragma unroll
         for (int i = 0; i < kR; ++i) {
             if (t0 + i < f1) {
-                u[(t0 + i - frame0) * channels + m] = unpack2(acc[i]);
+                u[(t0 + i) * channels + m] = unpack2(acc[i]);
             }
         }
     }
@@ -308,7 +306,7 @@ chan_branch_ring_kernel(const void* __restrict__ x, const float* __restrict__ ta
     for (int s = 0; s < kRingStages - 1; ++s) {
         issue();
     }
-    float2* dst = u + (t0 - frame0) * channels + m;
+    float2* dst = u + t0 * channels + m;
     long long dst_left = f1 - t0;
     uint32_t read_stage = 0;
     for (long long k0 = 0; k0 < nb; k0 += kN) {
@@ -369,9 +367,8 @@ chan_branch_ring_kernel(const void* __restrict__ x, const float* __restrict__ ta
     cp_async_wait<0>();
 }
 
-// Frames frame0 .. frame0 + frames - 1 into u (row 0 = frame frame0).
 static cudaError_t ring_launch(const void* x, const float* taps, float2* u, long long n,
-                               long long frame0, long long frames, int channels, int per_branch,
+                               long long frames, int channels, int per_branch,
                                cudaStream_t stream, int format)
 {
     const void* fn = nullptr;
@@ -420,37 +417,12 @@ static cudaError_t ring_launch(const void* x, const float* taps, float2* u, long
     }
     int guard_frames = kR * (per_branch / kR + 1);
     const dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(gy));
-    long long end = frame0 + frames;
-    void* args[] = {&x,   &taps,     &u, &n,           &frame0,
-                    &end, &channels, &w, &seg_frames, &guard_frames};
+    void* args[] = {&x, &taps, &u, &n, &frames, &channels, &w, &seg_frames, &guard_frames};
     err = cudaLaunchKernel(fn, grid, dim3(kRingThreads), args, 0, stream);
     if (err != cudaSuccess) {
         return err;
     }
     return cudaGetLastError();
-}
-
-bool chan_branch_ranged(int channels, int num_taps, int format)
-{
-    const int per_branch = num_taps / channels;
-    return format <= 1 && num_taps % channels == 0 && per_branch % kR == 0 && per_branch >= kR &&
-           per_branch <= 4 * kR;
-}
-
-cudaError_t chan_branch_launch_range(const void* x, const float* taps, void* u,
-                                     long long frame0, long long frames, int channels,
-                                     int num_taps, cudaStream_t stream, int format)
-{
-    if (frames == 0) {
-        return cudaSuccess;
-    }
-    if (!chan_branch_ranged(channels, num_taps, format)) {
-        return cudaErrorInvalidValue;
-    }
-    // The newest sample the range reads is x[(frame0 + frames - 1) M].
-    const long long n = (frame0 + frames - 1) * static_cast<long long>(channels) + 1;
-    return ring_launch(x, taps, static_cast<float2*>(u), n, frame0, frames, channels,
-                       num_taps / channels, stream, format);
 }
 
 cudaError_t chan_branch_launch(const void* x, const float* taps, void* u, long long frames,
@@ -462,9 +434,10 @@ cudaError_t chan_branch_launch(const void* x, const float* taps, void* u, long l
     {
         const long long n = (frames - 1) * static_cast<long long>(channels) + 1;
         const int per_branch = num_taps / channels;
-        if (chan_branch_ranged(channels, num_taps, format)) {
-            return ring_launch(x, taps, static_cast<float2*>(u), n, 0, frames, channels,
-                               per_branch, stream, format);
+        if (format <= 1 && num_taps % channels == 0 && per_branch % kR == 0 &&
+            per_branch >= kR && per_branch <= 4 * kR) {
+            return ring_launch(x, taps, static_cast<float2*>(u), n, frames, channels, per_branch,
+                               stream, format);
         }
     }
     // The newest sample any frame reads is the last frame's x[(frames - 1) M], which lies in the

@@ -174,13 +174,6 @@ struct rfx_chan_plan {
     int64_t frames;       // cuFFT batch (plain); maximum frames (tensor core)
     cufftHandle fft;
     bool has_fft;
-    // Plain form in chunks: branch sums then the inverse FFT in place, chunk by chunk, so each
-    // chunk's branch sums are still in L2 when the FFT reads them (0: one pass over all frames).
-    int64_t chunk_frames;
-    cufftHandle fft_chunk;    // batch chunk_frames
-    cufftHandle fft_tail;     // batch frames % chunk_frames (if not 0)
-    bool has_chunk;
-    bool has_tail;
     void* twiddles;       // tensor core: the DFT operand image, built once in FP64
     void* scratch;        // plain: channel outputs before their magnitude (first such call);
                           // tensor core, 1024 channels: the branch sums (made with the plan)
@@ -510,14 +503,6 @@ int64_t rfx_channelize_frames(int64_t num_samples, int channels)
 
 int rfx_chan_plan_create(int impl, int channels, int64_t max_samples, rfx_chan_plan** plan)
 {
-    return rfx::chan_plan_create_chunked(impl, channels, max_samples, -1, plan);
-}
-
-}  // extern "C"
-
-int rfx::chan_plan_create_chunked(int impl, int channels, long long max_samples, int chunk_log2,
-                                  rfx_chan_plan** plan)
-{
     if (plan == nullptr) {
         return fail(RFX_ERR_INVALID, "channelize: null plan pointer");
     }
@@ -535,10 +520,8 @@ int rfx::chan_plan_create_chunked(int impl, int channels, long long max_samples,
         return fail(RFX_ERR_INVALID, "channelize: %lld samples, expected 0 to %lld",
                     static_cast<long long>(max_samples), static_cast<long long>(kMaxSamples));
     }
-    auto* p = new rfx_chan_plan{impl,  channels, rfx_channelize_frames(max_samples, channels),
-                                0,     false,    0,
-                                0,     0,        false,
-                                false, nullptr,  nullptr};
+    auto* p = new rfx_chan_plan{impl, channels, rfx_channelize_frames(max_samples, channels), 0,
+                                false, nullptr, nullptr};
     if (impl == RFX_CHAN_TC) {
         const bool wide = rfx::chan_wide_supported(channels);
         if (!wide && !rfx::chan_tc_supported(channels, 1)) {
@@ -581,39 +564,10 @@ int rfx::chan_plan_create_chunked(int impl, int channels, long long max_samples,
             return cufft_fail(r, "cufftPlanMany");
         }
         p->has_fft = true;
-        // Chunks of 2^chunk_log2 samples (built in: 2^21, 16 MB of branch sums): a chunk's
-        // input, branch sums and channel outputs stay inside the 129 MB L2 between the kernels.
-        if (chunk_log2 < 0) {
-            chunk_log2 = rfx::tuned_chan_chunk_log2(channels, max_samples);
-        }
-        const int64_t chunk =
-            std::max<int64_t>(8, ((int64_t{1} << std::min(chunk_log2, 30)) / channels) / 8 * 8);
-        if (chunk_log2 > 0 && p->frames >= 2 * chunk) {
-            p->chunk_frames = chunk;
-            cufftResult rc = cufftPlanMany(&p->fft_chunk, 1, &nfft, nullptr, 1, nfft, nullptr, 1,
-                                           nfft, CUFFT_C2C, static_cast<int>(chunk));
-            p->has_chunk = rc == CUFFT_SUCCESS;
-            const int64_t tail = p->frames % chunk;
-            if (rc == CUFFT_SUCCESS && tail > 0) {
-                rc = cufftPlanMany(&p->fft_tail, 1, &nfft, nullptr, 1, nfft, nullptr, 1, nfft,
-                                   CUFFT_C2C, static_cast<int>(tail));
-                p->has_tail = rc == CUFFT_SUCCESS;
-            }
-            if (rc != CUFFT_SUCCESS) {
-                if (p->has_chunk) {
-                    cufftDestroy(p->fft_chunk);
-                }
-                cufftDestroy(p->fft);
-                delete p;
-                return cufft_fail(rc, "cufftPlanMany (chunks)");
-            }
-        }
     }
     *plan = p;
     return RFX_OK;
 }
-
-extern "C" {
 
 int rfx_chan_plan_destroy(rfx_chan_plan* plan)
 {
@@ -623,12 +577,6 @@ int rfx_chan_plan_destroy(rfx_chan_plan* plan)
     cufftResult r = CUFFT_SUCCESS;
     if (plan->has_fft) {
         r = cufftDestroy(plan->fft);
-    }
-    if (plan->has_chunk) {
-        cufftDestroy(plan->fft_chunk);
-    }
-    if (plan->has_tail) {
-        cufftDestroy(plan->fft_tail);
     }
     if (plan->twiddles != nullptr) {
         cudaFree(plan->twiddles);
@@ -755,35 +703,6 @@ int channelize_plan(rfx_chan_plan* plan, const void* x, const float* taps, void*
             }
         }
         z = plan->scratch;
-    }
-    if (plan->has_chunk && rfx::chan_branch_ranged(plan->channels, num_taps, format)) {
-        // Chunk by chunk: branch sums, inverse FFT in place (and the magnitudes), so the FFT
-        // reads the branch sums from L2 and HBM sees the input once and the output once.
-        const int64_t m = plan->channels;
-        for (int64_t f0 = 0; f0 < frames; f0 += plan->chunk_frames) {
-            const int64_t nf = std::min(plan->chunk_frames, frames - f0);
-            cufftComplex* zc = static_cast<cufftComplex*>(z) + f0 * m;
-            cudaError_t err = rfx::chan_branch_launch_range(x, taps, zc, f0, nf, plan->channels,
-                                                            num_taps, stream, format);
-            if (err != cudaSuccess) {
-                return cuda_fail(err, "chan_branch_launch_range");
-            }
-            const cufftHandle h = nf == plan->chunk_frames ? plan->fft_chunk : plan->fft_tail;
-            cufftResult r = cufftSetStream(h, stream);
-            if (r == CUFFT_SUCCESS) {
-                r = cufftExecC2C(h, zc, zc, CUFFT_INVERSE);
-            }
-            if (r != CUFFT_SUCCESS) {
-                return cufft_fail(r, "cufftExecC2C (chunk)");
-            }
-            if (magnitude) {
-                err = rfx::magnitude_launch(zc, static_cast<float*>(out) + f0 * m, nf * m, stream);
-                if (err != cudaSuccess) {
-                    return cuda_fail(err, "magnitude_launch");
-                }
-            }
-        }
-        return RFX_OK;
     }
     cudaError_t err = rfx::chan_branch_launch(x, taps, z, frames, plan->channels, num_taps,
                                               stream, format);

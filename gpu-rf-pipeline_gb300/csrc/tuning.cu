@@ -41,7 +41,6 @@ struct FirEntry {
 
 struct ChanEntry {
     int impl;
-    int chunk_log2;   // plain form: log2 of its chunk in samples, 0 for one pass
     double ms;
 };
 
@@ -120,7 +119,7 @@ std::string device_key()
 
 // Text format, one entry per line:
 //   fir  <device key> <taps bucket> <length bucket> <impl> <tile blocks> <stages> <ms>
-//   chan <device key> <channels> <length bucket> <impl> <chunk log2> <ms>
+//   chan <device key> <channels> <length bucket> <impl> <ms>
 int load_table(const char* path)
 {
     FILE* f = std::fopen(path, "r");
@@ -144,11 +143,9 @@ int load_table(const char* path)
             (impl == RFX_FIR_PLAIN || impl == RFX_FIR_TC)) {
             g_fir[{a, b}] = FirEntry{impl, TcConfig{blocks, stages}, ms};
         } else if (std::strcmp(kind, "chan") == 0 &&
-                   std::sscanf(line, "%*s %*s %d %d %d %d %lf", &a, &b, &impl, &blocks, &ms) ==
-                       5 &&
-                   (impl == RFX_CHAN_PLAIN || impl == RFX_CHAN_TC) && blocks >= 0 &&
-                   blocks <= 30) {
-            g_chan[{a, b}] = ChanEntry{impl, blocks, ms};
+                   std::sscanf(line, "%*s %*s %d %d %d %lf", &a, &b, &impl, &ms) == 4 &&
+                   (impl == RFX_CHAN_PLAIN || impl == RFX_CHAN_TC)) {
+            g_chan[{a, b}] = ChanEntry{impl, ms};
         }
     }
     std::fclose(f);
@@ -279,16 +276,6 @@ int tuned_chan_impl(int channels, long long n)
     return chan_tc_supported(channels, 1) ? RFX_CHAN_TC : RFX_CHAN_PLAIN;
 }
 
-// Built-in: one pass (no chunks).
-int tuned_chan_chunk_log2(int channels, long long n)
-{
-    ChanEntry e;
-    if (lookup_chan(channels, n, &e) && e.impl == RFX_CHAN_PLAIN) {
-        return e.chunk_log2;
-    }
-    return 0;
-}
-
 }  // namespace rfx
 
 extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, double* best_out)
@@ -355,18 +342,10 @@ extern "C" int rfx_autotune_channelize(int channels, int num_taps, int64_t num_s
         cudaGetLastError();
         return RFX_ERR_CUDA;
     }
-    ChanEntry best{RFX_CHAN_PLAIN, 0, 1e30};
-    struct Candidate {
-        int impl;
-        int chunk_log2;
-    };
-    const Candidate candidates[] = {{RFX_CHAN_PLAIN, 0},  {RFX_CHAN_PLAIN, 20},
-                                    {RFX_CHAN_PLAIN, 21}, {RFX_CHAN_PLAIN, 22},
-                                    {RFX_CHAN_TC, 0}};
-    for (const Candidate& cand : candidates) {
+    ChanEntry best{RFX_CHAN_PLAIN, 1e30};
+    for (int impl : {RFX_CHAN_PLAIN, RFX_CHAN_TC}) {
         rfx_chan_plan* plan = nullptr;
-        if (chan_plan_create_chunked(cand.impl, channels, num_samples, cand.chunk_log2, &plan) !=
-            RFX_OK) {
+        if (rfx_chan_plan_create(impl, channels, num_samples, &plan) != RFX_OK) {
             continue;  // e.g. no tensor-core form at this channel count
         }
         const double ms = best_ms([&]() {
@@ -377,7 +356,7 @@ extern "C" int rfx_autotune_channelize(int channels, int num_taps, int64_t num_s
         });
         rfx_chan_plan_destroy(plan);
         if (ms >= 0 && ms < best.ms) {
-            best = ChanEntry{cand.impl, cand.chunk_log2, ms};
+            best = ChanEntry{impl, ms};
         }
     }
     if (best.ms >= 1e29) {
@@ -411,8 +390,8 @@ extern "C" int rfx_autotune_save(const char* path)
                      kv.second.config.stages, kv.second.ms);
     }
     for (const auto& kv : g_chan) {
-        std::fprintf(f, "chan %s %d %d %d %d %.6f\n", key.c_str(), kv.first.first,
-                     kv.first.second, kv.second.impl, kv.second.chunk_log2, kv.second.ms);
+        std::fprintf(f, "chan %s %d %d %d %.6f\n", key.c_str(), kv.first.first, kv.first.second,
+                     kv.second.impl, kv.second.ms);
     }
     std::fclose(f);
     return RFX_OK;
