@@ -393,11 +393,6 @@ class BatchArm:
         self.caps = self.X = self.Y = self.graph = self.plan = None
 
 
-def auto_picks_tc(num_taps: int, n: int) -> bool:
-    """The library's built-in auto rule (tuning.cu): tensor core from 160 taps and 2^16 samples."""
-    return num_taps >= 160 and n >= (1 << 16)
-
-
 def chan_launches(channels: int, impl: str) -> int:
     """Kernel launches per channelizer step: plain = branch sums + cuFFT's inverse (counted as
     one of ours); tensor core = one fused kernel at 64 channels, branch sums + DFT kernel at
@@ -408,8 +403,9 @@ def chan_launches(channels: int, impl: str) -> int:
 
 def arm_order(w) -> list[str]:
     """Arms to time, the headline first: auto first where it is not simply the tensor-core
-    form (the short FIR, the batch, and the channelizer above 64 channels, whose plain form is
-    faster) — it is the arm a user runs."""
+    form at the headline's own configuration (the short FIR, where it picks the short-filter
+    tensor-core form over the exact plain kernel; the batch; and the channelizer above 64
+    channels, whose plain form is faster) — it is the arm a user runs."""
     auto_first = bool(w.captures or (not w.channels and w.taps.size < 160)
                       or (w.channels and w.channels != 64))
     return ["auto", "tc_split", "plain"] if auto_first else ["tc_split", "plain"]
@@ -828,6 +824,7 @@ def magnitude_fusion(rfx, w, args, dist, device) -> dict:
 NCU_TRAFFIC_BYTES = {
     ("fir1025_tones", "tc_split"): 134.5e6 + 80.1e6,   # profiles/fir_tc_fir1025_full.md
     ("fir63_white", "plain"): 134.2e6 + 89.1e6,        # profiles/fir_plain_fir63_full.md
+    ("fir63_white", "tc_split"): 134.3e6 + 79.6e6,     # profiles/fir_tcs_fir63_full.md
     ("pfb64", "tc_split"): 134.4e6 + 83.2e6,           # profiles/chan_tc_pfb64_full.md
 }
 
@@ -845,12 +842,15 @@ def useful_flops(w) -> float:
 
 def roofline_of(w, res: dict, n: int, pk: dict) -> dict:
     """Roofline of one arm's step: tensor-bound (useful FIR flops over the measured bf16 peak)
-    for the tensor-core FIR and the tensor-core batch; HBM-bound (16 B per sample: 8 read and 8
-    written, over the measured copy bandwidth) for everything else."""
+    for the long-filter tensor-core FIR (over 129 taps) and the tensor-core batch; HBM-bound (16 B
+    per sample: 8 read and 8 written, over the measured copy bandwidth) for everything else,
+    including the short-filter tensor-core form, which moves each sample through HBM once and
+    whose tensor work is a fraction of its time."""
     step_s = res["step_s"]
     gbs = 16.0 * n / step_s / 1e9
     kernel = res["kernel"]
-    if kernel == "tc_split" and not w.channels:
+    short_tc = kernel == "tc_split" and not w.channels and not w.captures and w.taps.size <= 129
+    if kernel == "tc_split" and not w.channels and not short_tc:
         tflops = useful_flops(w) / step_s / 1e12
         r = {"bound": "tensor", "achieved": tflops, "peak": pk["bf16_tflops"],
              "unit": "TFLOP/s", "frac": tflops / pk["bf16_tflops"], "traffic": None,

@@ -1151,7 +1151,8 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
         if (c.num_samples == 0) {
             continue;
         }
-        const int want = impl == RFX_FIR_AUTO ? tuned_fir_impl(c.num_taps, c.num_samples) : impl;
+        const int want =
+            impl == RFX_FIR_AUTO ? tuned_fir_batch_impl(c.num_taps, c.num_samples) : impl;
         const bool use_tc = want == RFX_FIR_TC && c.num_samples >= kB &&
                             fir_batch_supported(c.num_taps);
         if (use_tc) {

@@ -47,6 +47,7 @@
 #include "fir_plain.cuh"
 #include "fir_tc2.cuh"
 #include "tuning.hpp"
+#include "sample_fmt.cuh"
 #include "tc_common.cuh"
 #include "tmap.hpp"
 
@@ -189,73 +190,6 @@ __device__ __forceinline__ void h_group_range(const HGroups& g, int P, int gi, i
         c0 = (gi - st0 * g.gpk) * g.cpg;
         c1 = min(P, c0 + g.cpg);
     }
-}
-
-__host__ __device__ constexpr int component_bytes(int fmt) { return fmt == 0 ? 4 : fmt == 1 ? 2 : 1; }
-
-// Sample formats of x: 0 = cf32; 1 = ci16 and 2 = ci8, whose components decode as the
-// project's SigMF reader converts them (src/io.cpp:110-148): v / 32768 and v / 128, both exact
-// in float32, so a decoded run has the bits of a run over the converted samples.
-__device__ __forceinline__ float4 decode_ci16x2(uint2 w)
-{
-    constexpr float k = 1.0f / 32768.0f;
-    return make_float4(static_cast<float>(static_cast<int>(w.x << 16) >> 16) * k,
-                       static_cast<float>(static_cast<int>(w.x) >> 16) * k,
-                       static_cast<float>(static_cast<int>(w.y << 16) >> 16) * k,
-                       static_cast<float>(static_cast<int>(w.y) >> 16) * k);
-}
-
-__device__ __forceinline__ float4 decode_ci8x2(uint32_t w)
-{
-    constexpr float k = 1.0f / 128.0f;
-    return make_float4(static_cast<float>(static_cast<int>(w << 24) >> 24) * k,
-                       static_cast<float>(static_cast<int>(w << 16) >> 24) * k,
-                       static_cast<float>(static_cast<int>(w << 8) >> 24) * k,
-                       static_cast<float>(static_cast<int>(w) >> 24) * k);
-}
-
-// Samples s, s + 1 (s even) from shared memory holding components in format fmt at `addr`
-// (the first of the pair): re0, im0, re1, im1.
-__device__ __forceinline__ float4 lds_pair(uint32_t addr, int fmt)
-{
-    if (fmt == 0) {
-        return lds128(addr);
-    }
-    if (fmt == 1) {
-        uint2 w;
-        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(w.x), "=r"(w.y) : "r"(addr) : "memory");
-        return decode_ci16x2(w);
-    }
-    uint32_t w;
-    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(addr) : "memory");
-    return decode_ci8x2(w);
-}
-
-// Samples s, s + 1 of x (s even, s + 1 < n), and sample s alone, from global memory.
-__device__ __forceinline__ float4 ldg_pair(const void* x, int fmt, long long s)
-{
-    if (fmt == 0) {
-        return __ldg(reinterpret_cast<const float4*>(static_cast<const float2*>(x) + s));
-    }
-    if (fmt == 1) {
-        return decode_ci16x2(__ldg(reinterpret_cast<const uint2*>(static_cast<const short2*>(x) + s)));
-    }
-    return decode_ci8x2(__ldg(reinterpret_cast<const unsigned int*>(static_cast<const char2*>(x) + s)));
-}
-
-__device__ __forceinline__ float2 ldg_one(const void* x, int fmt, long long s)
-{
-    if (fmt == 0) {
-        return __ldg(static_cast<const float2*>(x) + s);
-    }
-    if (fmt == 1) {
-        const short2 v = __ldg(static_cast<const short2*>(x) + s);
-        return make_float2(static_cast<float>(v.x) * (1.0f / 32768.0f),
-                           static_cast<float>(v.y) * (1.0f / 32768.0f));
-    }
-    const char2 v = __ldg(static_cast<const char2*>(x) + s);
-    return make_float2(static_cast<float>(v.x) * (1.0f / 128.0f),
-                       static_cast<float>(v.y) * (1.0f / 128.0f));
 }
 
 }  // namespace
@@ -899,6 +833,9 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
         // Shorter than one block: the tensor map would be empty; the plain kernel is exact.
         return fir_plain_launch(x, taps, y, n, num_taps, stream);
     }
+    if (config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)) {
+        return fir_tcs_launch(0, x, taps, y, n, num_taps, stream);
+    }
     return launch_single(0, x, taps, y, n, num_taps, config.stages, stream);
 }
 
@@ -920,7 +857,10 @@ cudaError_t fir_tc_launch_format(int format, const void* x, const float* taps, v
     if (n < kB) {
         return fir_plain_launch_format(format, x, taps, y, n, num_taps, stream);
     }
-    // Integer input runs in the single-CTA form, whichever form the tuner chose for cf32.
+    if (config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)) {
+        return fir_tcs_launch(format, x, taps, y, n, num_taps, stream);
+    }
+    // Otherwise integer input runs in the single-CTA form (also where cf32 runs the pair form).
     return launch_single(format, x, taps, y, n, num_taps,
                          config.tile_blocks == kTcPairTile ? 6 : config.stages, stream);
 }
@@ -933,6 +873,9 @@ long long fir_tc_tile_outputs(int num_taps, long long n, TcConfig config)
     if (config.tile_blocks == kTcPairTile && n >= 2 * kB && fir_tc2_supported(num_taps)) {
         return 96LL * 256;
     }
+    if (n >= kB && config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)) {
+        return fir_tcs_tile_outputs();
+    }
     return n < kB ? 1 : static_cast<long long>(kNB) * kB;
 }
 
@@ -941,7 +884,12 @@ long long fir_tc_tile_outputs_format(int format, int num_taps, long long n, TcCo
     if (format == 0) {
         return fir_tc_tile_outputs(num_taps, n, config);
     }
-    return n <= 0 || n < kB || !fir_tc_supported(num_taps) ? 1 : static_cast<long long>(kNB) * kB;
+    if (n <= 0 || n < kB || !fir_tc_supported(num_taps)) {
+        return 1;
+    }
+    return config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)
+               ? fir_tcs_tile_outputs()
+               : static_cast<long long>(kNB) * kB;
 }
 
 cudaError_t fir_tc_take_fault(unsigned int* code)
@@ -978,7 +926,7 @@ cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int coun
             if (cap.num_samples == 0) {
                 continue;
             }
-            if (tuned_fir_impl(cap.num_taps, cap.num_samples) == RFX_FIR_TC) {
+            if (tuned_fir_batch_impl(cap.num_taps, cap.num_samples) == RFX_FIR_TC) {
                 tc.push_back(cap);
                 continue;
             }

@@ -206,6 +206,11 @@ int rfx_device_fault(unsigned int* code)
     }
     total |= part;
     part = 0;
+    if ((err = rfx::fir_tcs_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "fir_tcs fault word");
+    }
+    total |= part;
+    part = 0;
     if ((err = rfx::fir_tc2_take_fault(&part)) != cudaSuccess) {
         return cuda_fail(err, "fir_tc2 fault word");
     }
@@ -324,7 +329,10 @@ int rfx_fir_impl_used(int impl, int num_taps, int64_t num_samples, int batch, in
         return fail(RFX_ERR_INVALID, "fir_impl_used: %d taps, %lld samples", num_taps,
                     static_cast<long long>(num_samples));
     }
-    int r = resolve_fir_impl(impl, num_taps, num_samples);
+    int r = impl == RFX_FIR_AUTO && batch != 0
+                ? resolve_fir_impl(rfx::tuned_fir_batch_impl(num_taps, num_samples), num_taps,
+                                   num_samples)
+                : resolve_fir_impl(impl, num_taps, num_samples);
     constexpr int64_t kBlockOutputs = 128;  // the tensor-core kernels' output block
     if (r == RFX_FIR_TC && num_samples < kBlockOutputs) {
         r = RFX_FIR_PLAIN;  // no whole block to compute: the plain kernel is exact

@@ -50,6 +50,19 @@ __device__ __forceinline__ void mma_f16_acc(uint32_t d_tmem, unsigned long long 
         : "memory");
 }
 
+// One lane of a fully active warp (the same lane every time): the lane that issues a warp's
+// MMAs and commits. Running the issue loop on the whole warp and electing the issuer keeps
+// the loop's values (descriptors, TMEM addresses, counters) warp-uniform, so they can live in
+// the uniform registers the MMA instruction reads, instead of being moved there per MMA.
+__device__ __forceinline__ bool elect_one()
+{
+    uint32_t pred = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\telect.sync _|p, 0xffffffff;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(pred));
+    return pred != 0;
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar)
 {
     asm volatile(

@@ -239,13 +239,32 @@ double best_ms(Run run)
 }  // namespace
 
 // Built-in rule before tuning: the tensor-core form once the filter is long enough for FP32
-// FMA throughput to bound the plain kernel (measured on GB300: plain is HBM-bound and faster up
-// to about 130 taps, the tensor-core form from about 250) and the input fills the GPU; the
-// plain kernel otherwise.
+// FMA throughput to bound the plain kernel and the input fills the GPU; the plain kernel
+// otherwise. Measured on GB300 at 2^24 samples: the plain kernel is HBM-bound up to about 24
+// taps (42-49 us) and FMA-bound beyond (79 us at 63 taps, 149 us at 129); the short-filter
+// tensor-core form takes 48-54 us from 2 to 129 taps, the long-filter form ~115 us from 130 to
+// about 500 taps.
 int tuned_fir_impl(int num_taps, long long n)
 {
     FirEntry e;
     if (lookup_fir(num_taps, n, &e)) {
+        return e.impl;
+    }
+    constexpr int kTcMinTaps = 32;
+    constexpr long long kTcMinSamples = 1LL << 16;
+    return num_taps >= kTcMinTaps && n >= kTcMinSamples && fir_tc_supported(num_taps)
+               ? RFX_FIR_TC
+               : RFX_FIR_PLAIN;
+}
+
+// Where the batch kernels place a capture. Their tensor-core kernel is the long-filter form
+// (fir_batch.cu), whose tiles cost about the same whatever the filter, so short filters stay
+// on the plain tiles: the tensor core from 160 taps (plain and the long-filter form meet near
+// 130), or where a tuned entry for a filter beyond the short form's range says so.
+int tuned_fir_batch_impl(int num_taps, long long n)
+{
+    FirEntry e;
+    if (!fir_tcs_supported(num_taps) && lookup_fir(num_taps, n, &e)) {
         return e.impl;
     }
     constexpr int kTcMinTaps = 160;
@@ -261,7 +280,8 @@ TcConfig tuned_fir_tc_config(int num_taps, long long n)
     if (lookup_fir(num_taps, n, &e) && e.impl == RFX_FIR_TC) {
         return e.config;
     }
-    return TcConfig{96, 6};
+    // The short-filter form where it applies (one copy of each window, no scan slices).
+    return fir_tcs_supported(num_taps) ? TcConfig{kTcShortTile, 4} : TcConfig{96, 6};
 }
 
 // Built-in rule: the fused tensor-core form at 64 channels (one HBM pass against the plain
@@ -303,6 +323,9 @@ extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, dou
         }
         for (int st : {2, 4, 6}) {
             candidates.push_back({RFX_FIR_TC, TcConfig{kTcPairTile, st}});
+        }
+        if (fir_tcs_supported(num_taps)) {
+            candidates.push_back({RFX_FIR_TC, TcConfig{kTcShortTile, 4}});
         }
     }
     FirEntry best{RFX_FIR_PLAIN, TcConfig{96, 6}, 1e30};

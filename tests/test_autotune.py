@@ -11,7 +11,7 @@ from pathlib import Path
 from conftest import PKG, ROOT
 
 PICK = ("import sys; sys.path[:0] = [{root!r}, {pkg!r}]; import rfx; "
-        "print(rfx.fir_impl_used('auto', 63, 1 << 24), rfx.fir_impl_used('auto', 1025, 1 << 24))")
+        "print(rfx.fir_impl_used('auto', 24, 1 << 24), rfx.fir_impl_used('auto', 1025, 1 << 24))")
 
 
 def picks(env_file: Path | None) -> list[str]:
@@ -31,11 +31,11 @@ def test_builtin_rule_without_a_table() -> None:
 
 def test_table_named_by_the_environment_is_loaded_before_the_first_lookup(tmp_path) -> None:
     f = tmp_path / "tune.txt"
-    # taps bucket 5 (32-63) and 10 (1024-2047), length bucket 24: swap both choices; a line for
+    # taps bucket 4 (16-31) and 10 (1024-2047), length bucket 24: swap both choices; a line for
     # another device and a malformed line are skipped.
-    f.write_text("fir unknown 5 24 1 96 6 0.100000\n"
+    f.write_text("fir unknown 4 24 1 48 4 0.100000\n"
                  "fir unknown 10 24 0 0 0 0.200000\n"
-                 "fir NVIDIA_Other/1 5 24 0 0 0 0.1\n"
+                 "fir NVIDIA_Other/1 4 24 0 0 0 0.1\n"
                  "garbage line\n")
     assert picks(f) == ["tc_split", "plain"]
 

@@ -30,7 +30,7 @@ def workload(taps: int, channels: int = 0, captures: int = 0) -> Workload:
 
 @pytest.mark.parametrize("w,first", [
     (workload(1025), "tc_split"),                 # long FIR: the tensor-core form leads
-    (workload(63), "auto"),                       # short FIR: auto (= plain) leads
+    (workload(63), "auto"),                       # short FIR: auto leads
     (workload(1024, channels=64), "tc_split"),    # 64-channel channelizer
     (workload(32768, channels=1024), "auto"),     # 1024 channels: auto (= plain) leads
     (workload(1025, captures=3), "auto"),         # the batch

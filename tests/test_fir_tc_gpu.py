@@ -92,6 +92,54 @@ def test_tc_lengths(n: int) -> None:
     assert orc.normwise_error(y, orc.fir_fast(x, h)) <= TC_NORMWISE
 
 
+SHORT_TILE = 48 * 128  # outputs per tile of the short-filter form (2 to 129 taps)
+
+
+@pytest.mark.parametrize("k", [2, 63, 113, 114, 129])
+@pytest.mark.parametrize("n", [128, 129, 255, 49 * 128 + 5, SHORT_TILE - 1, SHORT_TILE,
+                               SHORT_TILE + 1, 3 * SHORT_TILE + 77, 152 * SHORT_TILE + 300])
+def test_tc_short_form_lengths(k: int, n: int) -> None:
+    # Tile edges of the short-filter form, its partial last block (outside the tensor map, read
+    # from global memory into the window), windows reaching past the input, and grids with
+    # more tiles than SMs; 113 and 114 taps bracket the first K-step that needs the previous
+    # block's taps.
+    x, h = rand_case(n, k, seed=n + k)
+    y = run(x, h)
+    assert orc.normwise_error(y, orc.fir_fast(x, h)) <= TC_NORMWISE
+
+
+def test_tc_short_form_per_tile_scale_spans_extreme_levels() -> None:
+    x, h = rand_case(6 * SHORT_TILE, 63, seed=12)
+    levels = np.array([1.0, 1e-30, 1e30, 3.0, 1e-12, 1.0])
+    x = (x * np.repeat(levels, SHORT_TILE).astype(np.float32)).astype(np.complex64)
+    y = run(x, h)
+    ref = orc.fir_fast(x, h)
+    assert orc.normwise_error(y, ref) <= TC_NORMWISE
+    for t in range(6):
+        if t > 0 and levels[t - 1] > levels[t]:
+            continue
+        seg = slice(t * SHORT_TILE + 128, (t + 1) * SHORT_TILE)
+        assert orc.normwise_error(y[seg], ref[seg]) <= TC_NORMWISE, t
+
+
+@pytest.mark.parametrize("fmt", ["ci16", "ci8"])
+def test_tc_short_form_integer_input_matches_converted(fmt: str) -> None:
+    # Integer recordings decoded in the short form's load stage give the bits of a run over
+    # the host-converted samples.
+    n, k = 3 * SHORT_TILE + 333, 63
+    rng = np.random.default_rng(21)
+    info = np.iinfo(np.int16 if fmt == "ci16" else np.int8)
+    raw = rng.integers(info.min, info.max + 1, size=2 * n).astype(info.dtype)
+    conv = (raw.astype(np.float32) / (32768.0 if fmt == "ci16" else 128.0)).view(np.complex64)
+    h = rand_case(1, k, seed=4)[1]
+    hd = torch.from_numpy(h).to(DEV)
+    yf = torch.empty(n, dtype=torch.complex64, device=DEV)
+    rfx.fir_launch_format("tc_split", fmt, torch.from_numpy(raw).to(DEV), hd, yf, num_samples=n)
+    yc = rfx.fir(torch.from_numpy(conv).to(DEV), hd, impl="tc_split")
+    torch.cuda.synchronize()
+    assert np.array_equal(yf.cpu().numpy().view(np.uint32), yc.cpu().numpy().view(np.uint32))
+
+
 @pytest.mark.parametrize("k", [TC_MAX_TAPS + 1, 8192])
 def test_tc_beyond_capacity_uses_the_plain_kernel(k: int) -> None:
     x, h = rand_case(30000, k, seed=3)
@@ -152,7 +200,7 @@ def test_tc_host_path() -> None:
     assert bench.kernel_ms_mean > 0
 
 
-@pytest.mark.parametrize("k", [255, 1025])
+@pytest.mark.parametrize("k", [63, 255, 1025])
 def test_tc_sixty_db_level_steps_per_block(k: int) -> None:
     # Every 128-output block at its own level, 1 or 1e-3 at random (60 dB steps inside every
     # tile, the workload's dynamic range). The split operands are floating point, so a quiet

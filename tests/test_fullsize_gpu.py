@@ -6,9 +6,10 @@ the C ABI; the complete output is compared with the oracle:
 * fir1025 (2^24 samples, 1025 Kaiser taps, 8 tones over 60 dB + noise): tc_split and auto,
   normwise error <= 2e-6 against float64 over the whole output and within every 2^16-output
   segment (so a wrong stretch far into the capture cannot hide behind the global maximum);
-* fir63 (2^24 samples, 63 taps): plain and auto, bit-exact against the float32 restatement of
-  the project's FIR kernels (one fma per tap in tap order, tests/test_pipeline.py:116-135 holds
-  them to 1e-5);
+* fir63 (2^24 samples, 63 taps): plain bit-exact against the float32 restatement of the
+  project's FIR kernels (one fma per tap in tap order, tests/test_pipeline.py:116-135 holds
+  them to 1e-5); tc_split and auto (the short-filter tensor-core form) <= 2e-6 normwise over the
+  whole output and every 2^16-output segment;
 * pfb64 (2^24 samples, 64 channels, 1024 taps): tc_split <= 2e-6 normwise, and per channel
   (against each channel's own level) within 2.5x of the FP32 cuFFT form; plain: branch sums
   bit-exact against the float32 restatement and the channels within the project's channelizer
@@ -93,16 +94,17 @@ def fir63():
     return w, orc.fir_f32_seq(w.x, w.taps)
 
 
-@pytest.mark.parametrize("impl", ["plain", "auto"])
-def test_fir63_full_output_bit_exact(fir63, impl: str) -> None:
+def test_fir63_full_output_bit_exact(fir63) -> None:
     w, ref32 = fir63
-    y = fir_on_gpu(w, impl)
+    y = fir_on_gpu(w, "plain")
     assert np.array_equal(y.view(np.uint32), ref32.view(np.uint32))
 
 
-def test_fir63_tensor_core_full_output(fir63) -> None:
+@pytest.mark.parametrize("impl", ["tc_split", "auto"])
+def test_fir63_tensor_core_full_output(fir63, impl: str) -> None:
     w, _ = fir63
-    y = fir_on_gpu(w, "tc_split")
+    assert rfx.fir_impl_used(impl, w.taps.size, w.x.size) == "tc_split"
+    y = fir_on_gpu(w, impl)
     ref = orc.fir_fast(w.x, w.taps)
     assert orc.normwise_error(y, ref) <= TC_NORMWISE
     assert worst_segment(y, ref) <= TC_NORMWISE
