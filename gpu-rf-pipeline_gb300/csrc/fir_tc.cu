@@ -833,8 +833,8 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
         // Shorter than one block: the tensor map would be empty; the plain kernel is exact.
         return fir_plain_launch(x, taps, y, n, num_taps, stream);
     }
-    if (config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)) {
-        return fir_tcs_launch(0, x, taps, y, n, num_taps, stream);
+    if (config.tile_blocks == kTcWindowTile && fir_tcw_supported(num_taps)) {
+        return fir_tcw_launch(0, x, taps, y, n, num_taps, stream);
     }
     return launch_single(0, x, taps, y, n, num_taps, config.stages, stream);
 }
@@ -857,8 +857,8 @@ cudaError_t fir_tc_launch_format(int format, const void* x, const float* taps, v
     if (n < kB) {
         return fir_plain_launch_format(format, x, taps, y, n, num_taps, stream);
     }
-    if (config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)) {
-        return fir_tcs_launch(format, x, taps, y, n, num_taps, stream);
+    if (config.tile_blocks == kTcWindowTile && fir_tcw_supported(num_taps)) {
+        return fir_tcw_launch(format, x, taps, y, n, num_taps, stream);
     }
     // Otherwise integer input runs in the single-CTA form (also where cf32 runs the pair form).
     return launch_single(format, x, taps, y, n, num_taps,
@@ -873,8 +873,8 @@ long long fir_tc_tile_outputs(int num_taps, long long n, TcConfig config)
     if (config.tile_blocks == kTcPairTile && n >= 2 * kB && fir_tc2_supported(num_taps)) {
         return 96LL * 256;
     }
-    if (n >= kB && config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)) {
-        return fir_tcs_tile_outputs();
+    if (n >= kB && config.tile_blocks == kTcWindowTile && fir_tcw_supported(num_taps)) {
+        return fir_tcw_tile_outputs();
     }
     return n < kB ? 1 : static_cast<long long>(kNB) * kB;
 }
@@ -887,8 +887,8 @@ long long fir_tc_tile_outputs_format(int format, int num_taps, long long n, TcCo
     if (n <= 0 || n < kB || !fir_tc_supported(num_taps)) {
         return 1;
     }
-    return config.tile_blocks == kTcShortTile && fir_tcs_supported(num_taps)
-               ? fir_tcs_tile_outputs()
+    return config.tile_blocks == kTcWindowTile && fir_tcw_supported(num_taps)
+               ? fir_tcw_tile_outputs()
                : static_cast<long long>(kNB) * kB;
 }
 

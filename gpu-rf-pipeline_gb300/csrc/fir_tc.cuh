@@ -11,11 +11,11 @@ namespace rfx {
 struct TcConfig {
     int tile_blocks;  // 128-output blocks per tile: 96 = one CTA per tile (fir_tc.cu),
                       // 192 = a CTA pair per tile of 96 256-output blocks (fir_tc2.cu),
-                      // 48 = the short-filter form, up to 129 taps (fir_tc_short.cu)
+                      // 48 = the resident-window form, 2 to 1025 taps (fir_tc_win.cu)
     int stages;       // operand ring depth cap (the largest that fits is used)
 };
 constexpr int kTcPairTile = 192;
-constexpr int kTcShortTile = 48;
+constexpr int kTcWindowTile = 48;
 
 constexpr int kTcBatchMax = 4096;
 
@@ -27,14 +27,14 @@ cudaError_t fir_tc_launch(const void* x, const float* taps, void* y, long long n
                           TcConfig config, cudaStream_t stream);
 cudaError_t fir_tc_take_fault(unsigned int* code);
 
-// The short-filter form (fir_tc_short.cu): 2 to 129 taps, tiles of 48 blocks whose whole input
+// The resident-window form (fir_tc_win.cu): 2 to 1025 taps, tiles of 48 blocks whose whole input
 // window arrives by one TMA copy; format 0 cf32, 1 ci16, 2 ci8 (decoded in the load stage, the
 // same bits as over the converted samples). n >= 128.
-bool fir_tcs_supported(int num_taps);
-long long fir_tcs_tile_outputs();
-cudaError_t fir_tcs_launch(int format, const void* x, const float* taps, void* y, long long n,
+bool fir_tcw_supported(int num_taps);
+long long fir_tcw_tile_outputs();
+cudaError_t fir_tcw_launch(int format, const void* x, const float* taps, void* y, long long n,
                            int num_taps, cudaStream_t stream);
-cudaError_t fir_tcs_take_fault(unsigned int* code);
+cudaError_t fir_tcw_take_fault(unsigned int* code);
 
 // The same FIR over integer I/Q input decoded in the load stage (format 1 = ci16, 2 = ci8; 0 =
 // cf32, fir_tc_launch): the copies move the stored components, the producers convert them as

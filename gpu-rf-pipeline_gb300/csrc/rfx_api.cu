@@ -206,8 +206,8 @@ int rfx_device_fault(unsigned int* code)
     }
     total |= part;
     part = 0;
-    if ((err = rfx::fir_tcs_take_fault(&part)) != cudaSuccess) {
-        return cuda_fail(err, "fir_tcs fault word");
+    if ((err = rfx::fir_tcw_take_fault(&part)) != cudaSuccess) {
+        return cuda_fail(err, "fir_tcw fault word");
     }
     total |= part;
     part = 0;

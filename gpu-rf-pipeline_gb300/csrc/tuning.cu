@@ -241,9 +241,9 @@ double best_ms(Run run)
 // Built-in rule before tuning: the tensor-core form once the filter is long enough for FP32
 // FMA throughput to bound the plain kernel and the input fills the GPU; the plain kernel
 // otherwise. Measured on GB300 at 2^24 samples: the plain kernel is HBM-bound up to about 24
-// taps (42-49 us) and FMA-bound beyond (79 us at 63 taps, 149 us at 129); the short-filter
-// tensor-core form takes 48-54 us from 2 to 129 taps, the long-filter form ~115 us from 130 to
-// about 500 taps.
+// taps (42-49 us) and FMA-bound beyond (79 us at 63 taps, 149 us at 129); the resident-window
+// tensor-core form takes 48-58 us from 2 to 129 taps, 68 us at 255 and 82 us at 385; the
+// long-filter form 120 us at 511 taps and 141 us at 1025.
 int tuned_fir_impl(int num_taps, long long n)
 {
     FirEntry e;
@@ -264,7 +264,7 @@ int tuned_fir_impl(int num_taps, long long n)
 int tuned_fir_batch_impl(int num_taps, long long n)
 {
     FirEntry e;
-    if (!fir_tcs_supported(num_taps) && lookup_fir(num_taps, n, &e)) {
+    if (!fir_tcw_supported(num_taps) && lookup_fir(num_taps, n, &e)) {
         return e.impl;
     }
     constexpr int kTcMinTaps = 160;
@@ -280,8 +280,8 @@ TcConfig tuned_fir_tc_config(int num_taps, long long n)
     if (lookup_fir(num_taps, n, &e) && e.impl == RFX_FIR_TC) {
         return e.config;
     }
-    // The short-filter form where it applies (one copy of each window, no scan slices).
-    return fir_tcs_supported(num_taps) ? TcConfig{kTcShortTile, 4} : TcConfig{96, 6};
+    // The resident-window form where it applies (one copy of each window, no scan slices).
+    return fir_tcw_supported(num_taps) ? TcConfig{kTcWindowTile, 4} : TcConfig{96, 6};
 }
 
 // Built-in rule: the fused tensor-core form at 64 channels (one HBM pass against the plain
@@ -324,8 +324,8 @@ extern "C" int rfx_autotune_fir(int impl, int num_taps, int64_t num_samples, dou
         for (int st : {2, 4, 6}) {
             candidates.push_back({RFX_FIR_TC, TcConfig{kTcPairTile, st}});
         }
-        if (fir_tcs_supported(num_taps)) {
-            candidates.push_back({RFX_FIR_TC, TcConfig{kTcShortTile, 4}});
+        if (fir_tcw_supported(num_taps)) {
+            candidates.push_back({RFX_FIR_TC, TcConfig{kTcWindowTile, 4}});
         }
     }
     FirEntry best{RFX_FIR_PLAIN, TcConfig{96, 6}, 1e30};

@@ -160,8 +160,8 @@ def test_impl_used_reports_the_kernel_that_runs(lib) -> None:
     assert rfx.fir_impl_used("plain", 1025, 1 << 24) == "plain"
     for name in ["naive", "tiled", "tiled_const", "register"]:
         assert rfx.fir_impl_used(name, 1025, 1 << 24) == "plain"
-    # auto's built-in rule: the tensor core from 32 taps and 2^16 samples (the short-filter form
-    # up to 129 taps); a batch keeps filters under 160 taps on the plain kernel.
+    # auto's built-in rule: the tensor core from 32 taps and 2^16 samples (the resident-window form
+    # up to 385 taps); a batch keeps filters under 160 taps on the plain kernel.
     assert rfx.fir_impl_used("auto", 1025, 1 << 24) == "tc_split"
     assert rfx.fir_impl_used("auto", 63, 1 << 24) == "tc_split"
     assert rfx.fir_impl_used("auto", 32, 1 << 24) == "tc_split"

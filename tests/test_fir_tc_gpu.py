@@ -92,23 +92,24 @@ def test_tc_lengths(n: int) -> None:
     assert orc.normwise_error(y, orc.fir_fast(x, h)) <= TC_NORMWISE
 
 
-SHORT_TILE = 48 * 128  # outputs per tile of the short-filter form (2 to 129 taps)
+SHORT_TILE = 48 * 128  # outputs per tile of the resident-window form (2 to 385 taps)
 
 
-@pytest.mark.parametrize("k", [2, 63, 113, 114, 129])
+@pytest.mark.parametrize("k", [2, 63, 113, 114, 129, 130, 241, 257, 385])
 @pytest.mark.parametrize("n", [128, 129, 255, 49 * 128 + 5, SHORT_TILE - 1, SHORT_TILE,
                                SHORT_TILE + 1, 3 * SHORT_TILE + 77, 152 * SHORT_TILE + 300])
-def test_tc_short_form_lengths(k: int, n: int) -> None:
-    # Tile edges of the short-filter form, its partial last block (outside the tensor map, read
-    # from global memory into the window), windows reaching past the input, and grids with
+def test_tc_window_form_lengths(k: int, n: int) -> None:
+    # Tile edges of the resident-window form, its partial last block (outside the tensor map,
+    # read from global memory into the window), windows reaching past the input, and grids with
     # more tiles than SMs; 113 and 114 taps bracket the first K-step that needs the previous
-    # block's taps.
+    # block's taps; 130 to 385 taps reach back two and three blocks, in H groups of several
+    # K-steps summed into running sums.
     x, h = rand_case(n, k, seed=n + k)
     y = run(x, h)
     assert orc.normwise_error(y, orc.fir_fast(x, h)) <= TC_NORMWISE
 
 
-def test_tc_short_form_per_tile_scale_spans_extreme_levels() -> None:
+def test_tc_window_form_per_tile_scale_spans_extreme_levels() -> None:
     x, h = rand_case(6 * SHORT_TILE, 63, seed=12)
     levels = np.array([1.0, 1e-30, 1e30, 3.0, 1e-12, 1.0])
     x = (x * np.repeat(levels, SHORT_TILE).astype(np.float32)).astype(np.complex64)
@@ -123,10 +124,11 @@ def test_tc_short_form_per_tile_scale_spans_extreme_levels() -> None:
 
 
 @pytest.mark.parametrize("fmt", ["ci16", "ci8"])
-def test_tc_short_form_integer_input_matches_converted(fmt: str) -> None:
-    # Integer recordings decoded in the short form's load stage give the bits of a run over
-    # the host-converted samples.
-    n, k = 3 * SHORT_TILE + 333, 63
+@pytest.mark.parametrize("k", [63, 300])
+def test_tc_window_form_integer_input_matches_converted(fmt: str, k: int) -> None:
+    # Integer recordings decoded in the resident-window form's load stage give the bits of a
+    # run over the host-converted samples.
+    n = 3 * SHORT_TILE + 333
     rng = np.random.default_rng(21)
     info = np.iinfo(np.int16 if fmt == "ci16" else np.int8)
     raw = rng.integers(info.min, info.max + 1, size=2 * n).astype(info.dtype)

@@ -8,8 +8,8 @@ the C ABI; the complete output is compared with the oracle:
   segment (so a wrong stretch far into the capture cannot hide behind the global maximum);
 * fir63 (2^24 samples, 63 taps): plain bit-exact against the float32 restatement of the
   project's FIR kernels (one fma per tap in tap order, tests/test_pipeline.py:116-135 holds
-  them to 1e-5); tc_split and auto (the short-filter tensor-core form) <= 2e-6 normwise over the
-  whole output and every 2^16-output segment;
+  them to 1e-5); tc_split and auto (the resident-window tensor-core form) <= 2e-6 normwise
+  over the whole output and every 2^16-output segment;
 * pfb64 (2^24 samples, 64 channels, 1024 taps): tc_split <= 2e-6 normwise, and per channel
   (against each channel's own level) within 2.5x of the FP32 cuFFT form; plain: branch sums
   bit-exact against the float32 restatement and the channels within the project's channelizer
