@@ -29,6 +29,7 @@
 #include "tc_common.cuh"
 #include "tmap.hpp"
 #include "tuning.hpp"
+#include "fir_tc_win.cuh"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -117,6 +118,14 @@ struct BatchView {
     uint32_t plain_region;   // shared-memory bytes per group
     uint32_t plain_slot;     // bytes per tile slot: region = 2 slots (pipelined) or 1
     int maps_global;         // tensor maps in global memory: fence them before first use
+    // Captures for the resident-window pipeline (fir_tc_win.cuh), by blocks reached back C =
+    // 1, 2, 3: capture list, window tensor maps, per-block item ranges; its control block sits
+    // in the last kilobyte of shared memory (win_ctl), clear of every other phase's barriers.
+    const tcw::WinCapture* wcap[tcw::kCMax];
+    const CUtensorMap* wmap[tcw::kCMax];
+    const int* cta_win[tcw::kCMax];
+    int wcount[tcw::kCMax];
+    uint32_t win_ctl;
 };
 
 // Per-capture window geometry.
@@ -185,7 +194,6 @@ struct Ctrl {
     unsigned long long sready[4];   // the output scale of item k is in shift[k % 4]
     unsigned long long strip_free;  // every MMA of the previous capture has completed
     unsigned long long teardown;
-    uint32_t tmem_base;
     int abort;
     uint32_t pmax[2][kProducerWarps];
     uint32_t tmaxw[2][kProducerWarps];
@@ -197,7 +205,7 @@ struct Ctrl {
     int item_groups[4];
     int shift[4];
 };
-static_assert(sizeof(Ctrl) <= 1024, "control block");
+static_assert(sizeof(Ctrl) <= 1020, "control block (the last word carries the TMEM base)");
 
 // Capture of a work-list item, searched forward from a cursor (items only increase).
 __device__ __forceinline__ int capture_of(const BatchView& p, int item, int cursor)
@@ -263,7 +271,7 @@ __device__ __forceinline__ void tmap_acquire(const CUtensorMap* map)
 // the same for every thread of the block). Every thread returns after a final block barrier.
 template <int S>
 __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_item, int my_items,
-                                               unsigned char* smem)
+                                               unsigned char* smem, uint32_t tmem)
 {
     Ctrl& ctl = *reinterpret_cast<Ctrl*>(smem);
     const int sbufs = p.sbufs;
@@ -314,9 +322,6 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
         ctl.abort = 0;
         fence_mbar_init();
     }
-    if (warp == kMmaWarp) {
-        tmem_alloc(smem_u32(&ctl.tmem_base), kTmemCols);
-    }
     __syncthreads();
     // Raw copy of K-step u into raw slot `slot`: item u / 8, floats 32 (u % 8) .. of its window.
     auto issue_raw = [&](int u, int cursor, uint32_t dst, uint32_t bar) -> int {
@@ -357,7 +362,6 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = ctl.tmem_base;
 
     if (warp < kDrainWarps) {
         // ---- drain warps: running sums, outputs ----------------------------------------------
@@ -821,10 +825,6 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == kMmaWarp) {
-        tmem_dealloc(tmem, kTmemCols);
-    }
-    __syncthreads();
 }
 
 // True on every thread of plain group `id` if `v` is true on all of them (one barrier).
@@ -890,20 +890,64 @@ __device__ __forceinline__ void batch_plain_tiles(const BatchView& p, int t0, in
     }
 }
 
+// One window phase: the block's items of the captures that reach back C blocks.
+template <int C>
+__device__ __forceinline__ void batch_window_items(const BatchView& v, unsigned char* smem,
+                                                   uint32_t tmem)
+{
+    if (v.wcount[C - 1] == 0) {
+        return;
+    }
+    const int w0 = v.cta_win[C - 1][blockIdx.x];
+    const int w1 = v.cta_win[C - 1][blockIdx.x + 1];
+    if (w1 <= w0) {
+        return;   // uniform across the block
+    }
+    const tcw::TcwListSrc src{v.wcap[C - 1], v.wmap[C - 1], v.wcount[C - 1], w0, w1 - w0};
+    tcw::Ctrl& wctl = *reinterpret_cast<tcw::Ctrl*>(smem + v.win_ctl);
+    tcw::tcw_pipeline<C, 0, 4>(src, smem, wctl, tmem, &g_fault_fir_batch);
+    if (threadIdx.x == 0) {
+        tcw::tcw_release<4>(wctl);
+    }
+    __syncthreads();
+}
+
 template <int S>
 __device__ __forceinline__ void batch_body(const BatchView& v, unsigned char* smem)
 {
+    static_assert(kThreads >= tcw::kThreads, "the window pipeline's roles fit the block");
+    // Tensor memory for every phase, taken once (a block relinquishes the right to allocate
+    // with its first allocation); the base travels through the control block's last word.
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 1020);
+    const int warp = threadIdx.x >> 5;
+    if (warp == kMmaWarp) {
+        tmem_alloc(smem_u32(tmem_slot), kTmemCols);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    __syncthreads();   // read before any phase writes shared memory
     const int first_item = v.cta_item[blockIdx.x];
     const int my_items = v.cta_item[blockIdx.x + 1] - first_item;
     if (my_items > 0) {
-        batch_tc_items<S>(v, first_item, my_items, smem);
+        batch_tc_items<S>(v, first_item, my_items, smem, tmem);
     }
+    batch_window_items<1>(v, smem, tmem);
+    batch_window_items<2>(v, smem, tmem);
+    batch_window_items<3>(v, smem, tmem);
     if (v.plain_groups > 0) {
         const int t0 = v.cta_plain[blockIdx.x];
         const int t1 = v.cta_plain[blockIdx.x + 1];
         if (t1 > t0) {
             batch_plain_tiles(v, t0, t1, smem);
         }
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == kMmaWarp) {
+        tmem_dealloc(tmem, kTmemCols);
     }
 }
 
@@ -914,7 +958,8 @@ fir_batch_kernel(const __grid_constant__ BatchParams p)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const BatchView v{p.cap,   p.xmap,  p.smap, p.cta_item, nullptr, nullptr, p.count,
-                      0,       p.cmax,  p.sbufs, 0,         0u,      0u,      0};
+                      0,       p.cmax,  p.sbufs, 0,         0u,      0u,      0,
+                      {},      {},      {},      {},        0u};
     batch_body<S>(v, smem);
 }
 
@@ -1089,6 +1134,11 @@ namespace {
 // 3.90, 6.54, 12.6 and 24.7 SM-us at 31, 63, 127, 255, 511 and 1025 taps.
 double tc_tile_us(int C) { return 17.6 + 0.4 * static_cast<double>(C + 1); }
 double plain_tile_us(int num_taps) { return 1.0 + 0.0233 * static_cast<double>(num_taps); }
+// A resident-window tile of 48 blocks (measured in batch plans of the 256-capture workload's
+// captures of one tap count: 3.2-3.8 SM-us at 31-127 taps, 4.6 at 255; single captures of 2^24
+// samples: 2.98, 3.82 and 4.69 for C = 1, 2, 3), and the tap strip built per capture.
+double win_tile_us(int C) { return C == 1 ? 3.3 : C == 2 ? 4.6 : 5.6; }
+constexpr double kWinStripUs = 1.0;
 
 constexpr int kPlainGroupsMax = kThreads / kPlainThreads;   // 3
 constexpr uint32_t kSmemMax = 227u * 1024u;
@@ -1140,6 +1190,10 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
     std::vector<BatchCap> tc;
     std::vector<CUtensorMap> xmaps, smaps;
     std::vector<PlainCapDev> pl;
+    // Resident-window captures by blocks reached back (C = 1, 2, 3), their maps and costs.
+    std::vector<tcw::WinCapture> wc[tcw::kCMax];
+    std::vector<CUtensorMap> wm[tcw::kCMax];
+    std::vector<double> wcost[tcw::kCMax];
     std::vector<double> cost;       // per work unit: tensor-core items, then plain tiles
     int kmax_plain = 0;
     int cmax = 0;
@@ -1153,9 +1207,31 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
         }
         const int want =
             impl == RFX_FIR_AUTO ? tuned_fir_batch_impl(c.num_taps, c.num_samples) : impl;
-        const bool use_tc = want == RFX_FIR_TC && c.num_samples >= kB &&
+        const bool use_win = want == RFX_FIR_TC && c.num_samples >= kB &&
+                             fir_tcw_supported(c.num_taps);
+        const bool use_tc = !use_win && want == RFX_FIR_TC && c.num_samples >= kB &&
                             fir_batch_supported(c.num_taps);
-        if (use_tc) {
+        if (use_win) {
+            const int C = (c.num_taps + kB - 2) / kB;
+            std::vector<tcw::WinCapture>& list = wc[C - 1];
+            const int item0 = list.empty() ? 0 : list.back().item0 +
+                                                     static_cast<int>(((list.back().n + kB - 1) / kB +
+                                                                       tcw::kNB - 1) / tcw::kNB);
+            list.push_back(tcw::WinCapture{c.x, static_cast<float2*>(c.y), c.taps, c.num_samples,
+                                           c.num_taps, item0});
+            CUtensorMap m;
+            err = encode_rows(&m, c.x, 4, c.num_samples / kB, 2 * kB, 2 * kB,
+                              static_cast<uint32_t>(tcw::kNB + C));
+            if (err != cudaSuccess) {
+                return err;
+            }
+            wm[C - 1].push_back(m);
+            const int tiles = static_cast<int>(((c.num_samples + kB - 1) / kB + tcw::kNB - 1) /
+                                               tcw::kNB);
+            for (int t = 0; t < tiles; ++t) {
+                wcost[C - 1].push_back(win_tile_us(C) + (t == 0 ? kWinStripUs : 0.0));
+            }
+        } else if (use_tc) {
             BatchCap b{};
             b.x = static_cast<const float2*>(c.x);
             b.y = static_cast<float2*>(c.y);
@@ -1202,10 +1278,21 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
             pl.push_back(q);
         }
     }
+    // The unit line: tensor-core items, window items (C = 1, 2, 3), plain tiles.
+    int wbase[tcw::kCMax];
+    int wunits[tcw::kCMax];
+    int nwin = 0;
+    for (int ci = 0; ci < tcw::kCMax; ++ci) {
+        wbase[ci] = static_cast<int>(cost.size());
+        wunits[ci] = static_cast<int>(wcost[ci].size());
+        cost.insert(cost.end(), wcost[ci].begin(), wcost[ci].end());
+        nwin += static_cast<int>(wc[ci].size());
+    }
+    const int pbase = static_cast<int>(cost.size());
     cost.insert(cost.end(), plain_cost.begin(), plain_cost.end());
     const int units = static_cast<int>(cost.size());
     auto* plan = new BatchPlan{};
-    plan->tc_caps = static_cast<int>(tc.size());
+    plan->tc_caps = static_cast<int>(tc.size()) + nwin;
     plan->plain_caps = static_cast<int>(pl.size());
     if (units == 0) {
         *out = plan;   // nothing to run
@@ -1253,6 +1340,17 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
     }
     plan->stages = stages == 0 ? 2 : stages;
     plan->smem = std::max({tc.empty() ? 0u : lay.bytes, 1024u + groups * region, 120u * 1024u});
+    // The window pipeline's layout (4 stages, two strip slots) and its control block in the
+    // last kilobyte.
+    for (int ci = 0; ci < tcw::kCMax; ++ci) {
+        if (!wc[ci].empty()) {
+            plan->smem = std::max(plan->smem, tcw::win_layout(ci + 1, 4, 2, 4).bytes + 1024u);
+        }
+    }
+    if (plan->smem > kSmemMax) {
+        delete plan;
+        return cudaErrorInvalidValue;
+    }
 
     // Partition: the units on one line (tensor-core items, then plain tiles), cut into grid
     // contiguous pieces of about equal cost; blocks of the first pieces run tensor-core items
@@ -1263,6 +1361,10 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
         prefix[u + 1] = prefix[u] + cost[u];
     }
     std::vector<int> cta_item(grid + 1), cta_plain(grid + 1);
+    std::vector<int> cta_win[tcw::kCMax];
+    for (auto& cw : cta_win) {
+        cw.assign(grid + 1, 0);
+    }
     for (int b = 0; b <= grid; ++b) {
         int u = b == grid ? units
                           : static_cast<int>(std::lower_bound(prefix.begin(), prefix.end(),
@@ -1270,10 +1372,16 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
                                              prefix.begin());
         u = std::min(u, units);
         cta_item[b] = std::min(u, items);
-        cta_plain[b] = std::max(u - items, 0);
+        for (int ci = 0; ci < tcw::kCMax; ++ci) {
+            cta_win[ci][b] = std::min(std::max(u - wbase[ci], 0), wunits[ci]);
+        }
+        cta_plain[b] = std::max(u - pbase, 0);
     }
     for (int b = 1; b <= grid; ++b) {   // monotone after rounding
         cta_item[b] = std::max(cta_item[b], cta_item[b - 1]);
+        for (int ci = 0; ci < tcw::kCMax; ++ci) {
+            cta_win[ci][b] = std::max(cta_win[ci][b], cta_win[ci][b - 1]);
+        }
         cta_plain[b] = std::max(cta_plain[b], cta_plain[b - 1]);
     }
 
@@ -1286,7 +1394,15 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
     const uint32_t off_item = align_up(off_smap + n_tc * sizeof(CUtensorMap), 16);
     const uint32_t off_plain = align_up(off_item + (grid + 1) * sizeof(int), 16);
     const uint32_t off_pcap = align_up(off_plain + (grid + 1) * sizeof(int), 16);
-    const uint32_t bytes = align_up(off_pcap + pl.size() * sizeof(PlainCapDev), 128);
+    uint32_t off_w = align_up(off_pcap + pl.size() * sizeof(PlainCapDev), 128);
+    uint32_t off_wmap[tcw::kCMax], off_wcap[tcw::kCMax], off_wcta[tcw::kCMax];
+    for (int ci = 0; ci < tcw::kCMax; ++ci) {
+        off_wmap[ci] = off_w;
+        off_wcap[ci] = align_up(off_wmap[ci] + wm[ci].size() * sizeof(CUtensorMap), 16);
+        off_wcta[ci] = align_up(off_wcap[ci] + wc[ci].size() * sizeof(tcw::WinCapture), 16);
+        off_w = align_up(off_wcta[ci] + (grid + 1) * sizeof(int), 128);
+    }
+    const uint32_t bytes = off_w;
     std::vector<unsigned char> host(bytes, 0);
     std::memcpy(host.data() + off_cap, tc.data(), n_tc * sizeof(BatchCap));
     std::memcpy(host.data() + off_xmap, xmaps.data(), n_tc * sizeof(CUtensorMap));
@@ -1294,6 +1410,12 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
     std::memcpy(host.data() + off_item, cta_item.data(), (grid + 1) * sizeof(int));
     std::memcpy(host.data() + off_plain, cta_plain.data(), (grid + 1) * sizeof(int));
     std::memcpy(host.data() + off_pcap, pl.data(), pl.size() * sizeof(PlainCapDev));
+    for (int ci = 0; ci < tcw::kCMax; ++ci) {
+        std::memcpy(host.data() + off_wmap[ci], wm[ci].data(), wm[ci].size() * sizeof(CUtensorMap));
+        std::memcpy(host.data() + off_wcap[ci], wc[ci].data(),
+                    wc[ci].size() * sizeof(tcw::WinCapture));
+        std::memcpy(host.data() + off_wcta[ci], cta_win[ci].data(), (grid + 1) * sizeof(int));
+    }
     unsigned char* dev = nullptr;
     if ((err = cudaMalloc(&dev, bytes)) != cudaSuccess ||
         (err = cudaMemcpy(dev, host.data(), bytes, cudaMemcpyHostToDevice)) != cudaSuccess) {
@@ -1318,6 +1440,13 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
     v.plain_region = region;
     v.plain_slot = slot;
     v.maps_global = 1;
+    for (int ci = 0; ci < tcw::kCMax; ++ci) {
+        v.wcap[ci] = reinterpret_cast<const tcw::WinCapture*>(dev + off_wcap[ci]);
+        v.wmap[ci] = reinterpret_cast<const CUtensorMap*>(dev + off_wmap[ci]);
+        v.cta_win[ci] = reinterpret_cast<const int*>(dev + off_wcta[ci]);
+        v.wcount[ci] = static_cast<int>(wc[ci].size());
+    }
+    v.win_ctl = plan->smem - 1024u;
     const void* fn = plan->stages == 6   ? reinterpret_cast<const void*>(fir_batch_list_kernel<6>)
                      : plan->stages == 4 ? reinterpret_cast<const void*>(fir_batch_list_kernel<4>)
                                          : reinterpret_cast<const void*>(fir_batch_list_kernel<2>);

@@ -926,7 +926,7 @@ cudaError_t fir_batch_launch(int impl, const rfx_fir_capture* captures, int coun
             if (cap.num_samples == 0) {
                 continue;
             }
-            if (tuned_fir_batch_impl(cap.num_taps, cap.num_samples) == RFX_FIR_TC) {
+            if (tuned_fir_batch_launch_impl(cap.num_taps, cap.num_samples) == RFX_FIR_TC) {
                 tc.push_back(cap);
                 continue;
             }

@@ -257,11 +257,11 @@ int tuned_fir_impl(int num_taps, long long n)
                : RFX_FIR_PLAIN;
 }
 
-// Where the batch kernels place a capture. Their tensor-core kernel is the long-filter form
-// (fir_batch.cu), whose tiles cost about the same whatever the filter, so short filters stay
-// on the plain tiles: the tensor core from 160 taps (plain and the long-filter form meet near
-// 130), or where a tuned entry for a filter beyond the short form's range says so.
-int tuned_fir_batch_impl(int num_taps, long long n)
+// Where rfx_fir_batch_launch places a capture. Its tensor-core kernel is the long-filter form
+// (fir_batch.cu), whose tiles cost about the same whatever the filter, so short filters stay on
+// the plain tiles: the tensor core from 160 taps (plain and the long-filter form meet near 130),
+// or where a tuned entry for a filter beyond the resident-window form's range says so.
+int tuned_fir_batch_launch_impl(int num_taps, long long n)
 {
     FirEntry e;
     if (!fir_tcw_supported(num_taps) && lookup_fir(num_taps, n, &e)) {
@@ -270,6 +270,22 @@ int tuned_fir_batch_impl(int num_taps, long long n)
     constexpr int kTcMinTaps = 160;
     constexpr long long kTcMinSamples = 1LL << 16;
     return num_taps >= kTcMinTaps && n >= kTcMinSamples && fir_tc_supported(num_taps)
+               ? RFX_FIR_TC
+               : RFX_FIR_PLAIN;
+}
+
+// Where a batch plan places a capture: a tensor-core phase for every filter of two taps or more
+// that one takes (its window phase up to 385 taps, its long-filter phase beyond), at any length:
+// a plan launches once for the whole batch, so a short capture is no reason for the plain tiles.
+// Measured on the 256-capture workload (batch plans of each tap count alone): a window tile of
+// 6144 outputs costs 3.2-3.8 SM-us at 31-127 taps, 4.6 at 255, a long-filter tile of 12288
+// outputs ~20-25 SM-us at 511-1025, against 2304-output plain tiles of 1.7 SM-us at 31 taps and
+// 12.6-24.7 at 511-1025; the whole batch took 1.27 ms this way against 1.32 ms with the short
+// captures of long filters on the plain tiles.
+int tuned_fir_batch_impl(int num_taps, long long n)
+{
+    (void)n;
+    return num_taps >= 2 && (fir_tcw_supported(num_taps) || fir_batch_supported(num_taps))
                ? RFX_FIR_TC
                : RFX_FIR_PLAIN;
 }

@@ -9,6 +9,7 @@ namespace rfx {
 
 int tuned_fir_impl(int num_taps, long long n);
 int tuned_fir_batch_impl(int num_taps, long long n);
+int tuned_fir_batch_launch_impl(int num_taps, long long n);
 TcConfig tuned_fir_tc_config(int num_taps, long long n);
 int tuned_chan_impl(int channels, long long n);
 

@@ -161,15 +161,20 @@ def test_impl_used_reports_the_kernel_that_runs(lib) -> None:
     for name in ["naive", "tiled", "tiled_const", "register"]:
         assert rfx.fir_impl_used(name, 1025, 1 << 24) == "plain"
     # auto's built-in rule: the tensor core from 32 taps and 2^16 samples (the resident-window form
-    # up to 385 taps); a batch keeps filters under 160 taps on the plain kernel.
+    # up to 385 taps); a batch plan puts every filter of two taps or more on a tensor-core phase
+    # at any length (its window phase up to 385 taps).
     assert rfx.fir_impl_used("auto", 1025, 1 << 24) == "tc_split"
     assert rfx.fir_impl_used("auto", 63, 1 << 24) == "tc_split"
     assert rfx.fir_impl_used("auto", 32, 1 << 24) == "tc_split"
     assert rfx.fir_impl_used("auto", 31, 1 << 24) == "plain"
     assert rfx.fir_impl_used("auto", 1025, 1 << 12) == "plain"
-    assert rfx.fir_impl_used("auto", 63, 1 << 24, batch=True) == "plain"
-    assert rfx.fir_impl_used("auto", 159, 1 << 24, batch=True) == "plain"
-    assert rfx.fir_impl_used("auto", 160, 1 << 24, batch=True) == "tc_split"
+    assert rfx.fir_impl_used("auto", 63, 1 << 24, batch=True) == "tc_split"
+    assert rfx.fir_impl_used("auto", 63, 4096, batch=True) == "tc_split"
+    assert rfx.fir_impl_used("auto", 31, 1 << 24, batch=True) == "tc_split"
+    assert rfx.fir_impl_used("auto", 1, 1 << 24, batch=True) == "plain"
+    assert rfx.fir_impl_used("auto", 386, 1 << 24, batch=True) == "tc_split"
+    assert rfx.fir_impl_used("auto", 386, 1 << 12, batch=True) == "tc_split"
+    assert rfx.fir_impl_used("auto", 1025, 127, batch=True) == "plain"   # under one block
     with pytest.raises(rfx.RfxError):
         rfx.fir_impl_used("tc_split", 0, 100)
     with pytest.raises(rfx.RfxError):
