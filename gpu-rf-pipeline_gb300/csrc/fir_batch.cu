@@ -23,6 +23,14 @@
 //    after the MMA thread has committed the last MMA of the previous capture (`strip_free`),
 //    before the first stage of the new capture is marked full;
 //  * the drain's scale is per tile: 2^-(ex + eh), eh the tile's capture's tap scale.
+//
+// A batch plan (work list in device memory) runs, in the same launch and after those items, the
+// resident-window pipeline of fir_tc_win.cuh over its captures of 2 to 385 taps: one phase per
+// reach-back C = 1, 2, 3 (the window geometry is compile-time), each block taking a contiguous
+// range of that phase's 48-block tiles; the scan warps rebuild the tap strip at every capture
+// switch into one of two slots, the MMA warp freeing a slot after its capture's last tile. Last
+// come the plain tiles of the captures below 2 taps (the plain kernel's tile function:
+// bit-exact). Tensor memory is allocated once per block for every phase.
 #include "fir_tc.cuh"
 #include "fir_plain.cuh"
 #include "fir_plain_tile.cuh"

@@ -166,9 +166,11 @@ int rfx_fir_batch_launch(int impl, const rfx_fir_capture* captures, int count,
  * every run of the batch is ONE persistent kernel launch, replayable from a CUDA graph. The
  * launch takes every capture of the batch: those the implementation puts on the tensor cores
  * (RFX_FIR_TC: all it can take; RFX_FIR_AUTO: as the tuned table or the built-in rule places
- * each capture) run the block-Toeplitz pipeline, the others (short filters under auto, one tap,
- * shorter than 128 samples, beyond the kernel's tap budget, or everything under RFX_FIR_PLAIN)
- * run the plain kernel's tile function with groups of the same blocks' threads, with its bits.
+ * each capture: every filter of 2 taps or more by the built-in rule) run the block-Toeplitz
+ * pipelines (the resident-window phases for 2 to 385 taps, the long-filter tiles beyond), the
+ * others (one tap, shorter than 128 samples, beyond the kernel's tap budget, or everything
+ * under RFX_FIR_PLAIN) run the plain kernel's tile function with groups of the same blocks'
+ * threads, with its bits.
  * The blocks are given contiguous shares of tensor-core tiles and plain tiles of about equal
  * cost, so tensor-bound and memory-bound work run side by side on different SMs.
  * Create allocates and copies (setup; call outside timed regions and stream capture); the
