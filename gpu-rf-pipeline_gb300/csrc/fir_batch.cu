@@ -215,13 +215,53 @@ struct Ctrl {
 };
 static_assert(sizeof(Ctrl) <= 1020, "control block (the last word carries the TMEM base)");
 
-// Capture of a work-list item, searched forward from a cursor (items only increase).
-__device__ __forceinline__ int capture_of(const BatchView& p, int item, int cursor)
+// The capture holding work-list item `item` (binary search over the captures' first items).
+__device__ __forceinline__ int capture_find(const BatchView& p, int item)
 {
-    while (cursor + 1 < p.count && p.cap[cursor + 1].item0 <= item) {
-        ++cursor;
+    int lo = 0;
+    int hi = p.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (p.cap[mid].item0 <= item) {
+            lo = mid;
+        } else {
+            hi = mid - 1;
+        }
     }
-    return cursor;
+    return lo;
+}
+
+// A role's copy, in registers, of the fields of the capture that holds its current item,
+// reloaded only when the item passes into the next capture (items only increase). Looking the
+// capture up in the table on every K-step kept the producers' critical path waiting on loads:
+// measured 145 against 124 us at 511 taps, 2^24 samples.
+struct CapCursor {
+    int idx;      // capture index
+    int end;      // first item of the next capture
+    int item0;    // first item of this capture
+    int C;
+    long long n;
+};
+
+__device__ __forceinline__ void cursor_load(const BatchView& p, int i, CapCursor& r)
+{
+    const BatchCap& c = p.cap[i];
+    r.idx = i;
+    r.item0 = c.item0;
+    r.C = c.C;
+    r.n = c.n;
+    r.end = i + 1 < p.count ? p.cap[i + 1].item0 : 0x7fffffff;
+}
+
+// Moves the cursor on to the capture of `item`; true if it moved.
+__device__ __forceinline__ bool cursor_seek(const BatchView& p, int item, CapCursor& r)
+{
+    bool moved = false;
+    while (item >= r.end) {
+        cursor_load(p, r.idx + 1, r);
+        moved = true;
+    }
+    return moved;
 }
 
 // H groups of a tile with P chunks (see fir_tc.cu).
@@ -289,21 +329,9 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
     const uint32_t sbase = smem_u32(smem);
     volatile int* abort = &ctl.abort;
     unsigned int* fault = &g_fault_fir_batch;
-    // The last capture whose tensor maps the calling thread has fenced (each thread that
-    // issues copies keeps its own; captures are met in increasing order).
-    int fenced = -1;
-    auto acquire_maps = [&](int cursor) {
-        if (p.maps_global) {
-            for (; fenced < cursor; ++fenced) {
-                tmap_acquire(p.xmap + fenced + 1);
-                tmap_acquire(p.smap + fenced + 1);
-            }
-        }
-    };
     const int my_steps = my_items * kStagesPerTile;
     const int scan_slices = (my_items - 1) * kStagesPerTile;
-    // Tile index of item k within its capture.
-    auto tile_in = [&](const BatchCap& c, int k) { return first_item + k - c.item0; };
+    const int cap_first = capture_find(p, first_item);
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < S; ++i) {
@@ -331,42 +359,6 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
         fence_mbar_init();
     }
     __syncthreads();
-    // Raw copy of K-step u into raw slot `slot`: item u / 8, floats 32 (u % 8) .. of its window.
-    auto issue_raw = [&](int u, int cursor, uint32_t dst, uint32_t bar) -> int {
-        const int k = u / kStagesPerTile;
-        cursor = capture_of(p, first_item + k, cursor);
-        const BatchCap& c = p.cap[cursor];
-        const Geo g = geo_of(c.C, c.n);
-        acquire_maps(cursor);
-        mbar_arrive_expect_tx(bar, g.raw_tx);
-        tma_load_2d(dst, p.xmap + cursor, 32 * (u % kStagesPerTile), tile_in(c, k) * kNB - c.C,
-                    bar);
-        return cursor;
-    };
-    // Scan slice q: item q / 8 + 1's window rows (q % 8) srows .. + srows.
-    auto issue_scan = [&](int q, int cursor) -> int {
-        const int kn = q / kStagesPerTile + 1;
-        cursor = capture_of(p, first_item + kn, cursor);
-        const BatchCap& c = p.cap[cursor];
-        const Geo g = geo_of(c.C, c.n);
-        const uint32_t bar = smem_u32(&ctl.scan_full[q % sbufs]);
-        acquire_maps(cursor);
-        mbar_arrive_expect_tx(bar, g.scan_tx);
-        tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(q % sbufs) * lay.scan,
-                    p.smap + cursor, 0,
-                    tile_in(c, kn) * kNB - c.C + (q % kStagesPerTile) * g.srows, bar);
-        return cursor;
-    };
-    if (threadIdx.x == 0) {
-        int cur = capture_of(p, first_item, 0);
-        for (int u = 0; u < kRaw && u < my_steps; ++u) {
-            cur = issue_raw(u, cur, sbase + lay.raw0 + u * lay.raw, smem_u32(&ctl.raw_full[u]));
-        }
-        cur = capture_of(p, first_item, 0);
-        for (int q = 0; q < sbufs - 2 && q < scan_slices; ++q) {
-            cur = issue_scan(q, cur);
-        }
-    }
     fence_before();
     __syncthreads();
     fence_after();
@@ -457,10 +449,48 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
         int switches = 0;           // tap strips rebuilt after the first (strip_free phases)
         int tmax_uses = 0;
         uint32_t next_max = 0;
-        int cur_prod = capture_of(p, first_item, 0);
-        int cur_scan = cur_prod;
-        int cur_raw = cur_prod;
-        int cur_issue = cur_prod;
+        CapCursor cp;               // capture of the K-step being converted
+        cursor_load(p, cap_first, cp);
+        CapCursor cs = cp;          // capture of the scan slice being read (one item ahead)
+        // Copies, issued by producer thread 0: raw K-step copies kRaw ahead, scan slices
+        // sbufs - 2 ahead, each capture's fields in the thread's own cursors.
+        CapCursor cr = cp;          // capture of the next raw copy
+        CapCursor cq = cp;          // capture of the next scan slice (one item ahead)
+        // The last capture whose tensor maps this thread has fenced (its captures are met in
+        // increasing order from cap_first).
+        int fenced = cap_first - 1;
+        auto acquire_maps = [&](int cursor) {
+            if (p.maps_global) {
+                for (; fenced < cursor; ++fenced) {
+                    tmap_acquire(p.xmap + fenced + 1);
+                    tmap_acquire(p.smap + fenced + 1);
+                }
+            }
+        };
+        // Raw copy of K-step u into raw slot `slot`: item u / 8, floats 32 (u % 8) .. of its
+        // window (rows from block tile * kNB - C).
+        auto issue_raw = [&](int u, int slot) {
+            const int k = u / kStagesPerTile;
+            cursor_seek(p, first_item + k, cr);
+            acquire_maps(cr.idx);
+            const uint32_t bar = smem_u32(&ctl.raw_full[slot]);
+            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(kNB + cr.C) * 128u);
+            tma_load_2d(sbase + lay.raw0 + static_cast<uint32_t>(slot) * lay.raw, p.xmap + cr.idx,
+                        32 * (u % kStagesPerTile), (first_item + k - cr.item0) * kNB - cr.C, bar);
+        };
+        // Scan slice q: item q / 8 + 1's window rows (q % 8) srows .. + srows.
+        auto issue_scan = [&](int q) {
+            const int kn = q / kStagesPerTile + 1;
+            cursor_seek(p, first_item + kn, cq);
+            acquire_maps(cq.idx);
+            const int srows = (kNB + cq.C + kStagesPerTile - 1) / kStagesPerTile;
+            const uint32_t bar = smem_u32(&ctl.scan_full[q % sbufs]);
+            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(srows) * 1024u);
+            tma_load_2d(sbase + lay.scan0 + static_cast<uint32_t>(q % sbufs) * lay.scan,
+                        p.smap + cq.idx, 0,
+                        (first_item + kn - cq.item0) * kNB - cq.C + (q % kStagesPerTile) * srows,
+                        bar);
+        };
 
         // Max of |samples| of capture c in [s, s + 2) clipped to hi_s.
         auto load_pair = [&](const BatchCap& c, long long s, long long hi_s) -> uint32_t {
@@ -515,7 +545,7 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                 ctl.shift[k & 3] = ex + eh;
                 ctl.item_y[k & 3] = c.y;
                 ctl.item_n[k & 3] = c.n;
-                ctl.item_block0[k & 3] = static_cast<long long>(tile_in(c, k)) * kNB;
+                ctl.item_block0[k & 3] = static_cast<long long>(first_item + k - c.item0) * kNB;
                 ctl.item_groups[k & 3] = h_groups(c.C + 1, S).per_tile;
                 mbar_arrive(smem_u32(&ctl.sready[k & 3]));
             }
@@ -551,10 +581,9 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                 return false;
             }
             const int k = q / kStagesPerTile + 1;
-            cur_scan = capture_of(p, first_item + k, cur_scan);
-            const BatchCap& c = p.cap[cur_scan];
-            const Geo g = geo_of(c.C, c.n);
-            const long long j0 = static_cast<long long>(tile_in(c, k)) * kNB;
+            cursor_seek(p, first_item + k, cs);
+            const Geo g = geo_of(cs.C, cs.n);
+            const long long j0 = static_cast<long long>(first_item + k - cs.item0) * kNB;
             const int r0 = (q % kStagesPerTile) * g.srows;
             const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
             const int quads = min(g.srows, g.rows - r0) * 64;   // sample pairs in the window
@@ -564,9 +593,9 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                 m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
             }
             // The capture's partial last block lies outside its tensor map.
-            const long long tail_row = g.full_blocks - (j0 - c.C) - r0;
+            const long long tail_row = g.full_blocks - (j0 - cs.C) - r0;
             if (tail_row >= 0 && tail_row * 64 < quads && ptid < 64) {
-                m = max(m, load_pair(c, g.full_blocks * kB + 2 * ptid, c.n));
+                m = max(m, load_pair(p.cap[cs.idx], g.full_blocks * kB + 2 * ptid, cs.n));
             }
             next_max = m;
             __syncwarp();
@@ -574,7 +603,7 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                 mbar_arrive(smem_u32(&ctl.scan_empty[qb]));
             }
             if (q % kStagesPerTile == kStagesPerTile - 1) {
-                reduce_scale(k, next_max, cur_scan);
+                reduce_scale(k, next_max, cs.idx);
                 next_max = 0;
             }
             return true;
@@ -588,20 +617,17 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
             }
             const int k = v / kStagesPerTile;
             const int st = v % kStagesPerTile;
-            const int prev = cur_prod;
-            cur_prod = capture_of(p, first_item + k, cur_prod);
-            const BatchCap& c = p.cap[cur_prod];
-            if (st == 0 && k > 0 && cur_prod != prev) {
+            if (cursor_seek(p, first_item + k, cp)) {   // a new capture's first K-step
                 // Every MMA that reads the old strip has completed before it is overwritten.
                 if (!mbar_wait_bounded(smem_u32(&ctl.strip_free), switches & 1, fault,
                                        kFaultStageEmpty, abort)) {
                     return false;
                 }
                 ++switches;
-                build_strip(cur_prod);
+                build_strip(cp.idx);
             }
-            const Geo g = geo_of(c.C, c.n);
-            const long long j0 = static_cast<long long>(tile_in(c, k)) * kNB;
+            const Geo g = geo_of(cp.C, cp.n);
+            const long long j0 = static_cast<long long>(first_item + k - cp.item0) * kNB;
             const int ex = (k & 1) ? ex_odd : ex_even;
             const float fs = exp2_exact(ex);   // ex in [-113, 127]: exact scaling
             const f32x2 fs2 = pack2(fs, fs);
@@ -615,7 +641,7 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
             }
             const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
             const uint32_t raw = sbase + lay.raw0 + static_cast<uint32_t>(rslot) * lay.raw;
-            const long long tail_rel = g.full_blocks - (j0 - c.C);
+            const long long tail_rel = g.full_blocks - (j0 - cp.C);
             const int b_tail = tail_rel >= 0 && tail_rel < g.rows ? static_cast<int>(tail_rel) : -1;
             static_assert(kProducers % 8 == 0, "producer stride");
             const int q = ptid & 7;
@@ -629,11 +655,12 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                     v4 = lds128(raw + static_cast<uint32_t>(f) * 16u);  // zero outside [0, n)
                 } else {
                     const long long sidx = g.full_blocks * kB + 16 * st + 2 * q;
+                    const float2* const cx = p.cap[cp.idx].x;
                     v4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (sidx + 1 < c.n) {
-                        v4 = __ldg(reinterpret_cast<const float4*>(c.x + sidx));
-                    } else if (sidx < c.n) {
-                        const float2 w2 = __ldg(c.x + sidx);
+                    if (sidx + 1 < cp.n) {
+                        v4 = __ldg(reinterpret_cast<const float4*>(cx + sidx));
+                    } else if (sidx < cp.n) {
+                        const float2 w2 = __ldg(cx + sidx);
                         v4.x = w2.x;
                         v4.y = w2.y;
                     }
@@ -661,7 +688,7 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                                            fault, kFaultStageEmpty, abort)) {
                         return false;
                     }
-                    cur_raw = issue_raw(v + kRaw, cur_raw, raw, smem_u32(&ctl.raw_full[rslot]));
+                    issue_raw(v + kRaw, rslot);
                 }
                 const int qn = v + sbufs - 2;
                 if (qn < scan_slices) {
@@ -670,16 +697,24 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                                            abort)) {
                         return false;
                     }
-                    cur_issue = issue_scan(qn, cur_issue);
+                    issue_scan(qn);
                 }
             }
             return true;
         };
 
+        if (ptid == 0) {
+            for (int u = 0; u < kRaw && u < my_steps; ++u) {
+                issue_raw(u, u);
+            }
+            for (int q = 0; q < sbufs - 2 && q < scan_slices; ++q) {
+                issue_scan(q);
+            }
+        }
         // Item 0: its capture's tap scale and strip, its scale from its whole window.
         {
-            const BatchCap& c = p.cap[cur_prod];
-            const long long j0 = static_cast<long long>(tile_in(c, 0)) * kNB;
+            const BatchCap& c = p.cap[cp.idx];
+            const long long j0 = static_cast<long long>(first_item - c.item0) * kNB;
             const long long win0 = (j0 - c.C) * kB;
             const long long lo0 = win0 > 0 ? win0 : 0;
             const long long hi0 = (j0 + kNB) * kB < c.n ? (j0 + kNB) * kB : c.n;
@@ -697,8 +732,8 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                     m = max(m, part[i]);
                 }
             }
-            reduce_scale(0, m, cur_prod);
-            build_strip(cur_prod);
+            reduce_scale(0, m, cp.idx);
+            build_strip(cp.idx);
         }
         bool ok = true;
         for (int v = 0; v < my_steps && ok && !*abort; ++v) {
@@ -712,13 +747,14 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
         const uint32_t split_units = lay.split >> 4;
         const uint32_t h_acc = tmem;
         const uint32_t x_acc = tmem + kXCol;
-        int cursor = capture_of(p, first_item, 0);
+        CapCursor cm;
+        cursor_load(p, cap_first, cm);
         int ready = 0;
         int g = 0;
         bool stop = false;
         for (int k = 0; k < my_items && !stop && !*abort; ++k) {
-            cursor = capture_of(p, first_item + k, cursor);
-            const int C = p.cap[cursor].C;
+            cursor_seek(p, first_item + k, cm);
+            const int C = cm.C;
             const int P = C + 1;
             const HGroups grp = h_groups(P, S);
             const uint32_t a_hi0 = ((sbase + lay.taps_hi) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
@@ -816,7 +852,7 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
             }
             mma_commit(smem_u32(&ctl.xfull));
             // The strip of this capture is free once these MMAs complete.
-            if (k + 1 < my_items && capture_of(p, first_item + k + 1, cursor) != cursor) {
+            if (k + 1 < my_items && first_item + k + 1 >= cm.end) {
                 mma_commit(smem_u32(&ctl.strip_free));
             }
         }
@@ -1137,15 +1173,16 @@ cudaError_t fir_batch_tc_launch(const rfx_fir_capture* captures, int count, cuda
 namespace {
 
 // Cost of a work unit in microseconds of one SM, for the partition. Measured on GB300 with this
-// kernel (batch plans of each tap count of the 256-capture workload alone): a tensor-core tile
-// of 96 blocks takes 18.0 to 21.2 SM-us (C = 1 .. 8); a plain tile of 2304 outputs 1.66, 2.27,
-// 3.90, 6.54, 12.6 and 24.7 SM-us at 31, 63, 127, 255, 511 and 1025 taps.
-double tc_tile_us(int C) { return 17.6 + 0.4 * static_cast<double>(C + 1); }
+// kernel (batch plans of each tap count of the 256-capture workload alone, CUDA-graph replay):
+// a long-filter tile of 96 blocks takes 16.4 SM-us at 511 taps (C = 4) and 18.7 at 1025
+// (C = 8); a plain tile of 2304 outputs 1.66, 2.27, 3.90, 6.54, 12.6 and 24.7 SM-us at 31, 63,
+// 127, 255, 511 and 1025 taps.
+double tc_tile_us(int C) { return 13.5 + 0.58 * static_cast<double>(C + 1); }
 double plain_tile_us(int num_taps) { return 1.0 + 0.0233 * static_cast<double>(num_taps); }
-// A resident-window tile of 48 blocks (measured in batch plans of the 256-capture workload's
-// captures of one tap count: 3.2-3.8 SM-us at 31-127 taps, 4.6 at 255; single captures of 2^24
-// samples: 2.98, 3.82 and 4.69 for C = 1, 2, 3), and the tap strip built per capture.
-double win_tile_us(int C) { return C == 1 ? 3.3 : C == 2 ? 4.6 : 5.6; }
+// A resident-window tile of 48 blocks (batch plans as above: 3.3, 3.2 and 3.8 SM-us at 31, 63
+// and 127 taps, 4.4 at 255; C = 3 scaled from single captures of 2^24 samples, 2.98, 3.82 and
+// 4.69 SM-us for C = 1, 2, 3), and the tap strip built per capture.
+double win_tile_us(int C) { return C == 1 ? 3.4 : C == 2 ? 4.4 : 5.4; }
 constexpr double kWinStripUs = 1.0;
 
 constexpr int kPlainGroupsMax = kThreads / kPlainThreads;   // 3

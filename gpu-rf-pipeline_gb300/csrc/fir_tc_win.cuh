@@ -115,6 +115,14 @@ __device__ __forceinline__ void tmap_acquire_global(const CUtensorMap* map)
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
 }
 
+// A role's place in the capture list: the capture index and the items it holds, in registers,
+// so that a lookup reads the list only when an item passes into the next capture.
+struct TcwCursor {
+    int idx = -1;
+    int item0 = 0;
+    int end = 0;   // first item of the next capture
+};
+
 struct TcwSingleSrc {
     static constexpr bool kMulti = false;
     const CUtensorMap* map;   // in the kernel parameters
@@ -126,9 +134,10 @@ struct TcwSingleSrc {
                    ? (tiles - 1 - static_cast<int>(blockIdx.x)) / gridDim.x + 1
                    : 0;
     }
-    __device__ void locate(int k, int& cur, long long& t) const
+    __device__ void locate(int k, TcwCursor& cur, long long& t) const
     {
-        cur = 0;
+        cur.idx = 0;
+        cur.end = 0x7fffffff;
         t = static_cast<long long>(blockIdx.x) + static_cast<long long>(k) * gridDim.x;
     }
     __device__ const WinCapture& capture(int) const { return cap; }
@@ -144,19 +153,45 @@ struct TcwListSrc {
     int first;                // this block's items: first .. first + items - 1
     int items;
     __device__ int count() const { return items; }
-    // Capture and tile of the block's k-th item, searched forward from the cursor.
-    __device__ void locate(int k, int& cur, long long& t) const
+    // Capture and tile of the block's k-th item: the cursor moves forward only when the item
+    // leaves its capture (its first position by binary search: a forward scan from the list's
+    // start cost every role of a late block a chain of dependent loads per phase).
+    __device__ void locate(int k, TcwCursor& cur, long long& t) const
     {
         const int item = first + k;
-        while (cur + 1 < ncaps && caps[cur + 1].item0 <= item) {
-            ++cur;
+        if (item >= cur.end) {
+            int i = cur.idx + 1;
+            if (cur.idx < 0) {
+                int hi = ncaps - 1;
+                i = 0;
+                while (i < hi) {
+                    const int mid = (i + hi + 1) >> 1;
+                    if (caps[mid].item0 <= item) {
+                        i = mid;
+                    } else {
+                        hi = mid - 1;
+                    }
+                }
+            } else {
+                while (i + 1 < ncaps && caps[i + 1].item0 <= item) {
+                    ++i;
+                }
+            }
+            cur.idx = i;
+            cur.item0 = caps[i].item0;
+            cur.end = i + 1 < ncaps ? caps[i + 1].item0 : 0x7fffffff;
         }
-        t = item - caps[cur].item0;
+        t = item - cur.item0;
     }
     __device__ const WinCapture& capture(int c) const { return caps[c]; }
     __device__ const CUtensorMap* tmap(int c) const { return maps + c; }
+    // Fences the maps up to capture c, from the thread's first capture on (the only ones it
+    // copies through).
     __device__ void acquire(int c, int& fenced) const
     {
+        if (fenced < 0) {
+            fenced = c - 1;
+        }
         for (; fenced < c; ++fenced) {
             tmap_acquire_global(maps + fenced + 1);
         }
@@ -224,16 +259,16 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
     const uint32_t sbase = smem_u32(smem);
     volatile int* abort = &ctl.abort;
     const int my_tiles = src.count();
-    int copy_cursor = 0;   // the copy thread's capture cursor and the maps it has fenced
+    TcwCursor copy_cursor;   // the copy thread's capture cursor and the maps it has fenced
     int fenced = -1;
     auto issue_window = [&](int k) {
         long long t;
         src.locate(k, copy_cursor, t);
-        src.acquire(copy_cursor, fenced);
+        src.acquire(copy_cursor.idx, fenced);
         const uint32_t bar = smem_u32(&ctl.win_full[k % wins]);
         mbar_arrive_expect_tx(bar, lay.win);
         tma_load_2d(sbase + lay.win0 + static_cast<uint32_t>(k % wins) * lay.win,
-                    src.tmap(copy_cursor), 0, static_cast<int>(t * kNB - C), bar);
+                    src.tmap(copy_cursor.idx), 0, static_cast<int>(t * kNB - C), bar);
     };
     auto strip_hi = [&](int slot) {
         return sbase + lay.taps0 + static_cast<uint32_t>(slot) * lay.strip;
@@ -317,7 +352,7 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
         bool stop = false;
         int u = 0;     // K-steps issued (block-wide numbering)
         int g = 0;     // H groups issued
-        int cur = 0;   // capture cursor
+        TcwCursor cur;
         int occ = -1;  // captures met so far (strip slot occ & 1)
         int cap_now = -1;
         int st_cmax = 0;
@@ -326,10 +361,10 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
         for (int k = 0; k < my_tiles && !stop && !*abort; ++k) {
             long long t;
             src.locate(k, cur, t);
-            if (cur != cap_now) {
+            if (cur.idx != cap_now) {
                 // A new capture: its strip slot, and the first K-step whose last chunk holds
                 // taps (16 st > C B - K - 15).
-                cap_now = cur;
+                cap_now = cur.idx;
                 ++occ;
                 if constexpr (kMulti) {
                     if (!mbar_wait_bounded(smem_u32(&ctl.strip_ready[occ & 1]), (occ >> 1) & 1,
@@ -337,7 +372,7 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
                         break;
                     }
                 }
-                const int zero_top = C * kB - src.capture(cur).num_taps - 15;
+                const int zero_top = C * kB - src.capture(cur.idx).num_taps - 15;
                 st_cmax = zero_top < 0 ? 0 : zero_top / 16 + 1;
                 a_hi0 = (strip_hi(occ & 1) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
                 a_lo0 = (strip_lo(occ & 1) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
@@ -406,12 +441,12 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
             if constexpr (kMulti) {
                 // The capture's last tile of this block: its strip slot is free once these
                 // MMAs complete.
-                int next = cur;
+                TcwCursor next = cur;
                 long long tn;
                 if (k + 1 < my_tiles) {
                     src.locate(k + 1, next, tn);
                 }
-                if (!stop && (k + 1 == my_tiles || next != cur) && elect_one()) {
+                if (!stop && (k + 1 == my_tiles || next.idx != cur.idx) && elect_one()) {
                     mma_commit(smem_u32(&ctl.strip_free[occ & 1]));
                 }
                 __syncwarp();
@@ -539,11 +574,13 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
         };
         bool ok = true;
         int g = 0;
-        int cur = 0;
+        TcwCursor cur;
         for (int k = 0; k < my_tiles && ok && !*abort; ++k) {
             long long t;
             src.locate(k, cur, t);
-            const WinCapture& cap = src.capture(cur);
+            // The capture's output and length in registers for the tile's stores.
+            float2* const cap_y = src.capture(cur.idx).y;
+            const long long cap_n = src.capture(cur.idx).n;
             const long long jb0 = t * kNB + half * (kNB / 2);
             if constexpr (groups == 1) {
                 // One H group per tile: H and X read side by side, summed and stored per 16
@@ -572,12 +609,12 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const long long o = (jb0 + c16 * 8 + i) * kB + r;
-                        if (o < cap.n) {
+                        if (o < cap_n) {
                             const float re =
                                 __uint_as_float(th[2 * i]) + __uint_as_float(tx[2 * i]);
                             const float im =
                                 __uint_as_float(th[2 * i + 1]) + __uint_as_float(tx[2 * i + 1]);
-                            cap.y[o] = make_float2(re * fa * fb, im * fa * fb);
+                            cap_y[o] = make_float2(re * fa * fb, im * fa * fb);
                         }
                     }
                 }
@@ -630,8 +667,8 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
 #pragma unroll
                 for (int i = 0; i < kNB / 2; ++i) {
                     const long long o = (jb0 + i) * kB + r;
-                    if (o < cap.n) {
-                        cap.y[o] = make_float2(acc[2 * i] * fa * fb, acc[2 * i + 1] * fa * fb);
+                    if (o < cap_n) {
+                        cap_y[o] = make_float2(acc[2 * i] * fa * fb, acc[2 * i + 1] * fa * fb);
                     }
                     acc[2 * i] = 0.0f;
                     acc[2 * i + 1] = 0.0f;
@@ -646,7 +683,7 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
         // never waits behind a drain.
         const int sw = warp - kFirstScanWarp;
         const int stid = static_cast<int>(threadIdx.x) - kFirstScanWarp * 32;
-        int cur = 0;
+        TcwCursor cur;
         int occ = -1;
         int cap_now = -1;
         int patches = 0;   // partial blocks written (phases of `patched`)
@@ -654,9 +691,9 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
         for (int j = 0; j < my_tiles && !*abort; ++j) {
             long long t;
             src.locate(j, cur, t);
-            const WinCapture& cap = src.capture(cur);
-            if (cur != cap_now) {
-                cap_now = cur;
+            const WinCapture& cap = src.capture(cur.idx);
+            if (cur.idx != cap_now) {
+                cap_now = cur.idx;
                 ++occ;
                 if constexpr (kMulti) {
                     // The capture's strip, into slot occ & 1 once the MMAs of the capture that
