@@ -573,6 +573,13 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
             }
             // Made visible to the MMAs by the fence before this K-step's full arrival.
         };
+        // The geometry of the item whose window the scan slices cover, computed at its first
+        // slice.
+        int sc_item = -1;
+        int sc_rows = 0;          // window rows
+        int sc_srows = 0;         // rows per slice
+        long long sc_full = 0;    // full blocks of the capture
+        long long sc_tail = 0;    // window row of the capture's partial block
         // Scan slice q (item q / 8 + 1), copied by TMA sbufs - 1 K-steps earlier.
         auto consume_slice = [&](int q) -> bool {
             const int qb = q % sbufs;
@@ -581,21 +588,26 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
                 return false;
             }
             const int k = q / kStagesPerTile + 1;
-            cursor_seek(p, first_item + k, cs);
-            const Geo g = geo_of(cs.C, cs.n);
-            const long long j0 = static_cast<long long>(first_item + k - cs.item0) * kNB;
-            const int r0 = (q % kStagesPerTile) * g.srows;
+            if (k != sc_item) {
+                sc_item = k;
+                cursor_seek(p, first_item + k, cs);
+                sc_rows = kNB + cs.C;
+                sc_srows = (sc_rows + kStagesPerTile - 1) / kStagesPerTile;
+                sc_full = cs.n / kB;
+                sc_tail = sc_full - (static_cast<long long>(first_item + k - cs.item0) * kNB - cs.C);
+            }
+            const int r0 = (q % kStagesPerTile) * sc_srows;
             const uint32_t buf = sbase + lay.scan0 + static_cast<uint32_t>(qb) * lay.scan;
-            const int quads = min(g.srows, g.rows - r0) * 64;   // sample pairs in the window
+            const int quads = min(sc_srows, sc_rows - r0) * 64;   // sample pairs in the window
             uint32_t m = next_max;
 #pragma unroll 4
             for (int f = ptid; f < quads; f += kProducers) {
                 m = max(m, absmax4(lds128(buf + static_cast<uint32_t>(f) * 16u)));
             }
             // The capture's partial last block lies outside its tensor map.
-            const long long tail_row = g.full_blocks - (j0 - cs.C) - r0;
+            const long long tail_row = sc_tail - r0;
             if (tail_row >= 0 && tail_row * 64 < quads && ptid < 64) {
-                m = max(m, load_pair(p.cap[cs.idx], g.full_blocks * kB + 2 * ptid, cs.n));
+                m = max(m, load_pair(p.cap[cs.idx], sc_full * kB + 2 * ptid, cs.n));
             }
             next_max = m;
             __syncwarp();
@@ -608,26 +620,23 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
             }
             return true;
         };
-        // Producing K-step v: finish scan slice v - 1; at a new capture's first K-step, rebuild
-        // the tap strip; convert the raw samples; queue step v + kRaw's raw copy and scan slice
-        // v + sbufs - 2.
+        // The capture of the K-steps being converted, as loop invariants of a segment (the
+        // block's K-steps of one capture).
+        int seg_C = 0;
+        int seg_rows = 0;
+        long long seg_full = 0;    // full blocks of the capture (rows its tensor maps cover)
+        long long seg_tile0 = 0;   // tile, within the capture, of the block's item 0
+        long long seg_n = 0;
+        const float2* seg_x = nullptr;
+        // Producing K-step v: finish scan slice v - 1, convert the raw samples, queue step
+        // v + kRaw's raw copy and scan slice v + sbufs - 2.
         auto produce = [&](int v) -> bool {
             if (v >= 1 && v - 1 < scan_slices && !consume_slice(v - 1)) {
                 return false;
             }
             const int k = v / kStagesPerTile;
             const int st = v % kStagesPerTile;
-            if (cursor_seek(p, first_item + k, cp)) {   // a new capture's first K-step
-                // Every MMA that reads the old strip has completed before it is overwritten.
-                if (!mbar_wait_bounded(smem_u32(&ctl.strip_free), switches & 1, fault,
-                                       kFaultStageEmpty, abort)) {
-                    return false;
-                }
-                ++switches;
-                build_strip(cp.idx);
-            }
-            const Geo g = geo_of(cp.C, cp.n);
-            const long long j0 = static_cast<long long>(first_item + k - cp.item0) * kNB;
+            const long long j0 = (seg_tile0 + k) * kNB;
             const int ex = (k & 1) ? ex_odd : ex_even;
             const float fs = exp2_exact(ex);   // ex in [-113, 127]: exact scaling
             const f32x2 fs2 = pack2(fs, fs);
@@ -641,26 +650,25 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
             }
             const uint32_t stage = sbase + lay.stages0 + static_cast<uint32_t>(slot) * lay.stage;
             const uint32_t raw = sbase + lay.raw0 + static_cast<uint32_t>(rslot) * lay.raw;
-            const long long tail_rel = g.full_blocks - (j0 - cp.C);
-            const int b_tail = tail_rel >= 0 && tail_rel < g.rows ? static_cast<int>(tail_rel) : -1;
+            const long long tail_rel = seg_full - (j0 - seg_C);
+            const int b_tail = tail_rel >= 0 && tail_rel < seg_rows ? static_cast<int>(tail_rel) : -1;
             static_assert(kProducers % 8 == 0, "producer stride");
             const int q = ptid & 7;
             const uint32_t elem_off = static_cast<uint32_t>(q >> 2) * lay.pitch +
                                       static_cast<uint32_t>(q & 3) * 4u;
 #pragma unroll 2
-            for (int b = ptid >> 3; b < g.rows; b += kProducers / 8) {
+            for (int b = ptid >> 3; b < seg_rows; b += kProducers / 8) {
                 const int f = 8 * b + q;
                 float4 v4;
                 if (b != b_tail) {
                     v4 = lds128(raw + static_cast<uint32_t>(f) * 16u);  // zero outside [0, n)
                 } else {
-                    const long long sidx = g.full_blocks * kB + 16 * st + 2 * q;
-                    const float2* const cx = p.cap[cp.idx].x;
+                    const long long sidx = seg_full * kB + 16 * st + 2 * q;
                     v4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (sidx + 1 < cp.n) {
-                        v4 = __ldg(reinterpret_cast<const float4*>(cx + sidx));
-                    } else if (sidx < cp.n) {
-                        const float2 w2 = __ldg(cx + sidx);
+                    if (sidx + 1 < seg_n) {
+                        v4 = __ldg(reinterpret_cast<const float4*>(seg_x + sidx));
+                    } else if (sidx < seg_n) {
+                        const float2 w2 = __ldg(seg_x + sidx);
                         v4.x = w2.x;
                         v4.y = w2.y;
                     }
@@ -736,8 +744,33 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
             build_strip(cp.idx);
         }
         bool ok = true;
-        for (int v = 0; v < my_steps && ok && !*abort; ++v) {
-            ok = produce(v);
+        int v = 0;
+        while (v < my_steps && ok && !*abort) {
+            if (cursor_seek(p, first_item + v / kStagesPerTile, cp)) {
+                // A new capture: every MMA that reads the old strip has completed before it is
+                // overwritten.
+                if (!mbar_wait_bounded(smem_u32(&ctl.strip_free), switches & 1, fault,
+                                       kFaultStageEmpty, abort)) {
+                    break;
+                }
+                ++switches;
+                // The strip is scaled by the new capture's tap exponent (all producers together;
+                // the scale of the capture's first item, published later, uses the same).
+                if (eh_cap != cp.idx) {
+                    tap_exponent(cp.idx);
+                }
+                build_strip(cp.idx);
+            }
+            seg_C = cp.C;
+            seg_rows = kNB + cp.C;
+            seg_full = cp.n / kB;
+            seg_tile0 = first_item - cp.item0;
+            seg_n = cp.n;
+            seg_x = p.cap[cp.idx].x;
+            const int end_item = min(my_items, cp.end - first_item);
+            for (; v < end_item * kStagesPerTile && ok && !*abort; ++v) {
+                ok = produce(v);
+            }
         }
     } else if (warp == kMmaWarp && lane == 0) {
         // ---- MMA issuer (one thread), as in fir_tc.cu, per item's capture -------------------
@@ -752,14 +785,24 @@ __device__ __forceinline__ void batch_tc_items(const BatchView& p, int first_ite
         int ready = 0;
         int g = 0;
         bool stop = false;
+        // The capture's chunk count, H groups and descriptor bases, recomputed at a switch.
+        int grp_cap = -1;
+        int P = 0;
+        HGroups grp{};
+        uint32_t a_hi0 = 0;
+        uint32_t a_lo0 = 0;
+        uint32_t b_base = 0;
         for (int k = 0; k < my_items && !stop && !*abort; ++k) {
             cursor_seek(p, first_item + k, cm);
-            const int C = cm.C;
-            const int P = C + 1;
-            const HGroups grp = h_groups(P, S);
-            const uint32_t a_hi0 = ((sbase + lay.taps_hi) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
-            const uint32_t a_lo0 = ((sbase + lay.taps_lo) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
-            const uint32_t b_base = ((sbase + lay.stages0) >> 4) + static_cast<uint32_t>(2 * C);
+            if (cm.idx != grp_cap) {
+                grp_cap = cm.idx;
+                const int C = cm.C;
+                P = C + 1;
+                grp = h_groups(P, S);
+                a_hi0 = ((sbase + lay.taps_hi) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+                a_lo0 = ((sbase + lay.taps_lo) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+                b_base = ((sbase + lay.stages0) >> 4) + static_cast<uint32_t>(2 * C);
+            }
             for (int gi = 0; gi < grp.per_tile && !stop; ++gi, ++g) {
                 int st0, st1, c0, c1;
                 h_group_range(grp, P, gi, st0, st1, c0, c1);
@@ -934,6 +977,14 @@ __device__ __forceinline__ void batch_plain_tiles(const BatchView& p, int t0, in
     }
 }
 
+// The window phase that reaches back C blocks runs with eight operand stages (converted four
+// K-steps at a time, as the single-capture kernel: four stages convert two at a time, measured
+// 3.2 - 3.8 SM-us per tile at C = 1 against 3.0), beside three windows and, where they fit, two
+// tap-strip slots (the next capture's strip built while the last one's MMAs run); at C = 2, 3
+// one slot, rebuilt once the capture's MMAs are done.
+__host__ __device__ constexpr int win_stages(int) { return 8; }
+__host__ __device__ constexpr int win_strips(int C) { return C == 1 ? 2 : 1; }
+
 // One window phase: the block's items of the captures that reach back C blocks.
 template <int C>
 __device__ __forceinline__ void batch_window_items(const BatchView& v, unsigned char* smem,
@@ -949,9 +1000,10 @@ __device__ __forceinline__ void batch_window_items(const BatchView& v, unsigned 
     }
     const tcw::TcwListSrc src{v.wcap[C - 1], v.wmap[C - 1], v.wcount[C - 1], w0, w1 - w0};
     tcw::Ctrl& wctl = *reinterpret_cast<tcw::Ctrl*>(smem + v.win_ctl);
-    tcw::tcw_pipeline<C, 0, 4>(src, smem, wctl, tmem, &g_fault_fir_batch);
+    tcw::tcw_pipeline<C, 0, win_stages(C), tcw::TcwListSrc, win_strips(C)>(src, smem, wctl, tmem,
+                                                                        &g_fault_fir_batch);
     if (threadIdx.x == 0) {
-        tcw::tcw_release<4>(wctl);
+        tcw::tcw_release<win_stages(C)>(wctl);
     }
     __syncthreads();
 }
@@ -1179,10 +1231,10 @@ namespace {
 // 127, 255, 511 and 1025 taps.
 double tc_tile_us(int C) { return 13.5 + 0.58 * static_cast<double>(C + 1); }
 double plain_tile_us(int num_taps) { return 1.0 + 0.0233 * static_cast<double>(num_taps); }
-// A resident-window tile of 48 blocks (batch plans as above: 3.3, 3.2 and 3.8 SM-us at 31, 63
-// and 127 taps, 4.4 at 255; C = 3 scaled from single captures of 2^24 samples, 2.98, 3.82 and
+// A resident-window tile of 48 blocks (batch plans as above: 3.0, 2.9 and 3.6 SM-us at 31, 63
+// and 127 taps, 4.2 at 255; C = 3 scaled from single captures of 2^24 samples, 2.98, 3.82 and
 // 4.69 SM-us for C = 1, 2, 3), and the tap strip built per capture.
-double win_tile_us(int C) { return C == 1 ? 3.4 : C == 2 ? 4.4 : 5.4; }
+double win_tile_us(int C) { return C == 1 ? 3.1 : C == 2 ? 4.2 : 5.2; }
 constexpr double kWinStripUs = 1.0;
 
 constexpr int kPlainGroupsMax = kThreads / kPlainThreads;   // 3
@@ -1385,11 +1437,13 @@ cudaError_t fir_batch_plan_make(int impl, const rfx_fir_capture* captures, int c
     }
     plan->stages = stages == 0 ? 2 : stages;
     plan->smem = std::max({tc.empty() ? 0u : lay.bytes, 1024u + groups * region, 120u * 1024u});
-    // The window pipeline's layout (4 stages, two strip slots) and its control block in the
-    // last kilobyte.
+    // The window pipeline's layout (win_stages stages, win_strips strip slots) and its control
+    // block in the last kilobyte.
     for (int ci = 0; ci < tcw::kCMax; ++ci) {
         if (!wc[ci].empty()) {
-            plan->smem = std::max(plan->smem, tcw::win_layout(ci + 1, 4, 2, 4).bytes + 1024u);
+            const int C = ci + 1;
+            plan->smem = std::max(
+                plan->smem, tcw::win_layout(C, win_stages(C), win_strips(C), 4).bytes + 1024u);
         }
     }
     if (plan->smem > kSmemMax) {

@@ -5,9 +5,11 @@
 //  * TcwSingleSrc: one capture, tile k of a block = blockIdx.x + k gridDim.x;
 //  * TcwListSrc: a contiguous range of (capture, tile) work items, captures in increasing order,
 //    each with its own taps, length and tensor map (in global memory). The tap strip is then
-//    rebuilt per capture into one of two strip slots by the scan warps (after the MMA thread's
-//    `strip_free` commit for the capture that used the slot two captures earlier) and published
-//    with `strip_ready`; the drain's tap scale travels with each tile's sample scale.
+//    rebuilt per capture by the scan warps, into one of two strip slots or into the only one
+//    (kStrips), after the MMA warp's `strip_free` commit for the capture that used the slot
+//    last, and published with `strip_ready`; the scan warps publish the capture's first tile
+//    scale before they wait for the slot, and the drain's tap scale travels with each tile's
+//    sample scale.
 #pragma once
 
 #include "sample_fmt.cuh"
@@ -230,7 +232,7 @@ __device__ __forceinline__ void build_strip(uint32_t hi, uint32_t lo, const floa
 // warps beyond the roles return at the final barrier) and returns after a block barrier.
 // With a list of captures (kMulti) the caller invalidates the control block's barriers before
 // the memory is used for anything else (tcw_release).
-template <int C, int kFmt, int S, class Src>
+template <int C, int kFmt, int S, class Src, int kStrips = 2>
 __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem, Ctrl& ctl,
                                              uint32_t tmem, unsigned int* fault)
 {
@@ -251,7 +253,7 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
     static_assert(hks >= 1, "an H group holds at least one K-step");
     static_assert(S == 4 || S == 8, "4 or 8 operand stages");
     static_assert(kSteps % kGroup == 0, "producer groups");
-    const Layout lay = win_layout(C, stages, kMulti ? 2 : 1, es);
+    const Layout lay = win_layout(C, stages, kMulti ? kStrips : 1, es);
     // The warp index through a shuffle: provably the same on every lane of a warp, so values
     // derived from it in a role's loop can stay in uniform registers.
     const int warp = __shfl_sync(0xFFFFFFFFu, static_cast<int>(threadIdx.x >> 5), 0);
@@ -274,6 +276,11 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
         return sbase + lay.taps0 + static_cast<uint32_t>(slot) * lay.strip;
     };
     auto strip_lo = [&](int slot) { return strip_hi(slot) + lay.strip / 2u; };
+    // With a list of captures, capture number occ (of those this block meets) builds its strip
+    // in slot strip_slot(occ), after strip_use(occ) earlier captures used that slot.
+    static_assert(kStrips == 1 || kStrips == 2, "one or two tap-strip slots");
+    auto strip_slot = [](int occ) { return kStrips == 2 ? (occ & 1) : 0; };
+    auto strip_use = [](int occ) { return kStrips == 2 ? (occ >> 1) : occ; };
 
     // ---- setup: barriers, the first windows, the tap strip of a single capture -------------
     if (threadIdx.x == 0) {
@@ -353,7 +360,7 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
         int u = 0;     // K-steps issued (block-wide numbering)
         int g = 0;     // H groups issued
         TcwCursor cur;
-        int occ = -1;  // captures met so far (strip slot occ & 1)
+        int occ = -1;  // captures met so far
         int cap_now = -1;
         int st_cmax = 0;
         uint32_t a_hi0 = 0;
@@ -367,15 +374,16 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
                 cap_now = cur.idx;
                 ++occ;
                 if constexpr (kMulti) {
-                    if (!mbar_wait_bounded(smem_u32(&ctl.strip_ready[occ & 1]), (occ >> 1) & 1,
+                    if (!mbar_wait_bounded(smem_u32(&ctl.strip_ready[strip_slot(occ)]),
+                                           strip_use(occ) & 1,
                                            fault, kFaultStageFull, abort)) {
                         break;
                     }
                 }
                 const int zero_top = C * kB - src.capture(cur.idx).num_taps - 15;
                 st_cmax = zero_top < 0 ? 0 : zero_top / 16 + 1;
-                a_hi0 = (strip_hi(occ & 1) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
-                a_lo0 = (strip_lo(occ & 1) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+                a_hi0 = (strip_hi(strip_slot(occ)) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
+                a_lo0 = (strip_lo(strip_slot(occ)) >> 4) + static_cast<uint32_t>(16 * C) * 8u;
             }
             if (!mbar_wait_bounded(smem_u32(&ctl.xempty[k & 1]), ((k >> 1) & 1) ^ 1, fault,
                                    kFaultAccumEmpty, abort)) {
@@ -447,7 +455,7 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
                     src.locate(k + 1, next, tn);
                 }
                 if (!stop && (k + 1 == my_tiles || next.idx != cur.idx) && elect_one()) {
-                    mma_commit(smem_u32(&ctl.strip_free[occ & 1]));
+                    mma_commit(smem_u32(&ctl.strip_free[strip_slot(occ)]));
                 }
                 __syncwarp();
             }
@@ -692,30 +700,18 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
             long long t;
             src.locate(j, cur, t);
             const WinCapture& cap = src.capture(cur.idx);
-            if (cur.idx != cap_now) {
+            const bool new_cap = cur.idx != cap_now;
+            if (new_cap) {
                 cap_now = cur.idx;
                 ++occ;
                 if constexpr (kMulti) {
-                    // The capture's strip, into slot occ & 1 once the MMAs of the capture that
-                    // used it last (two captures back) are done. Each scan warp takes the
-                    // whole tap maximum and half of the strip.
-                    if (!mbar_wait_bounded(smem_u32(&ctl.strip_free[occ & 1]),
-                                           ((occ >> 1) & 1) ^ 1, fault, kFaultStageEmpty,
-                                           abort)) {
-                        break;
-                    }
+                    // The capture's tap scale (each scan warp takes the whole maximum); its
+                    // strip follows the scale of its first tile, below.
                     uint32_t m = 0;
                     for (int i = lane; i < cap.num_taps; i += 32) {
                         m = max(m, absbits(__ldg(cap.taps + i)));
                     }
                     eh = scale_exponent(__reduce_max_sync(0xFFFFFFFFu, m));
-                    build_strip<C>(strip_hi(occ & 1), strip_lo(occ & 1), cap.taps,
-                                   cap.num_taps, eh, stid, kScanWarps * 32);
-                    fence_proxy_async_smem();
-                    __syncwarp();
-                    if (lane == 0) {
-                        mbar_arrive(smem_u32(&ctl.strip_ready[occ & 1]));
-                    }
                 }
             }
             const int wb = j % wins;
@@ -787,6 +783,26 @@ __device__ __forceinline__ void tcw_pipeline(const Src& src, unsigned char* smem
                 ctl.ex[j % kScales] = min(scale_exponent(tmax), 127);
                 ctl.ehr[j % kScales] = eh;
                 mbar_arrive(smem_u32(&ctl.sready[j % kScales]));
+            }
+            if constexpr (kMulti) {
+                if (new_cap) {
+                    // The capture's strip, into its slot once the MMAs of the capture that used
+                    // the slot last are done; after the first tile's scale, so that the
+                    // producers convert that tile meanwhile. Each scan warp builds half.
+                    const int slot = strip_slot(occ);
+                    if (!mbar_wait_bounded(smem_u32(&ctl.strip_free[slot]),
+                                           (strip_use(occ) & 1) ^ 1, fault, kFaultStageEmpty,
+                                           abort)) {
+                        break;
+                    }
+                    build_strip<C>(strip_hi(slot), strip_lo(slot), cap.taps, cap.num_taps, eh,
+                                   stid, kScanWarps * 32);
+                    fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0) {
+                        mbar_arrive(smem_u32(&ctl.strip_ready[slot]));
+                    }
+                }
             }
         }
     }

@@ -170,3 +170,25 @@ def test_plan_plain_tiles_with_tap_counts_changing_between_captures(impl: str) -
     # auto puts 2 to 385 taps in the plan's resident-window phase, one tap on a plain tile.
     expect = len(ks) if impl == "plain" else sum(1 for k in ks if k < 2)
     assert kinds["plain"] == expect
+
+
+@pytest.mark.parametrize("span", ["short", "long"])
+def test_plan_window_phases_switch_captures_within_blocks(span: str) -> None:
+    # Every reach-back of the resident-window phase (C = 1: 2 to 129 taps, 2: 130 to 257,
+    # 3: 258 to 385), with captures short enough that each block's range crosses several of
+    # them (480 captures of one to three tiles over the blocks): the strip is rebuilt at every
+    # switch, into the other of two slots (C = 1) or into the only one once the previous
+    # capture's MMAs are done (C = 2, 3). Lengths around tile edges (6144 outputs per tile)
+    # and partial last blocks; "long" puts several tiles of each capture in a block.
+    ks = [2, 64, 129, 130, 200, 257, 258, 300, 385, 31, 255, 384, 129, 258, 2, 386]
+    if span == "short":
+        spec = [(6144 * (1 + i % 3) + 37 * (i % 50) + 1, k) for i, k in enumerate(ks * 30)]
+    else:
+        spec = [(6144 * (20 + 7 * i) - 5 * i, k) for i, k in enumerate(ks)]
+    caps = rand_caps(spec, seed=58)
+    dev = to_dev(caps)
+    with rfx.FirBatchPlan(dev, "auto") as plan:
+        assert plan.info()["launches"] == 1
+        plan.run()
+        kinds = check(caps, dev, "auto")
+    assert kinds["plain"] == 0 and kinds["tc_split"] == len(spec)
