@@ -14,7 +14,11 @@ samples, each with its own 31 .. 1025 taps). --workload W reports W alone as the
 
 Timing: per workload, every implementation (arm) gets W untimed steps, then R rounds; a round
 times exactly K steps of each arm in turn, between a barrier + device synchronize on both
-sides, with CUDA events on the launching stream (max over ranks). Each arm's figure is the
+sides, with CUDA events on the launching stream (max over ranks). The K steps of a round (each
+the library's launch call for that arm, alternating buffer sets) are captured once, before the
+timed rounds, into one CUDA graph that each round replays (every arm alike): the device
+timeline holds the steps' kernels back to back, as a captured launch loop in an application,
+not the host side of each call. Each arm's figure is the
 median over the rounds; R >= 5 and large enough that the headline arm runs >= 0.5 s in total
 (so the clock sampler sees the load). Two input/output buffer pairs alternate, so each step
 touches more than the 129 MB L2 and nothing is served from L2 across steps. `value` = all
@@ -238,9 +242,47 @@ def peaks() -> dict:
             "source": "fallback"}
 
 
-class Arm:
+def capture_graph(enqueue):
+    """A CUDA graph holding what `enqueue(stream)` puts on a stream (run once on a side stream
+    first, outside the capture)."""
+    import torch
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        enqueue(side)
+    side.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+        enqueue(side)
+    torch.cuda.synchronize()
+    return graph
+
+
+class RoundGraphs:
+    """The K steps of a timed round as one CUDA graph, replayed once per round (captured before
+    the timed rounds, one per parity of the round's first step): consecutive launches inside a
+    graph start without a host submission between them, as a launch loop captured in a graph
+    runs in an application."""
+
+    def prepare(self, steps: int) -> None:
+        self.round_graphs = {}
+        for parity in (0, 1) if steps % 2 else (0,):
+            self.round_graphs[parity] = capture_graph(
+                lambda st, p=parity: [self.enqueue_step(p + i, st) for i in range(steps)])
+        self.round_steps = steps
+
+    def run_round(self, first: int, steps: int) -> None:
+        assert steps == self.round_steps
+        self.round_graphs[first % 2 if steps % 2 else 0].replay()
+
+
+class Arm(RoundGraphs):
     """One implementation on one single-capture workload: its device buffers and one step's
-    launch."""
+    launch, replayed from a CUDA graph (one per buffer set, each captured once after a warm-up
+    run), as the batch arm's step: a step's device work is the launch's kernels alone, and the
+    host side of a launch (argument checks, tensor-map encoding) stays off the device timeline.
+    The same for every arm."""
 
     def __init__(self, rfx, w, impl: str, device) -> None:
         import torch
@@ -264,12 +306,18 @@ class Arm:
             self.launches_per_step = 1
             self.kernel = rfx.fir_impl_used(impl, w.taps.size, n)
         self.dtype = "f16x3->f32" if self.kernel == "tc_split" else "f32"
+        self.graphs = [capture_graph(lambda st, i=i: self.enqueue_step(i, st)) for i in range(2)]
+
+    def enqueue_step(self, i: int, stream) -> None:
+        """One step on buffer set i % 2, through the library's launch call on `stream`."""
+        if self.w.channels:
+            self.plan.launch(self.xs[i % 2], self.h, self.outs[i % 2], stream=stream)
+        else:
+            self.rfx.fir_launch(self.impl, self.xs[i % 2], self.h, self.outs[i % 2],
+                                stream=stream)
 
     def launch(self, i: int) -> None:
-        if self.w.channels:
-            self.plan.launch(self.xs[i % 2], self.h, self.outs[i % 2])
-        else:
-            self.rfx.fir_launch(self.impl, self.xs[i % 2], self.h, self.outs[i % 2])
+        self.graphs[i % 2].replay()
 
     def error(self, ref) -> dict:
         """This arm's whole output against the float64 oracle's (`ref`): the normwise error
@@ -293,16 +341,18 @@ class Arm:
         return out
 
     def release(self) -> None:
+        self.graphs = self.round_graphs = None
         self.xs = self.outs = None
         if self.w.channels:
             self.plan.close()
 
 
-class BatchArm:
+class BatchArm(RoundGraphs):
     """The batched workload: every capture with its own taps, device-resident. auto and tc_split:
     one step is one run of a batch plan (rfx_fir_batch_plan_create, made once before timing):
-    ONE persistent launch over all captures, replayed from a CUDA graph captured once. plain:
-    one rfx_fir_batch_launch that runs one launch per capture, as the project runs a batch."""
+    ONE persistent launch over all captures. plain: one rfx_fir_batch_launch that runs one
+    launch per capture, as the project runs a batch. Either step is replayed from a CUDA graph
+    captured once."""
 
     def __init__(self, rfx, w, impl: str, device) -> None:
         import torch
@@ -337,28 +387,25 @@ class BatchArm:
                 self.arr[i] = rfx.FirCapture(xd.data_ptr(), yd.data_ptr(), hd.data_ptr(),
                                              xd.numel(), hd.numel(), 0)
             self.launches_per_step = sum(1 for x, _ in w.captures if x.size)
-            return
-        self.plan = rfx.FirBatchPlan(self.caps, impl)
-        info = self.plan.info()
-        self.launches_per_step = info["launches"]
-        self.plan_info = info
+        else:
+            self.plan = rfx.FirBatchPlan(self.caps, impl)
+            info = self.plan.info()
+            self.launches_per_step = info["launches"]
+            self.plan_info = info
         # One step captured into a CUDA graph (after a warm-up run), replayed per step.
-        side = torch.cuda.Stream()
-        side.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(side):
-            self.plan.run(side)
-        side.synchronize()
-        self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph, stream=side, capture_error_mode="relaxed"):
-            self.plan.run(side)
-        torch.cuda.synchronize()
+        self.graph = capture_graph(lambda st: self.enqueue_step(0, st))
 
-    def launch(self, i: int) -> None:
-        if self.graph is not None:
-            self.graph.replay()
+    def enqueue_step(self, i: int, stream) -> None:
+        """One step through the library's call on `stream` (the same buffers every step)."""
+        if self.plan is not None:
+            self.plan.run(stream)
         else:
             self.rfx._check(self.rfx.load().rfx_fir_batch_launch(
-                self.rfx.parse_fir_impl(self.impl), self.arr, len(self.caps), None))
+                self.rfx.parse_fir_impl(self.impl), self.arr, len(self.caps),
+                self.rfx._stream_ptr(stream)))
+
+    def launch(self, i: int) -> None:
+        self.graph.replay()
 
     def error(self, ref=None) -> dict:
         """Every capture's whole output against the float64 oracle: the largest normwise error
@@ -390,7 +437,7 @@ class BatchArm:
     def release(self) -> None:
         if self.plan is not None:
             self.plan.close()
-        self.caps = self.X = self.Y = self.graph = self.plan = None
+        self.caps = self.X = self.Y = self.graph = self.plan = self.round_graphs = None
 
 
 def chan_launches(channels: int, impl: str) -> int:
@@ -415,9 +462,10 @@ def make_arm(rfx, w, impl: str, device):
     return BatchArm(rfx, w, impl, device) if w.captures else Arm(rfx, w, impl, device)
 
 
-def time_round(launch, steps: int, dist, device, first: int = 0) -> float:
-    """Seconds for exactly `steps` launches: barrier + synchronize on both sides, CUDA events on
-    the current (launching) stream, max over ranks."""
+def time_round(launch, steps: int, dist, device, first: int = 0, run_round=None) -> float:
+    """Seconds for exactly `steps` steps (`launch(i)` per step, or `run_round(first, steps)` for
+    all of them): barrier + synchronize on both sides, CUDA events on the current (launching)
+    stream, max over ranks."""
     import torch
 
     torch.cuda.synchronize()
@@ -426,8 +474,11 @@ def time_round(launch, steps: int, dist, device, first: int = 0) -> float:
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
     start.record()
-    for i in range(steps):
-        launch(first + i)
+    if run_round is not None:
+        run_round(first, steps)
+    else:
+        for i in range(steps):
+            launch(first + i)
     stop.record()
     torch.cuda.synchronize()
     barrier(dist, device)
@@ -459,15 +510,17 @@ def measure_arms(rfx, w, impls, args, dist, device, sampler=None):
     for arm in arms.values():
         for i in range(args.warmup):
             arm.launch(i)
+        arm.prepare(args.steps)
     first = next(iter(arms))
-    rounds = rounds_for(time_round(arms[first].launch, args.steps, dist, device))
+    rounds = rounds_for(time_round(arms[first].launch, args.steps, dist, device,
+                                   run_round=arms[first].run_round))
     seconds = {impl: [] for impl in arms}
     ctx = sampler if sampler is not None else _Null()
     with ctx:
         for r in range(rounds):
             for impl, arm in arms.items():
                 seconds[impl].append(time_round(arm.launch, args.steps, dist, device,
-                                                first=r * args.steps))
+                                                first=r * args.steps, run_round=arm.run_round))
     world = dist.get_world_size() if dist is not None else 1
     out = {}
     for impl, arm in arms.items():
@@ -868,8 +921,8 @@ def roofline_of(w, res: dict, n: int, pk: dict) -> dict:
     r["peak_source"] = pk["source"] + " (MEASURED_PEAKS.json burst figures)" \
         if pk["source"] == "measured" else pk["source"]
     r["timing"] = (f"CUDA events over the timed rounds: median of {res['rounds']} rounds of "
-                   f"{res['steps_per_round']} steps, {res['launches_per_step']} launch(es) per "
-                   f"step")
+                   f"{res['steps_per_round']} steps (one CUDA-graph replay per round), "
+                   f"{res['launches_per_step']} launch(es) per step")
     traffic = NCU_TRAFFIC_BYTES.get((w.name, kernel))
     if traffic is not None:
         r["traffic"] = traffic
