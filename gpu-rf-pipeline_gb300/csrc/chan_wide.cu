@@ -102,7 +102,7 @@ __device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, ui
                  : "memory");
 }
 
-// Lane 0 waits, the warp synchronizes behind it, and every lane gets lane 0's verdict: the warp
+// Lane 0 waits, the warp synchronizes behind it, and every lane gets lane 0's result: the warp
 // never splits at a later warp-wide step.
 __device__ __forceinline__ bool lead_wait(uint32_t bar, uint32_t parity, unsigned int* fault,
                                           unsigned int code, volatile int* abort)

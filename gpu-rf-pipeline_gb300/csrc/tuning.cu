@@ -278,10 +278,11 @@ int tuned_fir_batch_launch_impl(int num_taps, long long n)
 // that one takes (its window phase up to 385 taps, its long-filter phase beyond), at any length:
 // a plan launches once for the whole batch, so a short capture is no reason for the plain tiles.
 // Measured on the 256-capture workload (batch plans of each tap count alone): a window tile of
-// 6144 outputs costs 3.2-3.8 SM-us at 31-127 taps, 4.6 at 255, a long-filter tile of 12288
-// outputs ~20-25 SM-us at 511-1025, against 2304-output plain tiles of 1.7 SM-us at 31 taps and
-// 12.6-24.7 at 511-1025; the whole batch took 1.27 ms this way against 1.32 ms with the short
-// captures of long filters on the plain tiles.
+// 6144 outputs costs 2.9-3.6 SM-us at 31-127 taps, 4.1 at 255, a long-filter tile of 12288
+// outputs 16.5-18.6 SM-us at 511-1025, against 2304-output plain tiles of 1.7 SM-us at 31 taps
+// and 12.6-24.7 at 511-1025 (per output the tensor-core tiles cost less at every tap count);
+// putting the short captures of long filters on the plain tiles instead made the whole batch
+// 4 % slower.
 int tuned_fir_batch_impl(int num_taps, long long n)
 {
     (void)n;

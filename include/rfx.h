@@ -346,9 +346,11 @@ int rfx_magnitude_host(const void* x_iq, int64_t num_samples, float* mag, rfx_be
 /* ---- tuning --------------------------------------------------------------------------- */
 
 /* The `auto` implementations consult in-process tables filled by the calls below, and apply
- * a built-in rule where an entry is missing (FIR: the tensor core from 160 taps and 2^16
- * samples; channelizer: the tensor core at 64 channels). The batch's auto form places each
- * capture by the FIR table. If the environment variable RFX_TUNE_FILE names a file saved by
+ * a built-in rule where an entry is missing (FIR: the tensor core from 32 taps and 2^16
+ * samples; channelizer: the tensor core at 64 channels). A batch plan's auto form puts every
+ * capture of 2 taps or more on a tensor-core phase; rfx_fir_batch_launch's auto form follows
+ * the FIR table beyond 385 taps and takes the tensor core from 160 taps (and 2^16 samples)
+ * otherwise. If the environment variable RFX_TUNE_FILE names a file saved by
  * rfx_autotune_save, it is loaded before the first lookup (entries of other GPUs or drivers
  * are skipped). The tuner is this library's own: the project picks kernels by name only
  * (src/main.cpp:156-167), and its plan object for a channelizer is a cuFFT plan. */
