@@ -39,6 +39,14 @@ def test_binding_declares_nothing_the_header_does_not() -> None:
     assert set(rfx.SIGNATURES) <= set(declared_functions())
 
 
+def test_integration_guide_lists_every_entry_point() -> None:
+    # The table of INTEGRATION.md maps each C entry point to the project interface it replaces
+    # (or says it has none): a function the header adds is listed there too.
+    guide = (ROOT / "INTEGRATION.md").read_text()
+    missing = [name for name in declared_functions() if f"{name}" not in guide]
+    assert not missing, missing
+
+
 def test_library_targets_sm_103a(lib) -> None:
     assert b"sm_103a" in lib.rfx_version()
 
