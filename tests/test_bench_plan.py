@@ -54,3 +54,31 @@ def test_rounds_cover_half_a_second_and_at_least_five(bench) -> None:
     assert bench.rounds_for(1.0) == bench.MIN_ROUNDS
     assert bench.rounds_for(0.0028) == 179          # 20 steps of 0.14 ms
     assert bench.rounds_for(1e-9) == bench.MAX_ROUNDS
+
+
+@pytest.mark.parametrize("steps", [1, 4, 5, 20])
+def test_round_graphs_hold_the_rounds_steps(bench, monkeypatch, steps: int) -> None:
+    # A timed round replays one graph holding its `steps` launches; the round starting at step
+    # `first` must run steps first .. first + steps - 1, i.e. the buffer sets (i % 2) of those
+    # steps. The capture is replaced by a recorder (no GPU): each "graph" remembers the step
+    # indices enqueued into it, modulo 2.
+    class Graph:
+        def __init__(self, enqueue):
+            self.steps = []
+            enqueue(self)          # the stream argument is the graph itself here
+
+        def replay(self):
+            replayed.append(list(self.steps))
+
+    class Arm(bench.RoundGraphs):
+        def enqueue_step(self, i, stream):
+            stream.steps.append(i % 2)
+
+    replayed = []
+    monkeypatch.setattr(bench, "capture_graph", Graph)
+    arm = Arm()
+    arm.prepare(steps)
+    for r in range(4):
+        first = r * steps
+        arm.run_round(first, steps)
+        assert replayed[-1] == [(first + i) % 2 for i in range(steps)], (r, steps)
